@@ -1,0 +1,67 @@
+/*
+ * calling.cuh - argument block of the fused consensus-calling kernels.
+ */
+#ifndef GSNP_CALLING_CUH
+#define GSNP_CALLING_CUH
+
+#include <stdint.h>
+
+#include "gsnp_device.cuh"
+
+namespace gsnp {
+
+constexpr int kTile = 128;        /* sites per tile (divides the window) */
+constexpr int kMaxStagedReads = 2048;
+constexpr int kNumBins = 4;       /* record slots 32 / 64 / 128 / 256 */
+
+/* per-window calling mode, decided by the host replay of the reference's
+ * window loop (cpp/call_genotype.cc:422-669) */
+enum WindowFlags : uint8_t {
+    kWinKeepCounts = 1,   /* a later gap window shows this window's host counts */
+    kWinKeepLik = 2,      /* a later window reuses this window's likelihood */
+    kWinExternalLik = 4,  /* likelihood comes from another window (or zeros) */
+};
+
+struct CallArgs {
+    /* deposited reads, sorted by start position (file order within a start) */
+    const int32_t* pos;
+    const int32_t* lenhit;       /* (read_len << 16) | hit */
+    const uint8_t* strand;       /* '+' or '-' */
+    const uint16_t* bq;          /* [n_reads][L]: base char | quality char << 8 */
+    int64_t n_reads;
+    int L;                       /* -L: read pitch and coordinate bound */
+    /* reference */
+    const uint8_t* ori;          /* 4-bit site code per position */
+    int64_t chr_len;
+    const DbSnpEntry* snp;       /* sorted by position */
+    int64_t n_snp;
+    /* tables */
+    const double* lik64;         /* [qa_rows][L][4][10] log10 genotype terms */
+    const float* lik32;          /* same, rounded to FP32 */
+    int qa_rows;
+    const uint8_t* qadj;         /* [tmax][gmax][65] adjusted quality */
+    int tmax, gmax;
+    const double* p_prior;       /* [8][16] */
+    const double* log_prior;     /* [8][16] correctly rounded log10 of p_prior */
+    const double* p_rank;        /* 64 x 64 x 2048 */
+    /* parameters */
+    int qmin;                    /* as a signed char */
+    int q_max_min;
+    int rank_sum, monoploid, refine;
+    double het_val, het_unval, althom_val, althom_unval;
+    int precision;               /* 0: FP64 sums, 1: FP32 compensated sums + FP64 fixup */
+    /* windows */
+    const uint8_t* win_flags;    /* per window */
+    const int32_t* win_lik_src;  /* per window: window whose likelihood is used (-1: zeros) */
+    /* outputs */
+    SiteCall* out;               /* [chr_len] */
+    SiteCounts* counts;          /* [chr_len] or null */
+    double* lik_keep;            /* [chr_len][10] or null */
+    float* lik_err;              /* optional: max |FP32 - FP64| per tile (diagnostics) */
+    unsigned long long* stats;   /* [4]: fixup sites, normal-path sites, ... */
+    int* error;                  /* nonzero on a capacity overflow */
+};
+
+}  // namespace gsnp
+
+#endif

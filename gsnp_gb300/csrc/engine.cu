@@ -1,0 +1,568 @@
+/*
+ * engine.cu - the C ABI of include/gsnp_gb300.h: context, tables, resident
+ * chromosome state, calibration and the whole-chromosome calling pass.
+ *
+ * Device memory layout of one chromosome (sized for HBM, all resident):
+ *   site codes      1 B/site      reference base, N and dbSNP bits
+ *   reads           2*L + 9 B/read after the gather: packed base|quality
+ *                   pairs [n][L] (uint16), start, len<<16|hit, strand
+ *   SiteCall        32 B/site     the caller's output
+ *   side buffers    40 B/site of SiteCounts and 80 B/site of likelihoods, only
+ *                   for windows that a later window refers to
+ * The raw alignment arrays are uploaded once per call and gathered on the
+ * device into the deposited, packed layout the calling kernel reads.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "calling.cuh"
+#include "gsnp_gb300.h"
+#include "plan.h"
+#include "tables.h"
+
+namespace gsnp {
+
+cudaError_t launch_calling(const CallArgs& a, int pass, int64_t n_tiles, int* d_bin_count, int32_t* d_bin_tiles,
+                           int* h_bin_count, cudaStream_t stream);
+
+/* ---- device helpers ---- */
+
+__global__ void gather_reads_kernel(int64_t n, const int64_t* __restrict__ idx, const uint8_t* __restrict__ seq,
+                                    const uint8_t* __restrict__ qual, int pitch, int L, uint16_t* __restrict__ bq,
+                                    int* __restrict__ error) {
+    /* one warp per read; bases go through the 2-bit round trip of the
+     * reference's pass-1 store (upper case; anything else is rejected) */
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int64_t src = idx[warp];
+    const uint8_t* s = seq + src * pitch;
+    const uint8_t* q = qual + src * pitch;
+    uint16_t* d = bq + warp * L;
+    for (int c = lane; c < L; c += 32) {
+        uint8_t b = 'A', qq = 0;
+        if (c < pitch) {
+            b = s[c];
+            qq = q[c];
+        }
+        d[c] = (uint16_t)b | ((uint16_t)qq << 8);
+    }
+}
+
+__global__ void normalise_bases_kernel(int64_t n, const int32_t* __restrict__ len, uint16_t* __restrict__ bq, int L,
+                                       int* __restrict__ error) {
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int rl = len[warp];
+    uint16_t* d = bq + warp * L;
+    for (int c = lane; c < L; c += 32) {
+        const uint16_t v = d[c];
+        uint8_t b = (uint8_t)(v & 0xff);
+        if (c >= rl) {
+            b = 'A';
+        } else {
+            switch (b) {
+                case 'A': case 'a': b = 'A'; break;
+                case 'C': case 'c': b = 'C'; break;
+                case 'G': case 'g': b = 'G'; break;
+                case 'T': case 't': b = 'T'; break;
+                default: atomicExch(error, 2); b = 'A';
+            }
+        }
+        d[c] = (uint16_t)b | (v & 0xff00);
+    }
+}
+
+/* pass-1 calibration histogram (cpp/matrix.cc:58-118): unique reads, non-N
+ * base, reference neither N nor dbSNP, whole read inside the chromosome.
+ * Counts land in [q_char - q_min][cycle][ref][obs]; identical bins within a
+ * warp are merged before the atomic. */
+__global__ void calib_count_kernel(int64_t n, const int32_t* __restrict__ pos, const int32_t* __restrict__ len,
+                                   const int32_t* __restrict__ hit, const uint8_t* __restrict__ strand,
+                                   const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual, int pitch,
+                                   const uint8_t* __restrict__ codes, int64_t chr_len, int qmin, int qmax, int L,
+                                   unsigned long long* __restrict__ counts) {
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const int64_t p = pos[warp];
+    const int rl = len[warp];
+    if (p < 0 || p + rl >= chr_len || hit[warp] != 1) return;
+    const bool minus = strand[warp] != '+';
+    for (int c0 = 0; c0 < rl; c0 += 32) {
+        const int c = c0 + lane;
+        int bin = -1;
+        if (c < rl) {
+            const signed char b = (signed char)seq[warp * pitch + c];
+            const signed char qc = (signed char)qual[warp * pitch + c];
+            const int ref = codes[p + c];
+            const int cyc = minus ? rl - 1 - c : c;
+            if (b != 'N' && (ref & 12) == 0 && qc >= qmin && qc <= qmax && cyc < L)
+                bin = (((qc - qmin) * L + cyc) << 4) | ((ref & 3) << 2) | ((b >> 1) & 3);
+        }
+        const unsigned active = __ballot_sync(0xffffffffu, bin >= 0);
+        if (bin >= 0) {
+            const unsigned peers = __match_any_sync(active, bin);
+            if ((int)(__ffs(peers) - 1) == lane) atomicAdd(counts + bin, (unsigned long long)__popc(peers));
+        }
+    }
+}
+
+}  // namespace gsnp
+
+using namespace gsnp;
+
+struct gsnp_context {
+    int device = 0;
+    std::string error;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    gsnp_params params{};
+    bool have_tables = false;
+    HostTables tables;
+    /* device tables */
+    double* d_lik64 = nullptr;
+    float* d_lik32 = nullptr;
+    uint8_t* d_qadj = nullptr;
+    double* d_p_prior = nullptr;
+    double* d_log_prior = nullptr;
+    double* d_p_rank = nullptr;
+    /* reference */
+    int64_t chr_len = 0;
+    std::vector<uint8_t> h_codes;
+    uint8_t* d_codes = nullptr;
+    DbSnpEntry* d_snp = nullptr;
+    int64_t n_snp = 0;
+    /* resident reads (deposited, packed) */
+    int64_t n_dep = 0;
+    int64_t cap_dep = 0;
+    int32_t* d_pos = nullptr;
+    int32_t* d_lenhit = nullptr;
+    int32_t* d_len = nullptr;
+    uint8_t* d_strand = nullptr;
+    uint16_t* d_bq = nullptr;
+    /* window plan */
+    WindowPlan plan;
+    uint8_t* d_win_flags = nullptr;
+    int32_t* d_win_lik_src = nullptr;
+    int64_t n_win_alloc = 0;
+    /* outputs */
+    SiteCall* d_out = nullptr;
+    SiteCounts* d_counts = nullptr;
+    double* d_lik_keep = nullptr;
+    int64_t out_sites = 0;
+    bool have_counts = false, have_lik_keep = false;
+    /* scratch */
+    int* d_error = nullptr;
+    unsigned long long* d_stats = nullptr;
+    int* d_bin_count = nullptr;
+    int32_t* d_bin_tiles = nullptr;
+    int64_t bin_tiles_cap = 0;
+    int h_bin_count[kNumBins] = {0, 0, 0, 0};
+    bool called = false;
+    uint64_t stats[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(gsnp_context* c, int code, const std::string& msg) {
+    if (c) c->error = msg;
+    return code;
+}
+
+int cuda_fail(gsnp_context* c, cudaError_t e, const char* what) {
+    return fail(c, GSNP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)
+
+template <class T>
+cudaError_t dev_alloc(T** p, size_t count) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+void free_all(gsnp_context* c) {
+    void* ptrs[] = {c->d_lik64, c->d_lik32, c->d_qadj, c->d_p_prior, c->d_log_prior, c->d_p_rank,
+                    c->d_codes, c->d_snp, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq,
+                    c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts, c->d_lik_keep,
+                    c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+CallArgs make_args(gsnp_context* c) {
+    CallArgs a;
+    memset(&a, 0, sizeof(a));
+    a.pos = c->d_pos;
+    a.lenhit = c->d_lenhit;
+    a.strand = c->d_strand;
+    a.bq = c->d_bq;
+    a.n_reads = c->n_dep;
+    a.L = c->params.read_length;
+    a.ori = c->d_codes;
+    a.chr_len = c->chr_len;
+    a.snp = c->d_snp;
+    a.n_snp = c->n_snp;
+    a.lik64 = c->d_lik64;
+    a.lik32 = c->d_lik32;
+    a.qa_rows = c->tables.qa_rows;
+    a.qadj = c->d_qadj;
+    a.tmax = c->tables.tmax;
+    a.gmax = c->tables.gmax;
+    a.p_prior = c->d_p_prior;
+    a.log_prior = c->d_log_prior;
+    a.p_rank = c->d_p_rank;
+    a.qmin = c->params.q_min;
+    a.q_max_min = (int)(signed char)(c->params.q_max - c->params.q_min);
+    a.rank_sum = c->params.rank_sum;
+    a.monoploid = c->params.monoploid;
+    a.refine = c->params.refine;
+    a.het_val = c->params.het_val;
+    a.het_unval = c->params.het_unval;
+    a.althom_val = c->params.althom_val;
+    a.althom_unval = c->params.althom_unval;
+    a.precision = c->params.precision;
+    a.win_flags = c->d_win_flags;
+    a.win_lik_src = c->d_win_lik_src;
+    a.out = c->d_out;
+    a.counts = c->d_counts;
+    a.lik_keep = c->d_lik_keep;
+    a.stats = c->d_stats;
+    a.error = c->d_error;
+    return a;
+}
+
+int run_calling(gsnp_context* c) {
+    const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    if (n_tiles > c->bin_tiles_cap) {
+        CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * kNumBins), "cudaMalloc bins");
+        c->bin_tiles_cap = n_tiles;
+    }
+    CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
+    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4, c->stream), "memset");
+    const CallArgs a = make_args(c);
+    bool any_external = false;
+    for (int64_t w = 0; w < c->plan.n_windows; ++w) any_external |= (c->plan.flags[w] & kWinExternalLik) != 0;
+    for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
+        CK(launch_calling(a, pass, n_tiles, c->d_bin_count, c->d_bin_tiles, c->h_bin_count, c->stream),
+           "calling kernels");
+    }
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
+    CK(cudaMemcpyAsync(c->stats, c->d_stats, sizeof(c->stats), cudaMemcpyDeviceToHost, c->stream), "stats");
+    CK(cudaStreamSynchronize(c->stream), "calling");
+    if (err) return fail(c, GSNP_ERR_CAPACITY, "a site's count_all exceeds 65535");
+    c->stats[0] = (uint64_t)c->chr_len;
+    c->called = true;
+    return GSNP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gsnp_context_create(int device, gsnp_context** out) {
+    if (!out) return GSNP_ERR_ARG;
+    *out = nullptr;
+    gsnp_context* c = new gsnp_context();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_error, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_stats, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bin_count, sizeof(int) * kNumBins);
+    if (e != cudaSuccess) {
+        free_all(c);
+        delete c;
+        return GSNP_ERR_CUDA;
+    }
+    c->own_stream = true;
+    *out = c;
+    return GSNP_OK;
+}
+
+void gsnp_context_destroy(gsnp_context* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* gsnp_context_error(const gsnp_context* c) { return c ? c->error.c_str() : "no context"; }
+
+int gsnp_set_stream(gsnp_context* c, void* stream) {
+    if (!c) return GSNP_ERR_ARG;
+    if (c->own_stream && c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+    return GSNP_OK;
+}
+
+int gsnp_load_tables(gsnp_context* c, const gsnp_params* p, const double* p_matrix, const double* p_prior,
+                     const double* p_rank) {
+    if (!c || !p || !p_matrix || !p_prior || !p_rank) return fail(c, GSNP_ERR_ARG, "null argument");
+    if (p->read_length <= 0 || p->read_length > 255) return fail(c, GSNP_ERR_ARG, "read_length must be 1..255");
+    cudaSetDevice(c->device);
+    c->params = *p;
+    std::string err;
+    if (build_tables(*p, p_matrix, p_prior, &c->tables, &err) != 0) return fail(c, GSNP_ERR_ARG, err);
+    const HostTables& t = c->tables;
+    CK(dev_alloc(&c->d_lik64, t.lik64.size()), "cudaMalloc");
+    CK(dev_alloc(&c->d_lik32, t.lik32.size()), "cudaMalloc");
+    CK(dev_alloc(&c->d_qadj, t.qadj.size()), "cudaMalloc");
+    CK(dev_alloc(&c->d_p_prior, 128), "cudaMalloc");
+    CK(dev_alloc(&c->d_log_prior, 128), "cudaMalloc");
+    CK(dev_alloc(&c->d_p_rank, 64UL * 64UL * 2048UL), "cudaMalloc");
+    CK(cudaMemcpy(c->d_lik64, t.lik64.data(), t.lik64.size() * 8, cudaMemcpyHostToDevice), "upload");
+    CK(cudaMemcpy(c->d_lik32, t.lik32.data(), t.lik32.size() * 4, cudaMemcpyHostToDevice), "upload");
+    CK(cudaMemcpy(c->d_qadj, t.qadj.data(), t.qadj.size(), cudaMemcpyHostToDevice), "upload");
+    CK(cudaMemcpy(c->d_p_prior, p_prior, 128 * 8, cudaMemcpyHostToDevice), "upload");
+    CK(cudaMemcpy(c->d_log_prior, t.log_prior.data(), 128 * 8, cudaMemcpyHostToDevice), "upload");
+    CK(cudaMemcpy(c->d_p_rank, p_rank, 64UL * 64UL * 2048UL * 8, cudaMemcpyHostToDevice), "upload");
+    c->have_tables = true;
+    return GSNP_OK;
+}
+
+int gsnp_load_reference(gsnp_context* c, const uint8_t* codes, int64_t length, const gsnp_snp* snp,
+                        int64_t n_snp) {
+    if (!c || !codes || length <= 0 || (n_snp > 0 && !snp)) return fail(c, GSNP_ERR_ARG, "bad reference");
+    if (length > 0x7fffffffLL) return fail(c, GSNP_ERR_CAPACITY, "chromosome longer than 2^31-1");
+    cudaSetDevice(c->device);
+    c->chr_len = length;
+    c->h_codes.assign(codes, codes + length);
+    CK(dev_alloc(&c->d_codes, (size_t)length), "cudaMalloc codes");
+    CK(cudaMemcpy(c->d_codes, codes, (size_t)length, cudaMemcpyHostToDevice), "upload codes");
+    static_assert(sizeof(gsnp_snp) == sizeof(DbSnpEntry), "dbSNP row layout");
+    c->n_snp = n_snp;
+    CK(dev_alloc(&c->d_snp, (size_t)std::max<int64_t>(n_snp, 1)), "cudaMalloc dbsnp");
+    if (n_snp > 0) CK(cudaMemcpy(c->d_snp, snp, sizeof(gsnp_snp) * n_snp, cudaMemcpyHostToDevice), "upload dbsnp");
+    CK(dev_alloc(&c->d_out, (size_t)length), "cudaMalloc calls");
+    c->out_sites = length;
+    c->called = false;
+    return GSNP_OK;
+}
+
+int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
+    if (!c || !r || r->n < 0 || (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
+        return fail(c, GSNP_ERR_ARG, "null read arrays");
+    if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
+    cudaSetDevice(c->device);
+    const int L = c->params.read_length;
+    for (int64_t i = 0; i < r->n; ++i)
+        if (r->len[i] < 0 || r->len[i] > L || r->len[i] > r->pitch)
+            return fail(c, GSNP_ERR_INPUT, "alignment " + std::to_string(i) + " is longer than -L");
+    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
+    std::string err;
+    const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, &c->plan, &err);
+    if (rc != 0) return fail(c, rc, err);
+    const WindowPlan& P = c->plan;
+    const int64_t nd = (int64_t)P.deposited.size();
+
+    /* window tables */
+    if (P.n_windows > c->n_win_alloc) {
+        CK(dev_alloc(&c->d_win_flags, (size_t)P.n_windows), "cudaMalloc");
+        CK(dev_alloc(&c->d_win_lik_src, (size_t)P.n_windows), "cudaMalloc");
+        c->n_win_alloc = P.n_windows;
+    }
+    CK(cudaMemcpyAsync(c->d_win_flags, P.flags.data(), P.n_windows, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(c->d_win_lik_src, P.lik_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
+       "upload");
+    bool need_counts = false, need_lik = false;
+    for (int64_t w = 0; w < P.n_windows; ++w) {
+        need_counts |= (P.flags[w] & kWinKeepCounts) != 0;
+        need_lik |= (P.flags[w] & kWinKeepLik) != 0;
+    }
+    if (need_counts && !c->have_counts) {
+        CK(dev_alloc(&c->d_counts, (size_t)c->chr_len), "cudaMalloc counts");
+        c->have_counts = true;
+    }
+    if (need_lik && !c->have_lik_keep) {
+        CK(dev_alloc(&c->d_lik_keep, (size_t)c->chr_len * 10), "cudaMalloc likelihood");
+        c->have_lik_keep = true;
+    }
+
+    /* upload the alignments and gather the deposited ones */
+    if (nd > c->cap_dep) {
+        CK(dev_alloc(&c->d_pos, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_lenhit, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_len, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_strand, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_bq, (size_t)nd * L), "cudaMalloc reads");
+        c->cap_dep = nd;
+    }
+    c->n_dep = nd;
+    {
+        std::vector<int32_t> pos(nd), lenhit(nd), len(nd);
+        std::vector<uint8_t> strand(nd);
+        for (int64_t k = 0; k < nd; ++k) {
+            const int64_t i = P.deposited[k];
+            pos[k] = r->pos[i];
+            len[k] = r->len[i];
+            lenhit[k] = (int32_t)(((r->len[i] & 0xffff) << 16) | r->hit[i]);
+            strand[k] = r->strand[i];
+        }
+        CK(cudaMemcpyAsync(c->d_pos, pos.data(), nd * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_lenhit, lenhit.data(), nd * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_len, len.data(), nd * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_strand, strand.data(), nd, cudaMemcpyHostToDevice, c->stream), "upload");
+        /* raw base/quality rows of every alignment, then gather on the device */
+        const size_t raw = (size_t)r->n * r->pitch;
+        uint8_t *d_seq = nullptr, *d_qual = nullptr;
+        int64_t* d_idx = nullptr;
+        CK(cudaMalloc((void**)&d_seq, std::max<size_t>(raw, 1)), "cudaMalloc raw");
+        CK(cudaMalloc((void**)&d_qual, std::max<size_t>(raw, 1)), "cudaMalloc raw");
+        CK(cudaMalloc((void**)&d_idx, std::max<int64_t>(nd, 1) * 8), "cudaMalloc raw");
+        CK(cudaMemcpyAsync(d_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload seq");
+        CK(cudaMemcpyAsync(d_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload qual");
+        CK(cudaMemcpyAsync(d_idx, P.deposited.data(), nd * 8, cudaMemcpyHostToDevice, c->stream), "upload idx");
+        CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
+        if (nd > 0) {
+            const int64_t threads = nd * 32;
+            gather_reads_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+                nd, d_idx, d_seq, d_qual, r->pitch, L, c->d_bq, c->d_error);
+            normalise_bases_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(nd, c->d_len, c->d_bq, L,
+                                                                                               c->d_error);
+        }
+        int err2 = 0;
+        CK(cudaMemcpyAsync(&err2, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
+        CK(cudaStreamSynchronize(c->stream), "gather");
+        cudaFree(d_seq);
+        cudaFree(d_qual);
+        cudaFree(d_idx);
+        if (err2) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
+    }
+    return run_calling(c);
+}
+
+int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, double* pm) {
+    if (!c || !p || !r || !pm) return fail(c, GSNP_ERR_ARG, "null argument");
+    if (!c->d_codes) return fail(c, GSNP_ERR_STATE, "reference must be loaded first");
+    if (p->read_length <= 0 || p->read_length > 255) return fail(c, GSNP_ERR_ARG, "read_length must be 1..255");
+    if (p->q_max < p->q_min) return fail(c, GSNP_ERR_ARG, "q_max below q_min");
+    cudaSetDevice(c->device);
+    const int L = p->read_length;
+    const int nq = p->q_max - p->q_min + 1;
+    const size_t nbins = (size_t)nq * L * 16;
+    for (int64_t i = 0; i < r->n; ++i)
+        if (r->len[i] < 0 || r->len[i] > L || r->len[i] > r->pitch)
+            return fail(c, GSNP_ERR_INPUT, "alignment " + std::to_string(i) + " is longer than -L");
+    unsigned long long* d_counts = nullptr;
+    int32_t *d_pos = nullptr, *d_len = nullptr, *d_hit = nullptr;
+    uint8_t *d_strand = nullptr, *d_seq = nullptr, *d_qual = nullptr;
+    const size_t raw = (size_t)r->n * r->pitch;
+    CK(cudaMalloc((void**)&d_counts, nbins * 8), "cudaMalloc");
+    CK(cudaMalloc((void**)&d_pos, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
+    CK(cudaMalloc((void**)&d_len, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
+    CK(cudaMalloc((void**)&d_hit, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
+    CK(cudaMalloc((void**)&d_strand, std::max<int64_t>(r->n, 1)), "cudaMalloc");
+    CK(cudaMalloc((void**)&d_seq, std::max<size_t>(raw, 1)), "cudaMalloc");
+    CK(cudaMalloc((void**)&d_qual, std::max<size_t>(raw, 1)), "cudaMalloc");
+    CK(cudaMemsetAsync(d_counts, 0, nbins * 8, c->stream), "memset");
+    CK(cudaMemcpyAsync(d_pos, r->pos, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(d_len, r->len, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(d_hit, r->hit, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(d_strand, r->strand, r->n, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(d_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(d_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload");
+    if (r->n > 0) {
+        const int64_t threads = r->n * 32;
+        calib_count_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+            r->n, d_pos, d_len, d_hit, d_strand, d_seq, d_qual, r->pitch, c->d_codes, c->chr_len,
+            (int)(signed char)p->q_min, (int)(signed char)p->q_max, L, d_counts);
+    }
+    std::vector<unsigned long long> counts(nbins);
+    CK(cudaMemcpyAsync(counts.data(), d_counts, nbins * 8, cudaMemcpyDeviceToHost, c->stream), "download");
+    CK(cudaStreamSynchronize(c->stream), "calibration");
+    cudaFree(d_counts); cudaFree(d_pos); cudaFree(d_len); cudaFree(d_hit);
+    cudaFree(d_strand); cudaFree(d_seq); cudaFree(d_qual);
+    for (size_t i = 0; i < 256UL * 256UL * 16UL; ++i) pm[i] = 1.0;
+    calibration_fill(*p, counts.data(), pm);
+    return GSNP_OK;
+}
+
+int gsnp_prior_table(const gsnp_params* p, double* out) {
+    if (!p || !out) return GSNP_ERR_ARG;
+    prior_table(*p, p->transition_dominant, p->het_novel, p->althom_novel, out);
+    return GSNP_OK;
+}
+
+int gsnp_rank_table(double* out) {
+    if (!out) return GSNP_ERR_ARG;
+    rank_table(out);
+    return GSNP_OK;
+}
+
+int gsnp_recall_resident(gsnp_context* c) {
+    if (!c || !c->have_tables || c->plan.n_windows == 0) return fail(c, GSNP_ERR_STATE, "nothing resident");
+    cudaSetDevice(c->device);
+    return run_calling(c);
+}
+
+int gsnp_fetch_sites(gsnp_context* c, int64_t first, int64_t count, gsnp_site_call* out) {
+    if (!c || !out || first < 0 || count < 0 || first + count > c->out_sites) return fail(c, GSNP_ERR_ARG, "range");
+    if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
+    cudaSetDevice(c->device);
+    static_assert(sizeof(gsnp_site_call) == sizeof(SiteCall), "site call layout");
+    CK(cudaMemcpyAsync(out, c->d_out + first, (size_t)count * sizeof(SiteCall), cudaMemcpyDeviceToHost, c->stream),
+       "fetch");
+    CK(cudaStreamSynchronize(c->stream), "fetch");
+    return GSNP_OK;
+}
+
+int gsnp_get_stats(gsnp_context* c, uint64_t* s) {
+    if (!c || !s) return GSNP_ERR_ARG;
+    memcpy(s, c->stats, sizeof(c->stats));
+    return GSNP_OK;
+}
+
+}  // extern "C"
+
+/* cns text: cpp/call_genotype.cc:353-411.  Exposed to format.cpp. */
+namespace gsnp {
+int format_cns_host(const WindowPlan& plan, const std::vector<uint8_t>& codes, const SiteCall* calls,
+                    const SiteCounts* counts, const char* chr_name, std::string* out);
+}
+
+extern "C" int gsnp_format_cns(gsnp_context* c, const char* chr_name, char* buf, int64_t* size) {
+    if (!c || !chr_name || !size) return fail(c, GSNP_ERR_ARG, "null argument");
+    if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
+    cudaSetDevice(c->device);
+    std::vector<SiteCall> calls((size_t)c->chr_len);
+    CK(cudaMemcpy(calls.data(), c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost), "fetch");
+    std::vector<SiteCounts> counts;
+    if (c->have_counts) {
+        counts.resize((size_t)c->chr_len);
+        CK(cudaMemcpy(counts.data(), c->d_counts, (size_t)c->chr_len * sizeof(SiteCounts), cudaMemcpyDeviceToHost),
+           "fetch");
+    }
+    std::string text;
+    format_cns_host(c->plan, c->h_codes, calls.data(), c->have_counts ? counts.data() : nullptr, chr_name, &text);
+    if (!buf) {
+        *size = (int64_t)text.size();
+        return GSNP_OK;
+    }
+    const int64_t n = std::min<int64_t>(*size, (int64_t)text.size());
+    memcpy(buf, text.data(), (size_t)n);
+    *size = n;
+    return GSNP_OK;
+}

@@ -1,0 +1,155 @@
+/*
+ * gsnp_gb300.h - C ABI of the GB300 consensus caller.
+ *
+ * Plain C types only: pointers, sizes and status codes.  Every function returns
+ * GSNP_OK (0) on success or a GSNP_ERR_* code; gsnp_context_error() then holds
+ * a one-line message.  Host pointers are read and written synchronously; the
+ * device state lives in the context until gsnp_context_destroy().
+ *
+ * Two ways in:
+ *   1. Whole chromosome (this build's fast path): gsnp_load_tables,
+ *      gsnp_load_reference, gsnp_call_chromosome, then gsnp_fetch_sites or
+ *      gsnp_format_cns.  One call replaces the reference's window loop
+ *      Call_win::new_soap2cns (cpp/call_genotype.cc:422-669) and, per window,
+ *      cuda_updateSparse / cuda_likelihoodSparse / cuda_posterior
+ *      (kernel/update_kernel.cu:328, kernel/likelihood_kernel.cu:262,
+ *      kernel/posterior_kernel.cu:867).  The reference's window quirks (stale
+ *      host arrays in gap windows, the dropped last read, the reused
+ *      likelihood) are reproduced, so the output bytes are the reference's.
+ *   2. Window by window, the reference's own entry points, declared with
+ *      their original C++ names in gsnp_backend.h and implemented on top of
+ *      this context (gsnp_gb300/csrc/compat.cu).
+ */
+#ifndef GSNP_GB300_H
+#define GSNP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSNP_OK 0
+#define GSNP_ERR_CUDA 1        /* a CUDA call failed */
+#define GSNP_ERR_ARG 2         /* bad argument */
+#define GSNP_ERR_STATE 3       /* call out of order (e.g. no tables loaded) */
+#define GSNP_ERR_CAPACITY 4    /* an input exceeds a stated limit */
+#define GSNP_ERR_UNSORTED 5    /* alignments not sorted by position (the reference exits 255) */
+#define GSNP_ERR_INPUT 6       /* invalid alignment (read longer than -L, bad base) */
+
+#define GSNP_PRECISION_FP64 0        /* likelihood summed in FP64, in the reference's order */
+#define GSNP_PRECISION_FP32_FIXUP 1  /* FP32 compensated sums, FP64 recomputation near ties */
+
+typedef struct gsnp_context gsnp_context;
+
+/* Calling parameters (cpp/common.h:123-154 Parameter). */
+typedef struct gsnp_params {
+    int read_length;          /* -L, at most 255 */
+    int q_min;                /* quality char meaning 0 (-z), as a signed char */
+    int q_max;                /* highest calibrated quality char (-Q) */
+    double pcr_dependency;    /* log10 of -p */
+    double global_dependency; /* log10 of -g */
+    double het_val;           /* validated dbSNP HET prior (-b) */
+    double het_unval;         /* unvalidated dbSNP HET prior (-k) */
+    double althom_val;        /* validated dbSNP altHOM prior (-a) */
+    double althom_unval;      /* unvalidated dbSNP altHOM prior (-j) */
+    int rank_sum;             /* -u */
+    int monoploid;            /* -m */
+    int refine;               /* -2 */
+    int precision;            /* GSNP_PRECISION_* */
+    double het_novel;         /* novel HET prior (-e) */
+    double althom_novel;      /* novel altHOM prior (-r) */
+    int transition_dominant;  /* -t */
+} gsnp_params;
+
+/* One dbSNP row (cpp/soap_snp.h:714-760 Snp_info), position 0-based. */
+typedef struct gsnp_snp {
+    uint32_t pos;
+    uint8_t validated, hapmap, indel, pad;
+    double freq[4];           /* A, C, T, G */
+} gsnp_snp;
+
+/* Alignments of one chromosome in file order (cpp/soap_snp.h:119-201):
+ * bases and qualities at a fixed pitch of read_length bytes per read. */
+typedef struct gsnp_reads {
+    int64_t n;
+    const int32_t* pos;       /* 0-based start */
+    const int32_t* len;       /* read length */
+    const int32_t* hit;       /* number of hits */
+    const uint8_t* strand;    /* '+' or '-' */
+    const uint8_t* seq;       /* [n][pitch] base chars */
+    const uint8_t* qual;      /* [n][pitch] quality chars */
+    int32_t pitch;
+} gsnp_reads;
+
+/* Per-site call (32 bytes), the binary form of one cns row. */
+typedef struct gsnp_site_call {
+    uint8_t type1, base1, base2, q_cns;
+    uint8_t avg_q1, avg_q2, flags, pad;
+    uint16_t cu1, ca1, cu2, ca2;
+    uint32_t depth, repeat_time;
+    double rank_sum;
+} gsnp_site_call;
+
+/* Select device `device` and create a context (replaces GPUInit,
+ * kernel/gsnp_kernel.cu:20-22). */
+int gsnp_context_create(int device, gsnp_context** out);
+void gsnp_context_destroy(gsnp_context* ctx);
+const char* gsnp_context_error(const gsnp_context* ctx);
+
+/* Run the context's work on this cudaStream_t (default: a stream it owns). */
+int gsnp_set_stream(gsnp_context* ctx, void* stream);
+
+/* Calibration, prior and rank-sum tables in the reference's layouts:
+ * p_matrix[256*256*16] (cpp/matrix.cc:4), p_prior[8*16] (cpp/prior.cc:3),
+ * p_rank[64*64*2048] (cpp/rank_sum.cc:3).  Replaces GSNPKernelInit
+ * (kernel/gsnp_kernel.cu:24-33): the materialised log10 table and the
+ * adjusted-quality table are built here once. */
+int gsnp_load_tables(gsnp_context* ctx, const gsnp_params* params, const double* p_matrix,
+                     const double* p_prior, const double* p_rank);
+
+/* Reference of the called chromosome: one 4-bit site code per byte
+ * (bit 3 dbSNP, bit 2 N, bits 1:0 base ACTG; cpp/chromosome.cc:28-64) and its
+ * dbSNP rows sorted by position. */
+int gsnp_load_reference(gsnp_context* ctx, const uint8_t* site_codes, int64_t length, const gsnp_snp* snp,
+                        int64_t n_snp);
+
+/* Pass-1 calibration (cpp/matrix.cc:42-213): count every unique base of the
+ * alignments on the device by (quality, cycle, reference base, observed base)
+ * and fill the calibration matrix p_matrix[256*256*16] on the host.  The
+ * reference must be loaded. */
+int gsnp_calibrate(gsnp_context* ctx, const gsnp_params* params, const gsnp_reads* reads, double* p_matrix);
+
+/* Novel genotype priors p_prior[8*16] (cpp/prior.cc:3-43). */
+int gsnp_prior_table(const gsnp_params* params, double* p_prior);
+
+/* Exact Wilcoxon rank-sum table p_rank[64*64*2048] (cpp/rank_sum.cc:3-42). */
+int gsnp_rank_table(double* p_rank);
+
+/* Call every site of the chromosome from its alignments (host buffers).
+ * Reads with pos < 0 or pos + len >= length are skipped, an unsorted input is
+ * GSNP_ERR_UNSORTED, and the reference's window semantics are reproduced. */
+int gsnp_call_chromosome(gsnp_context* ctx, const gsnp_reads* reads);
+
+/* Re-run the calling kernels on the alignments already resident on the device
+ * (no host transfer); used to time the kernels alone. */
+int gsnp_recall_resident(gsnp_context* ctx);
+
+/* Copy calls for sites [first, first + count) to host memory. */
+int gsnp_fetch_sites(gsnp_context* ctx, int64_t first, int64_t count, gsnp_site_call* out);
+
+/* Format the cns text of the whole chromosome (cpp/call_genotype.cc:353-411).
+ * With buf == NULL, *size receives the number of bytes; otherwise up to *size
+ * bytes are written and *size receives the count. */
+int gsnp_format_cns(gsnp_context* ctx, const char* chr_name, char* buf, int64_t* size);
+
+/* Diagnostics of the last call: [0] sites called, [1] sites that took the
+ * FP64 fixup, [2] sites on the rank-sum normal path, [3] max |FP32 - FP64|
+ * of type_likely over fixup-checked sites (as raw double bits). */
+int gsnp_get_stats(gsnp_context* ctx, uint64_t* stats4);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSNP_GB300_H */

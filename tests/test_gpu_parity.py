@@ -1,0 +1,60 @@
+"""GPU parity: the sm_103a caller against the CPU oracle, byte for byte.
+
+Each case generates a seeded workload, runs the oracle binary on its text
+files, runs the same alignments through the C ABI (calibration, tables, whole
+chromosome call) and compares the cns text.  The shapes cover the window
+quirks: c4 has an N block longer than a window (gap windows, stale host
+counts), c2 has deep hotspots (record cap, deep tile bins) and mixed read
+lengths, c1/c3 carry dbSNP priors and c3 qualities up to 60.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gsnp_gb300 import api, synth
+
+from oracle_run import first_diff, flags_for, oracle_outputs
+
+CASES = [("c0", 0.1), ("c1", 0.004), ("c2", 0.01), ("c3", 0.004), ("c4", 0.0101)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,scale", CASES)
+def test_cns_text_matches_oracle(name, scale, tmp_path, oracle_bin, native_lib):
+    w = synth.make_workload(name, scale=scale)
+    paths = synth.write_inputs(w, str(tmp_path))
+    flags = flags_for(w, paths)
+    ref = oracle_outputs(oracle_bin, w, flags, str(tmp_path))
+    assert ref["rc"] == 0, ref["stderr"]
+    c, reads, pm = api.run_workload(w, flags)
+    try:
+        got = c.format_cns(w.chr_name)
+    finally:
+        c.close()
+    if got != ref["cns"]:
+        i, x, y = first_diff(got, ref["cns"])
+        pytest.fail(f"{name}: first differing row {i}:\n gpu   : {x!r}\n oracle: {y!r}")
+
+
+@pytest.mark.gpu
+def test_calibration_matrix_matches_oracle(tmp_path, oracle_bin, native_lib):
+    w = synth.make_workload("c0", scale=0.05)
+    paths = synth.write_inputs(w, str(tmp_path))
+    flags = flags_for(w, paths)
+    mat = os.path.join(str(tmp_path), "mat.txt")
+    ref = oracle_outputs(oracle_bin, w, flags + ["-M", mat], str(tmp_path))
+    assert ref["rc"] == 0, ref["stderr"]
+    c, reads, pm = api.run_workload(w, flags)
+    c.close()
+    L = int(flags[flags.index("-L") + 1])
+    rows = 0
+    with open(mat) as f:
+        for line in f:
+            parts = line.split()
+            q, coord = int(parts[0]), int(parts[1])
+            vals = np.array([float(x) for x in parts[2:]])
+            base = (q << 12) | (coord << 4)
+            np.testing.assert_array_equal(pm[base:base + 16], vals)
+            rows += 1
+    assert rows == 41 * L
