@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 consensus caller on the 30x workload (c1 shape).
+
+Workload: 50 Mbp reference (GC 41%, one 2 kbp N run), 100 bp single-end reads
+at 30x (15 M alignments, 1.5e9 bases), dbSNP rows on 1% of sites, flags
+-L 100 -t -u -2 -s.  The inputs are seeded synthetic data of that shape
+(gsnp_gb300.synth), generated on the GPU; there is no public dataset.
+
+A step is one calling pass over the whole chromosome.
+  value : sites/s with the alignments resident in HBM (tile classification and
+          the binned calling kernels, CUDA events on the launching stream);
+          the alignments (3 GB) exceed L2, so no flush is needed between steps.
+  e2e   : sites/s through the C ABI from pinned host buffers: upload of the
+          alignments, window replay, gather, calling, and the download of
+          every site's 32-byte call, all inside the timed step.
+The calling kernels' roofline is the HBM bandwidth; the algorithmic bytes of a
+site are 2*D + 9*D/Lbar + 0.5 + 32 (bases and qualities of the covering reads,
+per-read start/length/strand, the 4-bit reference code, a 32-byte call).
+
+--impl reference times the reference's calling algorithm on the host cores:
+the CPU oracle (oracle/, a restatement of the reference's single-threaded
+calling code) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = "c1"
+METRIC = "sites/s at 30x (bases/s = sites/s x mean depth)"
+UNIT = "sites/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gsnp", "reference"], default="gsnp")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
+    ap.add_argument("--scale", type=float, default=1.0, help="genome scale (1.0 = the named 50 Mbp workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def site_bytes(w):
+    """Algorithmic bytes of one called site."""
+    sites = w.genome_len
+    D = w.num_bases / sites
+    reads_per_site = w.num_reads / sites
+    return 2.0 * D + 9.0 * reads_per_site + 0.5 + 32.0
+
+
+class OracleSample:
+    """A bounded sample of the workload's shape written as the reference's
+    input files, timed through the CPU oracle (a port of the reference's
+    single-threaded calling code, run on one core)."""
+
+    def __init__(self, sample_len: int):
+        from gsnp_gb300 import synth
+        self.oracle = os.path.join(ROOT, "oracle", "_build", "gsnp_oracle")
+        if not os.path.exists(self.oracle):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True)
+        self.w = synth.make_workload(CONFIG, genome_len=sample_len)
+        self.dir = tempfile.TemporaryDirectory()
+        self.paths = synth.write_inputs(self.w, self.dir.name)
+        self.flags = [f for f in self.w.cli_flags(self.paths.get("dbsnp")) if f != "-C"]
+        self.sample = "%d-site c1-shaped sample (%d reads), calling pass (window loop + cns text), 1 thread" % (
+            self.w.genome_len, self.w.num_reads)
+
+    def run(self) -> float:
+        d = self.dir.name
+        env = dict(os.environ, GSNP_ORACLE_TIMING="1")
+        r = subprocess.run([self.oracle, "-i", self.paths["soap"], "-d", self.paths["ref"], "-o",
+                            os.path.join(d, "cns")] + self.flags, cwd=d, env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle failed: " + r.stderr[-500:])
+        for line in r.stderr.splitlines():
+            if line.startswith("pass2_seconds="):
+                return self.w.genome_len / float(line.split("=")[1])
+        raise RuntimeError("oracle printed no timing")
+
+
+def cpu_baseline(sample_len: int):
+    s = OracleSample(sample_len)
+    return s.run(), s.sample
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sample_len = 600_000 if args.scale >= 1.0 else max(40_000, int(600_000 * args.scale))
+    smp = OracleSample(sample_len)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v = smp.run()
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sample_len / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "c1: 50 Mbp, 100 bp reads at 30x, dbSNP 1%, -L 100 -t -u -2 -s",
+                   "sample_sites": sample_len},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp.sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import numpy as np
+    import torch
+    from gsnp_gb300 import api, synth
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist = None
+
+    precision = api.PRECISION_FP64 if args.precision == "fp64" else api.PRECISION_FP32_FIXUP
+    t0 = time.time()
+    w = synth.make_workload(CONFIG, scale=args.scale, backend="torch", device="cuda:%d" % local)
+    t_gen = time.time() - t0
+    flags = w.cli_flags("dbsnp")   # the dbSNP rows are passed in memory
+    p = api.params_from_flags(flags, precision)
+    codes = api.site_codes(w.ref, w.db_pos)
+    caller = api.Caller(local)
+    caller.load_reference(codes, api.snp_table(w))
+    arrs = [np.ascontiguousarray(x) for x in (w.pos, w.length, w.hit, w.strand)] + [w.seq, w.qual]
+    reads = api.Caller.reads_struct(*arrs)
+    pm = caller.calibrate(p, reads)
+    caller.load_tables(p, pm, caller.prior_table(p), caller.rank_table())
+    stream = torch.cuda.current_stream()
+    caller.set_stream(stream.cuda_stream)
+    caller.call(reads)                       # uploads the alignments, first pass
+    sites = w.genome_len
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident timing ----
+    for _ in range(args.warmup):
+        caller.recall_resident()
+    launches_per_step = len(caller.last_launches())
+    barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kernel_ms = {}
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            caller.recall_resident()
+            for li in caller.last_launches():
+                key = (li["kind"], li["slots"])
+                kernel_ms.setdefault(key, []).append((li["ms"], li["sites"], li["tiles"]))
+        end.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms_total = start.elapsed_time(end)
+    if dist is not None:
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = world * sites / (ms_step / 1000.0)
+
+    # ---- end to end through the C ABI from pinned host buffers ----
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 3)
+    out_pinned = torch.empty(sites * 32, dtype=torch.uint8, pin_memory=True)
+    e2e_times = []
+    for _ in range(e2e_steps):
+        barrier()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        caller.call(reads)
+        caller.lib.gsnp_fetch_sites(caller.ctx, 0, sites, out_pinned.data_ptr())
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t1)
+    h2d, d2h = caller.transfer_bytes()
+    e2e_s = max(statistics.mean(e2e_times), 1e-9)
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * sites / e2e_s
+    stats = caller.stats()
+
+    # ---- roofline of the dominant kernel (the calling bin with most device time) ----
+    peaks, peak_kind = load_peaks()
+    bsite = site_bytes(w)
+    dom_key = max((k for k in kernel_ms if k[0] == 1), key=lambda k: sum(x[0] for x in kernel_ms[k]))
+    dom = kernel_ms[dom_key]
+    dom_ms = statistics.mean(x[0] for x in dom)
+    dom_sites = dom[0][1]
+    achieved = bsite * dom_sites / (dom_ms / 1000.0) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    kernels = {("classify" if k[0] == 0 else "call_%d" % k[1]): round(statistics.mean(x[0] for x in v), 4)
+               for k, v in kernel_ms.items()}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cv, sample = cpu_baseline(1_200_000 if args.scale >= 1.0 else max(40_000, int(1_200_000 * args.scale)))
+            cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+        except Exception as exc:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": "failed: %s" % exc}
+
+    if rank == 0:
+        depth = w.num_bases / sites
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if precision == api.PRECISION_FP64 else "f32+f64",
+            "data": "synthetic (seeded generator of the c1 shape, generated on the GPU in %.1f s)" % t_gen,
+            "config": {"workload": "c1: 50 Mbp reference, 100 bp reads at 30x (15 M alignments), dbSNP 1%%, "
+                                   "-L 100 -t -u -2 -s; scale %.3g" % args.scale,
+                       "sites": sites, "reads": w.num_reads, "bases": w.num_bases, "mean_depth": depth,
+                       "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs (3 GB of alignments) exceed the 129 MB L2; no flush"},
+            "bases_per_s": value * depth,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "steps": e2e_steps},
+            "gpu_launches": launches_per_step * args.steps,
+            "kernels_ms": kernels,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "call_tiles_kernel<%d>" % dom_key[1], "sites_per_launch": dom_sites,
+                         "bytes_per_site": bsite, "peak_source": peak_kind},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "stats": {"fixup_sites": int(stats[1]), "normal_path_sites": int(stats[2])},
+        }
+        print(json.dumps(line), flush=True)
+    caller.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

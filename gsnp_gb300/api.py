@@ -51,6 +51,11 @@ class Reads(ctypes.Structure):
     ]
 
 
+class LaunchInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("slots", ctypes.c_int), ("tiles", ctypes.c_int64),
+                ("sites", ctypes.c_int64), ("ms", ctypes.c_float)]
+
+
 SNP_DTYPE = np.dtype([("pos", "<u4"), ("validated", "u1"), ("hapmap", "u1"), ("indel", "u1"), ("pad", "u1"),
                       ("freq", "<f8", (4,))])
 SITE_DTYPE = np.dtype([("type1", "u1"), ("base1", "u1"), ("base2", "u1"), ("q_cns", "u1"),
@@ -79,6 +84,8 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_fetch_sites": (ctypes.c_int, [_P, _I64, _I64, _P]),
         "gsnp_format_cns": (ctypes.c_int, [_P, ctypes.c_char_p, _P, ctypes.POINTER(_I64)]),
         "gsnp_get_stats": (ctypes.c_int, [_P, _P]),
+        "gsnp_last_launches": (ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_int)]),
+        "gsnp_transfer_bytes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -249,6 +256,18 @@ class Caller:
         self._check(self.lib.gsnp_format_cns(self.ctx, chr_name.encode(), buf, ctypes.byref(size)),
                     "gsnp_format_cns")
         return buf.raw[:size.value]
+
+    def last_launches(self) -> List[dict]:
+        n = ctypes.c_int(16)
+        arr = (LaunchInfo * 16)()
+        self._check(self.lib.gsnp_last_launches(self.ctx, arr, ctypes.byref(n)), "gsnp_last_launches")
+        return [dict(kind=arr[i].kind, slots=arr[i].slots, tiles=arr[i].tiles, sites=arr[i].sites, ms=arr[i].ms)
+                for i in range(min(n.value, 16))]
+
+    def transfer_bytes(self):
+        h, d = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self.lib.gsnp_transfer_bytes(self.ctx, ctypes.byref(h), ctypes.byref(d)), "gsnp_transfer_bytes")
+        return h.value, d.value
 
     def stats(self) -> np.ndarray:
         out = np.zeros(4, dtype=np.uint64)

@@ -239,10 +239,15 @@ struct SitePileup {
     int dep_uni, num;
 };
 
-/* posterior_kernel + posterior_kernel2 for one site (kernel/posterior_kernel.cu:680-864) */
-__device__ void site_posterior(const CallArgs& a, int64_t site, uint8_t ori, const SitePileup& p,
-                               const double* tl /* by genotype code, 16 */, const uint32_t* recs,
-                               SiteCall* out) {
+/* posterior_kernel + posterior_kernel2 for one site (kernel/posterior_kernel.cu:680-864).
+ *
+ * tl holds type_likely by genotype code.  When eps is given, tl is an FP32
+ * approximation and eps[g] bounds |tl[g] - FP64 type_likely[g]|; the function
+ * then returns false, writing nothing, unless every decision it makes (the
+ * genotype order behind type1/type2 and the truncated, clamped consensus
+ * quality) is provably the one the FP64 values give. */
+__device__ bool site_posterior(const CallArgs& a, int64_t site, uint8_t ori, const SitePileup& p,
+                               const double* tl, const double* eps, const uint32_t* recs, SiteCall* out) {
     const int ori7 = ori & 7;
     int base1 = 0, base2 = 0;
     int qual1 = -1, qual2 = -2, qual3 = -3;
@@ -270,25 +275,16 @@ __device__ void site_posterior(const CallArgs& a, int64_t site, uint8_t ori, con
 #pragma unroll
     for (int i = 0; i < 16; ++i) lp[i] = __ldg(a.log_prior + (ori7 << 4) + i);
     if ((ori & 0x8) && a.refine) {
-        /* dbSNP prior (kernel/posterior_kernel.cu:575-633, device version) */
+        /* dbSNP prior, precomputed per dbSNP row by snp_log_prior_kernel */
         const int64_t k = find_snp(a, site);
-        if (k >= 0 && !a.snp[k].indel) {
-            const DbSnpEntry& e = a.snp[k];
-            const int t_base = ori & 3;
-            for (int a1 = 0; a1 != 4; ++a1)
-                for (int a2 = a1; a2 != 4; ++a2) {
-                    if (!(e.freq[a1] > 0 && e.freq[a2] > 0)) continue;
-                    double pr;
-                    if (!e.hapmap) {
-                        if (a1 == a2 && a1 == t_base) pr = 1;
-                        else if (a1 == t_base || a2 == t_base) pr = e.validated ? a.het_val : a.het_unval;
-                        else if (a1 == a2) pr = e.validated ? a.althom_val : a.althom_unval;
-                        else pr = e.validated ? a.het_val : a.het_unval;
-                    } else {
-                        pr = GSNP_DMUL(GSNP_DMUL((a1 == a2 ? 1.0 : GSNP_DMUL(2.0, a.het_val)), e.freq[a1]), e.freq[a2]);
-                    }
-                    lp[(a1 << 2) | a2] = gsnp_cr_log10(pr);
-                }
+        if (k >= 0) {
+            const double2* src = reinterpret_cast<const double2*>(a.snp_lp + k * 16);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const double2 v = __ldg(src + i);
+                lp[2 * i] = v.x;
+                lp[2 * i + 1] = v.y;
+            }
         }
     }
     double tp[17];
@@ -305,35 +301,66 @@ __device__ void site_posterior(const CallArgs& a, int64_t site, uint8_t ori, con
             if (tp[g] >= tp[type1] || type1 == 16) { type2 = type1; type1 = g; }
             else if (tp[g] >= tp[type2] || type2 == 16) { type2 = g; }
         }
+    double ep[16];
+    if (eps) {
+        /* bound of |tp - tp_FP64|: the likelihood bound plus the rounding of the
+         * prior addition; exact (0) where the likelihood is exact */
+#pragma unroll
+        for (int g = 0; g < 16; ++g)
+            ep[g] = eps[g] == 0.0 ? 0.0 : eps[g] + 0x1p-51 * (fabs(tl[g]) + fabs(lp[g])) + 0x1p-1000;
+#pragma unroll
+        for (int a1 = 0; a1 != 4; ++a1)
+#pragma unroll
+            for (int a2 = a1; a2 != 4; ++a2) {
+                const int g = a1 << 2 | a2;
+                if ((a.monoploid && a1 != a2) || g == type1) continue;
+                if (ep[g] + ep[type1] > 0.0 && !(tp[type1] - tp[g] > ep[g] + ep[type1])) return false;
+                if (g == type2) continue;
+                if (ep[g] + ep[type2] > 0.0 && !(tp[type2] - tp[g] > ep[g] + ep[type2])) return false;
+            }
+    }
     bool normal_path = false;
     const double rs = a.rank_sum ? rank_test(a, recs, p.num, p.cu, type1, &normal_path) : 1.0;
-    int q;
-    if (rs == 0.0) {
-        q = 0;
-    } else {
-        const double d = GSNP_DMUL(10.0, GSNP_DSUB(tp[type1], tp[type2]));
-        q = (int)GSNP_DADD(d, GSNP_DMUL(10.0, gsnp_cr_log10(rs)));
-    }
-    if ((type1 & 3) == ((type1 >> 2) & 3)) {
-        if (qual1 > 0 && base1 != (type1 & 3)) q = 0;
-        else if (q > qual1 - qual2) q = qual1 - qual2;
-    } else {
+    /* clamps of posterior_kernel2 (kernel/posterior_kernel.cu:839-864) */
+    const bool hom = (type1 & 3) == ((type1 >> 2) & 3);
+    bool het_ok = false;
+    if (!hom) {
         /* base1/base2 may name an N reference base (4..7): the reference then
          * reads q_sum[4*site + base], i.e. the next site's q_sum[base - 4].
          * With q_sum summing to zero that is never consulted; otherwise
          * (base2 = N code) the next site's value is recomputed. */
         const int comb = base1 < base2 ? (base1 << 2 | base2) : (base2 << 2 | base1);
-        bool ok = type1 == comb;
-        if (ok) ok = (base1 < 4 ? p.qs[base1] : neighbour_qsum(a, site, base1 - 4)) > 0;
-        if (ok) ok = (base2 < 4 ? p.qs[base2] : neighbour_qsum(a, site, base2 - 4)) > 0;
-        if (ok) {
-            if (q > qual2 - qual3) q = qual2 - qual3;
+        het_ok = type1 == comb;
+        if (het_ok) het_ok = (base1 < 4 ? p.qs[base1] : neighbour_qsum(a, site, base1 - 4)) > 0;
+        if (het_ok) het_ok = (base2 < 4 ? p.qs[base2] : neighbour_qsum(a, site, base2 - 4)) > 0;
+    }
+    auto finalize = [&](int q) {
+        if (hom) {
+            if (qual1 > 0 && base1 != (type1 & 3)) q = 0;
+            else if (q > qual1 - qual2) q = qual1 - qual2;
         } else {
-            q = 0;
+            if (het_ok) {
+                if (q > qual2 - qual3) q = qual2 - qual3;
+            } else {
+                q = 0;
+            }
+        }
+        if (q > 99) q = 99;
+        if (q < 0) q = 0;
+        return q;
+    };
+    int q;
+    if (rs == 0.0) {
+        q = finalize(0);
+    } else {
+        const double d = GSNP_DMUL(10.0, GSNP_DSUB(tp[type1], tp[type2]));
+        const double raw = GSNP_DADD(d, GSNP_DMUL(10.0, gsnp_cr_log10(rs)));
+        q = finalize((int)raw);
+        if (eps && ep[type1] + ep[type2] > 0.0) {
+            const double delta = 10.0 * (ep[type1] + ep[type2]) * (1.0 + 0x1p-20) + 0x1p-48 * (fabs(raw) + 1.0);
+            if (finalize((int)(raw - delta)) != finalize((int)(raw + delta))) return false;
         }
     }
-    if (q > 99) q = 99;
-    if (q < 0) q = 0;
     SiteCall c;
     c.type1 = (uint8_t)type1;
     c.base1 = (uint8_t)base1;
@@ -351,6 +378,137 @@ __device__ void site_posterior(const CallArgs& a, int64_t site, uint8_t ori, con
     c.repeat_time = p.repeat;
     c.rank_sum = rs;
     *out = c;
+    return true;
+}
+
+/* log10 genotype priors of every dbSNP row (kernel/posterior_kernel.cu:575-633,
+ * the device version: no check of the number of listed alleles).  Run once per
+ * reference and parameter set so that the calling kernel only loads them. */
+__global__ void snp_log_prior_kernel(CallArgs a, double* out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n_snp) return;
+    const DbSnpEntry e = a.snp[k];
+    const int ori = a.ori[e.pos];
+    const int ori7 = ori & 7;
+    double lp[16];
+    for (int i = 0; i < 16; ++i) lp[i] = a.log_prior[(ori7 << 4) + i];
+    if (!e.indel) {
+        const int t_base = ori & 3;
+        for (int a1 = 0; a1 != 4; ++a1)
+            for (int a2 = a1; a2 != 4; ++a2) {
+                if (!(e.freq[a1] > 0 && e.freq[a2] > 0)) continue;
+                double pr;
+                if (!e.hapmap) {
+                    if (a1 == a2 && a1 == t_base) pr = 1;
+                    else if (a1 == t_base || a2 == t_base) pr = e.validated ? a.het_val : a.het_unval;
+                    else if (a1 == a2) pr = e.validated ? a.althom_val : a.althom_unval;
+                    else pr = e.validated ? a.het_val : a.het_unval;
+                } else {
+                    pr = GSNP_DMUL(GSNP_DMUL((a1 == a2 ? 1.0 : GSNP_DMUL(2.0, a.het_val)), e.freq[a1]), e.freq[a2]);
+                }
+                lp[(a1 << 2) | a2] = gsnp_cr_log10(pr);
+            }
+    }
+    for (int i = 0; i < 16; ++i) out[k * 16 + i] = lp[i];
+}
+
+cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, cudaStream_t stream) {
+    if (a.n_snp == 0) return cudaSuccess;
+    snp_log_prior_kernel<<<(unsigned)((a.n_snp + 127) / 128), 128, 0, stream>>>(a, out);
+    return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* likelihood walk (kernel/likelihood_kernel.cu:187-255)                      */
+/* ------------------------------------------------------------------------ */
+
+/* Walk one site's sorted records: per observed-base group, count repeats of
+ * each (strand, cycle) and of distinct ones, and hand each record's adjusted
+ * quality, cycle and base to f.  The per-site counters are left at zero. */
+template <class F>
+__device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* recs, uint8_t* cnt, int num, F&& f) {
+    const int L = a.L;
+    int gdc = -1, last_o = -1, gstart = 0;
+    for (int i = 0; i < num; ++i) {
+        const uint32_t w = recs[i * kTile];
+        const int o = rec_base(w);
+        const int q = rec_q(w);
+        const int coord = rec_coord(w);
+        const int key = rec_strand(w) * L + coord;
+        if (o != last_o) {
+            for (int j = gstart; j < i; ++j) {
+                const uint32_t wj = recs[j * kTile];
+                cnt[(rec_strand(wj) * L + rec_coord(wj)) * kTile] = 0;
+            }
+            gstart = i;
+            gdc = -1;
+            last_o = o;
+        }
+        int tmp = cnt[key * kTile];
+        const int occ = rec_occ(w);
+        for (int k = 0; k < occ; ++k) {
+            if (tmp == 0) gdc += 1;
+            tmp++;
+            const int qa = (tmp < a.tmax && gdc < a.gmax)
+                               ? (int)__ldg(a.qadj + ((size_t)tmp * a.gmax + gdc) * 65 + q)
+                               : 1;
+            f(qa, coord, o);
+        }
+        cnt[key * kTile] = (uint8_t)tmp;
+    }
+    for (int j = gstart; j < num; ++j) {
+        const uint32_t wj = recs[j * kTile];
+        cnt[(rec_strand(wj) * L + rec_coord(wj)) * kTile] = 0;
+    }
+}
+
+/* FP64 sums in the reference's order: the plain form and the fixup */
+__device__ __forceinline__ void likelihood_fp64(const CallArgs& a, const uint32_t* recs, uint8_t* cnt, int num,
+                                                double* tl) {
+    double s[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) s[i] = 0.0;
+    walk_records(a, recs, cnt, num, [&](int qa, int coord, int o) {
+        const double2* row = reinterpret_cast<const double2*>(a.lik64 + ((size_t)(qa * a.L + coord) * 4 + o) * 10);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            const double2 x = __ldg(row + v);
+            s[2 * v] = GSNP_DADD(s[2 * v], x.x);
+            s[2 * v + 1] = GSNP_DADD(s[2 * v + 1], x.y);
+        }
+    });
+#pragma unroll
+    for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = s[i];
+}
+
+/* FP32 Kahan sums with a bound on their distance to the FP64 sums.  Every
+ * term is <= 0 (the host checks the table), so sum|x| = |S|; the bound covers
+ * the rounding of each term to FP32, the compensated summation error
+ * (2u + O(n u^2)) sum|x| and the FP64 sum's own rounding (n u64 sum|x|). */
+__device__ __forceinline__ void likelihood_fp32(const CallArgs& a, const uint32_t* recs, uint8_t* cnt, int num,
+                                                double* tl, double* eps) {
+    float s[10], c[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) { s[i] = 0.f; c[i] = 0.f; }
+    walk_records(a, recs, cnt, num, [&](int qa, int coord, int o) {
+        const float4* row = reinterpret_cast<const float4*>(a.lik32 + ((size_t)(qa * a.L + coord) * 4 + o) * 12);
+        const float4 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2);
+        const float x[10] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x, x2.y};
+#pragma unroll
+        for (int v = 0; v < 10; ++v) {
+            const float y = __fsub_rn(x[v], c[v]);
+            const float t = __fadd_rn(s[v], y);
+            c[v] = __fsub_rn(__fsub_rn(t, s[v]), y);
+            s[v] = t;
+        }
+    });
+    const double k = 0x1p-22 + (double)num * 0x1p-45;
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        const int g = genotype_of(i);
+        tl[g] = (double)s[i];
+        eps[g] = fabs(tl[g]) * k;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -436,62 +594,22 @@ __global__ void __launch_bounds__(kTile) call_tiles_kernel(CallArgs a, const int
     if (p.ca[0] > 0xffff || p.ca[1] > 0xffff || p.ca[2] > 0xffff || p.ca[3] > 0xffff) atomicExch(a.error, 1);
 
     /* ---- likelihood over the sorted records (kernel/likelihood_kernel.cu:187-255) ---- */
-    double tl[16];
+    double tl[16], eps[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) tl[i] = 0.0;
-    if (!(wflags & kWinExternalLik)) {
-        double s[10];
-#pragma unroll
-        for (int i = 0; i < 10; ++i) s[i] = 0.0;
-        int gdc = -1, last_o = -1, gstart = 0;
-        for (int i = 0; i < p.num; ++i) {
-            const uint32_t w = recs[i * kTile];
-            const int o = rec_base(w);
-            const int q = rec_q(w);
-            const int coord = rec_coord(w);
-            const int key = rec_strand(w) * L + coord;
-            if (o != last_o) {
-                for (int j = gstart; j < i; ++j) {
-                    const uint32_t wj = recs[j * kTile];
-                    cnt[(rec_strand(wj) * L + rec_coord(wj)) * kTile] = 0;
-                }
-                gstart = i;
-                gdc = -1;
-                last_o = o;
-            }
-            int tmp = cnt[key * kTile];
-            const int occ = rec_occ(w);
-            for (int k = 0; k < occ; ++k) {
-                if (tmp == 0) gdc += 1;
-                tmp++;
-                const int qa = (tmp < a.tmax && gdc < a.gmax)
-                                   ? (int)__ldg(a.qadj + ((size_t)tmp * a.gmax + gdc) * 65 + q)
-                                   : 1;
-                const double2* row = reinterpret_cast<const double2*>(
-                    a.lik64 + ((size_t)(qa * L + coord) * 4 + o) * 10);
-#pragma unroll
-                for (int v = 0; v < 5; ++v) {
-                    const double2 x = __ldg(row + v);
-                    s[2 * v] = GSNP_DADD(s[2 * v], x.x);
-                    s[2 * v + 1] = GSNP_DADD(s[2 * v + 1], x.y);
-                }
-            }
-            cnt[key * kTile] = (uint8_t)tmp;
-        }
-#pragma unroll
-        for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = s[i];
-        if (wflags & kWinKeepLik) {
-            double* dst = a.lik_keep + site * 10;
-#pragma unroll
-            for (int i = 0; i < 10; ++i) dst[i] = s[i];
-        }
-    } else {
+    for (int i = 0; i < 16; ++i) { tl[i] = 0.0; eps[i] = 0.0; }
+    const bool external = (wflags & kWinExternalLik) != 0;
+    const bool fp32 = a.precision == 1 && !(wflags & (kWinKeepLik | kWinExternalLik));
+    if (external) {
         const int src = a.win_lik_src[win];
         if (src >= 0) {
             const double* srcp = a.lik_keep + ((int64_t)src * kWin + (site - (int64_t)win * kWin)) * 10;
 #pragma unroll
             for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = srcp[i];
         }
+    } else if (fp32) {
+        likelihood_fp32(a, recs, cnt, p.num, tl, eps);
+    } else {
+        likelihood_fp64(a, recs, cnt, p.num, tl);
         if (wflags & kWinKeepLik) {
             double* dst = a.lik_keep + site * 10;
 #pragma unroll
@@ -509,7 +627,28 @@ __global__ void __launch_bounds__(kTile) call_tiles_kernel(CallArgs a, const int
     }
 
     /* ---- posterior, rank-sum, consensus quality ---- */
-    site_posterior(a, site, __ldg(a.ori + site), p, tl, recs, a.out + site);
+    const uint8_t ori = __ldg(a.ori + site);
+    SiteCall call;
+    if (fp32 && (site & 4095) == 0 && a.stats) {
+        /* sampled accuracy of the FP32 sums against the FP64 ones */
+        double t64[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) t64[i] = 0.0;
+        likelihood_fp64(a, recs, cnt, p.num, t64);
+        double m = 0.0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) m = fmax(m, fabs(t64[i] - tl[i]));
+        atomicMax(a.stats + 3, (unsigned long long)__double_as_longlong(m));
+        atomicAdd(a.stats + 2, 1ull);
+    }
+    if (!site_posterior(a, site, ori, p, tl, fp32 ? eps : nullptr, recs, &call)) {
+        /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
+        likelihood_fp64(a, recs, cnt, p.num, tl);
+        site_posterior(a, site, ori, p, tl, nullptr, recs, &call);
+        call.flags |= 1;
+        atomicAdd(a.stats + 1, 1ull);
+    }
+    a.out[site] = call;
 }
 
 template __global__ void call_tiles_kernel<32>(CallArgs, const int32_t*);
@@ -521,45 +660,37 @@ size_t call_smem_bytes(int slots, int L) {
     return (size_t)slots * kTile * 4 + (((size_t)2 * L * kTile + 15) & ~(size_t)15) + (size_t)kMaxStagedReads * 4;
 }
 
-/* Launch classification and the binned calling kernels for one pass.
- * pass 0: windows with their own likelihood; pass 1: windows that reuse
- * another window's likelihood (run after pass 0). */
-cudaError_t launch_calling(const CallArgs& a, int pass, int64_t n_tiles, int* d_bin_count, int32_t* d_bin_tiles,
-                           int* h_bin_count, cudaStream_t stream) {
+cudaError_t launch_classify(const CallArgs& a, int pass, int64_t n_tiles, int* d_bin_count, int32_t* d_bin_tiles,
+                            cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(d_bin_count, 0, sizeof(int) * kNumBins, stream);
     if (e != cudaSuccess) return e;
     classify_tiles_kernel<<<(unsigned)n_tiles, kTile, 0, stream>>>(a, pass, n_tiles, d_bin_count, d_bin_tiles);
-    e = cudaMemcpyAsync(h_bin_count, d_bin_count, sizeof(int) * kNumBins, cudaMemcpyDeviceToHost, stream);
-    if (e != cudaSuccess) return e;
-    e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess) return e;
-    const int slots[kNumBins] = {32, 64, 128, 256};
-    for (int b = 0; b < kNumBins; ++b) {
-        if (h_bin_count[b] == 0) continue;
-        const size_t smem = call_smem_bytes(slots[b], a.L);
-        const int32_t* tl = d_bin_tiles + (int64_t)b * n_tiles;
-        switch (b) {
-            case 0:
-                cudaFuncSetAttribute(call_tiles_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                call_tiles_kernel<32><<<h_bin_count[b], kTile, smem, stream>>>(a, tl);
-                break;
-            case 1:
-                cudaFuncSetAttribute(call_tiles_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                call_tiles_kernel<64><<<h_bin_count[b], kTile, smem, stream>>>(a, tl);
-                break;
-            case 2:
-                cudaFuncSetAttribute(call_tiles_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                call_tiles_kernel<128><<<h_bin_count[b], kTile, smem, stream>>>(a, tl);
-                break;
-            default:
-                cudaFuncSetAttribute(call_tiles_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                call_tiles_kernel<256><<<h_bin_count[b], kTile, smem, stream>>>(a, tl);
-                break;
-        }
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+/* Launch the calling kernel for the `count` tiles of one depth bin. */
+cudaError_t launch_bin(const CallArgs& a, int bin, const int32_t* tiles, int count, cudaStream_t stream) {
+    static const int slots[kNumBins] = {32, 64, 128, 256};
+    const size_t smem = call_smem_bytes(slots[bin], a.L);
+    switch (bin) {
+        case 0:
+            cudaFuncSetAttribute(call_tiles_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            call_tiles_kernel<32><<<count, kTile, smem, stream>>>(a, tiles);
+            break;
+        case 1:
+            cudaFuncSetAttribute(call_tiles_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            call_tiles_kernel<64><<<count, kTile, smem, stream>>>(a, tiles);
+            break;
+        case 2:
+            cudaFuncSetAttribute(call_tiles_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            call_tiles_kernel<128><<<count, kTile, smem, stream>>>(a, tiles);
+            break;
+        default:
+            cudaFuncSetAttribute(call_tiles_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            call_tiles_kernel<256><<<count, kTile, smem, stream>>>(a, tiles);
+            break;
     }
-    return cudaSuccess;
+    return cudaGetLastError();
 }
 
 }  // namespace gsnp

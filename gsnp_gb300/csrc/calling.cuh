@@ -35,6 +35,7 @@ struct CallArgs {
     int64_t chr_len;
     const DbSnpEntry* snp;       /* sorted by position */
     int64_t n_snp;
+    const double* snp_lp;        /* [n_snp][16] log10 prior of each dbSNP site (refine mode) */
     /* tables */
     const double* lik64;         /* [qa_rows][L][4][10] log10 genotype terms */
     const float* lik32;          /* same, rounded to FP32 */

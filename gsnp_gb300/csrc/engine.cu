@@ -29,8 +29,10 @@
 
 namespace gsnp {
 
-cudaError_t launch_calling(const CallArgs& a, int pass, int64_t n_tiles, int* d_bin_count, int32_t* d_bin_tiles,
-                           int* h_bin_count, cudaStream_t stream);
+cudaError_t launch_classify(const CallArgs& a, int pass, int64_t n_tiles, int* d_bin_count, int32_t* d_bin_tiles,
+                            cudaStream_t stream);
+cudaError_t launch_bin(const CallArgs& a, int bin, const int32_t* tiles, int count, cudaStream_t stream);
+cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, cudaStream_t stream);
 
 /* ---- device helpers ---- */
 
@@ -141,6 +143,8 @@ struct gsnp_context {
     uint8_t* d_codes = nullptr;
     DbSnpEntry* d_snp = nullptr;
     int64_t n_snp = 0;
+    double* d_snp_lp = nullptr;
+    bool snp_lp_ready = false;
     /* resident reads (deposited, packed) */
     int64_t n_dep = 0;
     int64_t cap_dep = 0;
@@ -169,6 +173,12 @@ struct gsnp_context {
     int h_bin_count[kNumBins] = {0, 0, 0, 0};
     bool called = false;
     uint64_t stats[4] = {0, 0, 0, 0};
+    /* CUDA events around each launch of the last calling pass */
+    static const int kMaxLaunches = 16;
+    cudaEvent_t ev[2 * kMaxLaunches] = {};
+    gsnp_launch_info launches[kMaxLaunches];
+    int n_launches = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
 };
 
 namespace {
@@ -198,7 +208,7 @@ cudaError_t dev_alloc(T** p, size_t count) {
 
 void free_all(gsnp_context* c) {
     void* ptrs[] = {c->d_lik64, c->d_lik32, c->d_qadj, c->d_p_prior, c->d_log_prior, c->d_p_rank,
-                    c->d_codes, c->d_snp, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq,
+                    c->d_codes, c->d_snp, c->d_snp_lp, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq,
                     c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts, c->d_lik_keep,
                     c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles};
     for (void* p : ptrs)
@@ -218,6 +228,7 @@ CallArgs make_args(gsnp_context* c) {
     a.chr_len = c->chr_len;
     a.snp = c->d_snp;
     a.n_snp = c->n_snp;
+    a.snp_lp = c->d_snp_lp;
     a.lik64 = c->d_lik64;
     a.lik32 = c->d_lik32;
     a.qa_rows = c->tables.qa_rows;
@@ -236,7 +247,8 @@ CallArgs make_args(gsnp_context* c) {
     a.het_unval = c->params.het_unval;
     a.althom_val = c->params.althom_val;
     a.althom_unval = c->params.althom_unval;
-    a.precision = c->params.precision;
+    /* the FP32 error bound needs every table term <= 0 */
+    a.precision = c->tables.all_nonpositive ? c->params.precision : GSNP_PRECISION_FP64;
     a.win_flags = c->d_win_flags;
     a.win_lik_src = c->d_win_lik_src;
     a.out = c->d_out;
@@ -249,23 +261,58 @@ CallArgs make_args(gsnp_context* c) {
 
 int run_calling(gsnp_context* c) {
     const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    if (!c->snp_lp_ready) {
+        CK(dev_alloc(&c->d_snp_lp, (size_t)std::max<int64_t>(c->n_snp, 1) * 16), "cudaMalloc dbSNP priors");
+        const CallArgs a0 = make_args(c);
+        CK(launch_snp_log_prior(a0, c->d_snp_lp, c->stream), "dbSNP prior kernel");
+        c->snp_lp_ready = true;
+    }
     if (n_tiles > c->bin_tiles_cap) {
         CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * kNumBins), "cudaMalloc bins");
         c->bin_tiles_cap = n_tiles;
     }
+    if (!c->ev[0])
+        for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i) CK(cudaEventCreate(&c->ev[i]), "cudaEventCreate");
     CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
     CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4, c->stream), "memset");
     const CallArgs a = make_args(c);
     bool any_external = false;
     for (int64_t w = 0; w < c->plan.n_windows; ++w) any_external |= (c->plan.flags[w] & kWinExternalLik) != 0;
+    static const int slots[kNumBins] = {32, 64, 128, 256};
+    c->n_launches = 0;
+    auto begin = [&](int kind, int sl, int64_t tiles) -> int {
+        if (c->n_launches >= gsnp_context::kMaxLaunches) return -1;
+        const int k = c->n_launches++;
+        c->launches[k].kind = kind;
+        c->launches[k].slots = sl;
+        c->launches[k].tiles = tiles;
+        c->launches[k].sites = std::min<int64_t>(tiles * kTile, c->chr_len);
+        c->launches[k].ms = 0.f;
+        cudaEventRecord(c->ev[2 * k], c->stream);
+        return k;
+    };
+    auto end = [&](int k) {
+        if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], c->stream);
+    };
     for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
-        CK(launch_calling(a, pass, n_tiles, c->d_bin_count, c->d_bin_tiles, c->h_bin_count, c->stream),
-           "calling kernels");
+        int k = begin(0, 0, n_tiles);
+        CK(launch_classify(a, pass, n_tiles, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
+        end(k);
+        CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(int) * kNumBins, cudaMemcpyDeviceToHost, c->stream),
+           "bin counts");
+        CK(cudaStreamSynchronize(c->stream), "classify");
+        for (int b = 0; b < kNumBins; ++b) {
+            if (c->h_bin_count[b] == 0) continue;
+            k = begin(1, slots[b], c->h_bin_count[b]);
+            CK(launch_bin(a, b, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b], c->stream), "calling kernel");
+            end(k);
+        }
     }
     int err = 0;
     CK(cudaMemcpyAsync(&err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
     CK(cudaMemcpyAsync(c->stats, c->d_stats, sizeof(c->stats), cudaMemcpyDeviceToHost, c->stream), "stats");
     CK(cudaStreamSynchronize(c->stream), "calling");
+    for (int k = 0; k < c->n_launches; ++k) cudaEventElapsedTime(&c->launches[k].ms, c->ev[2 * k], c->ev[2 * k + 1]);
     if (err) return fail(c, GSNP_ERR_CAPACITY, "a site's count_all exceeds 65535");
     c->stats[0] = (uint64_t)c->chr_len;
     c->called = true;
@@ -301,6 +348,8 @@ void gsnp_context_destroy(gsnp_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_all(c);
+    for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -340,6 +389,7 @@ int gsnp_load_tables(gsnp_context* c, const gsnp_params* p, const double* p_matr
     CK(cudaMemcpy(c->d_log_prior, t.log_prior.data(), 128 * 8, cudaMemcpyHostToDevice), "upload");
     CK(cudaMemcpy(c->d_p_rank, p_rank, 64UL * 64UL * 2048UL * 8, cudaMemcpyHostToDevice), "upload");
     c->have_tables = true;
+    c->snp_lp_ready = false;
     return GSNP_OK;
 }
 
@@ -358,6 +408,7 @@ int gsnp_load_reference(gsnp_context* c, const uint8_t* codes, int64_t length, c
     if (n_snp > 0) CK(cudaMemcpy(c->d_snp, snp, sizeof(gsnp_snp) * n_snp, cudaMemcpyHostToDevice), "upload dbsnp");
     CK(dev_alloc(&c->d_out, (size_t)length), "cudaMalloc calls");
     c->out_sites = length;
+    c->snp_lp_ready = false;
     c->called = false;
     return GSNP_OK;
 }
@@ -411,6 +462,8 @@ int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
         c->cap_dep = nd;
     }
     c->n_dep = nd;
+    c->h2d_bytes = (uint64_t)P.n_windows * 5 + (uint64_t)nd * (4 + 4 + 4 + 1 + 8) + 2ULL * (uint64_t)r->n * r->pitch;
+    c->d2h_bytes = 0;
     {
         std::vector<int32_t> pos(nd), lenhit(nd), len(nd);
         std::vector<uint8_t> strand(nd);
@@ -525,7 +578,23 @@ int gsnp_fetch_sites(gsnp_context* c, int64_t first, int64_t count, gsnp_site_ca
     static_assert(sizeof(gsnp_site_call) == sizeof(SiteCall), "site call layout");
     CK(cudaMemcpyAsync(out, c->d_out + first, (size_t)count * sizeof(SiteCall), cudaMemcpyDeviceToHost, c->stream),
        "fetch");
+    c->d2h_bytes += (uint64_t)count * sizeof(SiteCall);
     CK(cudaStreamSynchronize(c->stream), "fetch");
+    return GSNP_OK;
+}
+
+int gsnp_last_launches(gsnp_context* c, gsnp_launch_info* out, int* n) {
+    if (!c || !n) return GSNP_ERR_ARG;
+    const int m = std::min(*n, c->n_launches);
+    if (out) memcpy(out, c->launches, sizeof(gsnp_launch_info) * m);
+    *n = c->n_launches;
+    return GSNP_OK;
+}
+
+int gsnp_transfer_bytes(gsnp_context* c, uint64_t* h2d, uint64_t* d2h) {
+    if (!c || !h2d || !d2h) return GSNP_ERR_ARG;
+    *h2d = c->h2d_bytes;
+    *d2h = c->d2h_bytes;
     return GSNP_OK;
 }
 

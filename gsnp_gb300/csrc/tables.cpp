@@ -75,7 +75,7 @@ int build_tables(const gsnp_params& p, const double* pm, const double* p_prior, 
     /* materialised genotype terms (kernel/likelihood_kernel.cu:137-161) for
      * the adjusted qualities and read cycles that can occur */
     t->lik64.assign((size_t)t->qa_rows * L * 4 * 10, 0.0);
-    t->lik32.assign(t->lik64.size(), 0.0f);
+    t->lik32.assign((size_t)t->qa_rows * L * 4 * 12, 0.0f);
     t->all_nonpositive = true;
     for (int q = 0; q < t->qa_rows; ++q)
         for (int c = 0; c < L; ++c)
@@ -91,7 +91,9 @@ int build_tables(const gsnp_params& p, const double* pm, const double* p_prior, 
                         ++k;
                     }
             }
-    for (size_t i = 0; i < t->lik64.size(); ++i) t->lik32[i] = (float)t->lik64[i];
+    /* FP32 copy with rows padded to 12 entries (three 16-byte loads) */
+    for (size_t r = 0; r < (size_t)t->qa_rows * L * 4; ++r)
+        for (int k = 0; k < 10; ++k) t->lik32[r * 12 + k] = (float)t->lik64[r * 10 + k];
 
     t->log_prior.resize(128);
     for (int i = 0; i < 128; ++i) t->log_prior[i] = gsnp_cr_log10(p_prior[i]);

@@ -15,7 +15,10 @@ caller is measured on:
 Every random quantity is drawn from a counter-based SplitMix64 stream keyed by
 (seed, stream id, element index).  The draws therefore do not depend on numpy's
 Generator implementation or on how the work is chunked, and the same seed gives
-byte-identical inputs on x86-64 and aarch64.
+byte-identical inputs on x86-64 and aarch64.  The per-base stage (qualities,
+sequencing errors) uses integer arithmetic only - inverse-CDF tables of 2^16
+entries per read cycle and 32-bit error thresholds - so it can also run on the
+GPU through torch (backend="torch") and produce the same bytes.
 
 Base codes follow the caller's ACTG order (A=0, C=1, T=2, G=3).  Positions are
 0-based in memory and written 1-based in the SOAP and dbSNP text formats.
@@ -165,11 +168,13 @@ def _alt_base(ref_code: np.ndarray, u: np.ndarray, pick: np.ndarray) -> np.ndarr
 
 
 def make_workload(name: str, scale: float = 1.0, seed: Optional[int] = None,
-                  genome_len: Optional[int] = None) -> Workload:
+                  genome_len: Optional[int] = None, backend: str = "numpy", device: str = "cuda") -> Workload:
     """Build workload `name` ("c0".."c4").
 
     scale shrinks the genome (and with it the read count) while keeping depth,
     read lengths and quality model.  seed defaults to 20260000 + config index.
+    backend "torch" runs the per-base stage on `device` and returns seq/qual in
+    pinned host memory; the bytes equal the numpy backend's.
     """
     cfg = CONFIGS[name]
     if seed is None:
@@ -202,7 +207,7 @@ def make_workload(name: str, scale: float = 1.0, seed: Optional[int] = None,
     a_p = st.below(2 * snp_pos.size, snp_pos.size, 2)
     h_p = st.below(3 * snp_pos.size, snp_pos.size, 2)
     alt = _alt_base(code[snp_pos], a_u, a_p)
-    hap = np.stack([code.copy(), code.copy()])
+    hap = np.stack([code.astype(np.uint8), code.astype(np.uint8)])
     is_het = t_u < 2.0 / 3.0
     hap[h_p[is_het], snp_pos[is_het]] = alt[is_het]
     hap[0, snp_pos[~is_het]] = alt[~is_het]
@@ -232,15 +237,18 @@ def make_workload(name: str, scale: float = 1.0, seed: Optional[int] = None,
     lens = np.empty(0, dtype=np.int64)
     ss = Stream(seed, S_START)
     ls = Stream(seed, S_LEN)
-    cw = np.cumsum(weight)
-    total_w = cw[-1]
+    cw = np.cumsum(weight) if cfg.cn_segments else None
+    total_w = cw[-1] if cfg.cn_segments else float(G)
     drawn = 0
     while starts.size < R:
         need = int((R - starts.size) * 1.1) + 64
-        uu = ss.uniform(drawn, need)
         ln = np.asarray(cfg.read_lens, dtype=np.int64)[ls.below(drawn, need, len(cfg.read_lens))]
+        if cfg.cn_segments:
+            uu = ss.uniform(drawn, need)
+            cand = np.searchsorted(cw, uu * total_w, side="right").astype(np.int64)
+        else:
+            cand = ss.below(drawn, need, G)
         drawn += need
-        cand = np.searchsorted(cw, uu * total_w, side="right").astype(np.int64)
         ok = (cand + ln < G) & (n_prefix[np.minimum(cand + ln, G)] - n_prefix[np.minimum(cand, G)] == 0)
         starts = np.concatenate([starts, cand[ok]])
         lens = np.concatenate([lens, ln[ok]])
@@ -286,54 +294,11 @@ def make_workload(name: str, scale: float = 1.0, seed: Optional[int] = None,
     multi = hu.uniform(0, R) < cfg.multi_hit_frac
     hit = np.where(multi, 2 + hu.below(R, R, 4), 1).astype(np.int32)
 
-    # ---- bases and qualities (chunked over reads) ----
-    seq = np.zeros((R, Lmax), dtype=np.uint8)
-    qual = np.zeros((R, Lmax), dtype=np.uint8)
-    mism = np.zeros(R, dtype=np.int32)
-    qs, es, eb, lq = Stream(seed, S_QUAL), Stream(seed, S_ERR), Stream(seed, S_ERRBASE), Stream(seed, S_LOWQ)
-    q_levels = np.arange(0, 128, dtype=np.float64)
-    p_err = np.power(10.0, -q_levels / 10.0)
-    coord = np.arange(Lmax, dtype=np.int64)
-    CH = 1 << 18
-    for r0 in range(0, R, CH):
-        r1 = min(R, r0 + CH)
-        n = r1 - r0
-        st_ = starts[r0:r1]
-        ln_ = lens[r0:r1]
-        valid = coord[None, :] < ln_[:, None]
-        gpos = np.minimum(st_[:, None] + coord[None, :], G - 1)
-        truth = hap[hap_id[r0:r1][:, None], gpos]
-        # machine cycle: coord on '+', len-1-coord on '-'
-        minus = strand_minus[r0:r1][:, None]
-        cycle = np.where(minus, ln_[:, None] - 1 - coord[None, :], coord[None, :])
-        denom = np.maximum(ln_[:, None] - 1, 1).astype(np.float64)
-        mu = cfg.q_mu0 + (cfg.q_mu1 - cfg.q_mu0) * (cycle / denom)
-        z = qs.normal(r0 * Lmax, n * Lmax).reshape(n, Lmax)
-        q = np.clip(np.rint(mu + cfg.q_sd * z), cfg.q_lo, cfg.q_hi).astype(np.int64)
-        if cfg.lowq_clusters > 0:
-            # clusters of 5 consecutive cycles forced to Q2-Q8
-            uq = lq.uniform(r0 * Lmax, n * Lmax).reshape(n, Lmax)
-            startc = (uq < cfg.lowq_clusters) & (cycle + 5 <= ln_[:, None])
-            lowv = 2 + lq.below(1_000_000_000_000 + r0 * Lmax, n * Lmax, 7).reshape(n, Lmax)
-            cyc_hit = np.zeros((n, Lmax + 5), dtype=np.int64)
-            # mark cycles c..c+4 of every cluster start (in cycle coordinates)
-            rows, cols = np.nonzero(startc)
-            cstart = cycle[rows, cols]
-            for d in range(5):
-                cyc_hit[rows, cstart + d] = lowv[rows, cols]
-            forced = np.take_along_axis(cyc_hit, cycle, axis=1)
-            q = np.where(forced > 0, forced, q)
-        err = es.uniform(r0 * Lmax, n * Lmax).reshape(n, Lmax) < p_err[q]
-        shift = 1 + eb.below(r0 * Lmax, n * Lmax, 3).reshape(n, Lmax)
-        obs = np.where(err, (truth + shift) & 3, truth)
-        s_ascii = ACTG[obs]
-        q_ascii = (64 + q).astype(np.uint8)
-        s_ascii[~valid] = 0
-        q_ascii[~valid] = 0
-        seq[r0:r1] = s_ascii
-        qual[r0:r1] = q_ascii
-        refc = np.where(valid, code[gpos], -1)
-        mism[r0:r1] = np.sum((obs != refc) & valid, axis=1)
+    # ---- bases and qualities ----
+    if backend == "torch":
+        seq, qual, mism = _bases_torch(cfg, seed, G, Lmax, starts, lens, hap, hap_id, strand_minus, code, device)
+    else:
+        seq, qual, mism = _bases_numpy(cfg, seed, G, Lmax, starts, lens, hap, hap_id, strand_minus, code)
 
     strand = np.where(strand_minus, ord("-"), ord("+")).astype(np.uint8)
 
@@ -365,6 +330,186 @@ def make_workload(name: str, scale: float = 1.0, seed: Optional[int] = None,
                     strand=strand, seq=seq, qual=qual, mismatch=mism,
                     db_pos=db_pos.astype(np.int64), db_hapmap=hapmap, db_validated=validated,
                     db_freq=freq)
+
+
+# ---------------------------------------------------------------------------
+# per-base stage: integer-only draws
+# ---------------------------------------------------------------------------
+
+_U64 = (1 << 64) - 1
+
+
+def _signed(x: int) -> int:
+    x &= _U64
+    return x - (1 << 64) if x >= (1 << 63) else x
+
+
+def quality_tables(cfg: Config, read_len: int) -> np.ndarray:
+    """[read_len][65536] uint8: inverse CDF of the Phred quality at each cycle.
+
+    q = round(N(mu(c), sd)) clipped to [q_lo, q_hi], mu falling linearly from
+    q_mu0 at the first cycle to q_mu1 at the last; the CDF is resolved to
+    1/65536.
+    """
+    out = np.empty((read_len, 65536), dtype=np.uint8)
+    ks = np.arange(cfg.q_lo, cfg.q_hi + 1)
+    grid = np.arange(65536, dtype=np.int64)
+    for c in range(read_len):
+        mu = cfg.q_mu0 + (cfg.q_mu1 - cfg.q_mu0) * (c / max(read_len - 1, 1))
+        cdf = [0.5 * (1.0 + math.erf((k + 0.5 - mu) / (cfg.q_sd * math.sqrt(2.0)))) for k in ks[:-1]]
+        thr = np.array([int(round(x * 65536.0)) for x in cdf] + [65536], dtype=np.int64)
+        out[c] = ks[np.searchsorted(thr, grid, side="right")]
+    return out
+
+
+def error_thresholds() -> np.ndarray:
+    """floor(10^(-q/10) * 2^32) for q in [0, 128): a base is miscalled when the
+    high 32 bits of its draw fall below the threshold of its quality."""
+    return np.array([min(int(math.floor((10.0 ** (-q / 10.0)) * 4294967296.0)), (1 << 32) - 1)
+                     for q in range(128)], dtype=np.uint64)
+
+
+def _bases_numpy(cfg, seed, G, Lmax, starts, lens, hap, hap_id, strand_minus, code):
+    R = starts.size
+    seq = np.zeros((R, Lmax), dtype=np.uint8)
+    qual = np.zeros((R, Lmax), dtype=np.uint8)
+    mism = np.zeros(R, dtype=np.int32)
+    qs, es, lq = Stream(seed, S_QUAL), Stream(seed, S_ERR), Stream(seed, S_LOWQ)
+    lens_set = sorted(set(int(x) for x in cfg.read_lens))
+    tables = np.stack([np.vstack([quality_tables(cfg, Lr), np.zeros((Lmax - Lr, 65536), np.uint8)])
+                       for Lr in lens_set])
+    len_index = np.zeros(Lmax + 1, dtype=np.int64)
+    for i, Lr in enumerate(lens_set):
+        len_index[Lr] = i
+    thr = error_thresholds()
+    low_thr = np.uint64(int(cfg.lowq_clusters * 4294967296.0))
+    coord = np.arange(Lmax, dtype=np.int64)
+    CH = 1 << 16
+    m32 = np.uint64(0xFFFFFFFF)
+    for r0 in range(0, R, CH):
+        r1 = min(R, r0 + CH)
+        n = r1 - r0
+        st_ = starts[r0:r1]
+        ln_ = lens[r0:r1]
+        valid = coord[None, :] < ln_[:, None]
+        gpos = np.minimum(st_[:, None] + coord[None, :], G - 1)
+        truth = hap[hap_id[r0:r1][:, None], gpos].astype(np.int64)
+        minus = strand_minus[r0:r1][:, None]
+        cycle = np.where(minus, ln_[:, None] - 1 - coord[None, :], coord[None, :])
+        cycle = np.where(valid, cycle, 0)
+        uq = qs.u64(r0 * Lmax, n * Lmax).reshape(n, Lmax)
+        q = tables[len_index[ln_][:, None], cycle, (uq >> np.uint64(48)).astype(np.int64)].astype(np.int64)
+        if cfg.lowq_clusters > 0:
+            ul = lq.u64(r0 * Lmax, n * Lmax).reshape(n, Lmax)
+            startc = ((ul >> np.uint64(32)) < low_thr) & (cycle + 5 <= ln_[:, None]) & valid
+            lowv = (2 + (((ul & m32) * np.uint64(7)) >> np.uint64(32))).astype(np.int64)
+            forced = np.zeros((n, Lmax + 5), dtype=np.int64)
+            rows, cols = np.nonzero(startc)
+            cst = cycle[rows, cols]
+            for d in range(5):
+                forced[rows, cst + d] = lowv[rows, cols]
+            fq = np.take_along_axis(forced, cycle, axis=1)
+            q = np.where(fq > 0, fq, q)
+        ue = es.u64(r0 * Lmax, n * Lmax).reshape(n, Lmax)
+        err = (ue >> np.uint64(32)) < thr[q]
+        shift = (1 + (((ue & m32) * np.uint64(3)) >> np.uint64(32))).astype(np.int64)
+        obs = np.where(err, (truth + shift) & 3, truth)
+        s_ascii = ACTG[obs]
+        q_ascii = (64 + q).astype(np.uint8)
+        s_ascii[~valid] = 0
+        q_ascii[~valid] = 0
+        seq[r0:r1] = s_ascii
+        qual[r0:r1] = q_ascii
+        refc = np.where(valid, code[gpos], -1)
+        mism[r0:r1] = np.sum((obs != refc) & valid, axis=1)
+    return seq, qual, mism
+
+
+def _bases_torch(cfg, seed, G, Lmax, starts, lens, hap, hap_id, strand_minus, code, device):
+    import torch
+    dev = torch.device(device)
+    R = starts.size
+    pin = dev.type == "cuda"
+    seq = torch.empty((R, Lmax), dtype=torch.uint8, pin_memory=pin)
+    qual = torch.empty((R, Lmax), dtype=torch.uint8, pin_memory=pin)
+    mism = torch.empty(R, dtype=torch.int32, pin_memory=pin)
+    M1 = torch.tensor(_signed(0xBF58476D1CE4E5B9), dtype=torch.int64, device=dev)
+    M2 = torch.tensor(_signed(0x94D049BB133111EB), dtype=torch.int64, device=dev)
+    GAM = torch.tensor(_signed(0x9E3779B97F4A7C15), dtype=torch.int64, device=dev)
+
+    def lsr(z, k):
+        return (z >> k) & ((1 << (64 - k)) - 1)
+
+    def mix(z):
+        z = (z ^ lsr(z, 30)) * M1
+        z = (z ^ lsr(z, 27)) * M2
+        return z ^ lsr(z, 31)
+
+    def u64(stream: Stream, start: int, n: int):
+        key = torch.tensor(_signed(int(stream.key)), dtype=torch.int64, device=dev)
+        idx = torch.arange(start + 1, start + 1 + n, dtype=torch.int64, device=dev)
+        return mix(key + idx * GAM)
+
+    qs, es, lq = Stream(seed, S_QUAL), Stream(seed, S_ERR), Stream(seed, S_LOWQ)
+    lens_set = sorted(set(int(x) for x in cfg.read_lens))
+    tables = np.stack([np.vstack([quality_tables(cfg, Lr), np.zeros((Lmax - Lr, 65536), np.uint8)])
+                       for Lr in lens_set])
+    len_index = np.zeros(Lmax + 1, dtype=np.int64)
+    for i, Lr in enumerate(lens_set):
+        len_index[Lr] = i
+    t_tab = torch.from_numpy(tables).to(dev).to(torch.int64)
+    t_len_index = torch.from_numpy(len_index).to(dev)
+    t_thr = torch.from_numpy(error_thresholds().astype(np.int64)).to(dev)
+    t_hap = torch.from_numpy(hap).to(dev)
+    t_code = torch.from_numpy(code.astype(np.uint8)).to(dev).to(torch.int64)
+    t_starts = torch.from_numpy(starts.astype(np.int64)).to(dev)
+    t_lens = torch.from_numpy(lens.astype(np.int64)).to(dev)
+    t_hapid = torch.from_numpy(hap_id.astype(np.int64)).to(dev)
+    t_minus = torch.from_numpy(strand_minus).to(dev)
+    t_actg = torch.tensor([65, 67, 84, 71], dtype=torch.uint8, device=dev)
+    low_thr = int(cfg.lowq_clusters * 4294967296.0)
+    coord = torch.arange(Lmax, dtype=torch.int64, device=dev)
+    m32 = 0xFFFFFFFF
+    CH = 1 << 20
+    for r0 in range(0, R, CH):
+        r1 = min(R, r0 + CH)
+        n = r1 - r0
+        st_ = t_starts[r0:r1]
+        ln_ = t_lens[r0:r1]
+        valid = coord[None, :] < ln_[:, None]
+        gpos = torch.clamp(st_[:, None] + coord[None, :], max=G - 1)
+        truth = t_hap[t_hapid[r0:r1][:, None], gpos].to(torch.int64)
+        minus = t_minus[r0:r1][:, None]
+        cycle = torch.where(minus, ln_[:, None] - 1 - coord[None, :], coord[None, :])
+        cycle = torch.where(valid, cycle, torch.zeros_like(cycle))
+        uq = u64(qs, r0 * Lmax, n * Lmax).reshape(n, Lmax)
+        q = t_tab[t_len_index[ln_][:, None], cycle, lsr(uq, 48)]
+        if cfg.lowq_clusters > 0:
+            ul = u64(lq, r0 * Lmax, n * Lmax).reshape(n, Lmax)
+            startc = (lsr(ul, 32) < low_thr) & (cycle + 5 <= ln_[:, None]) & valid
+            lowv = 2 + (((ul & m32) * 7) >> 32)
+            forced = torch.zeros((n, Lmax + 5), dtype=torch.int64, device=dev)
+            rows, cols = torch.nonzero(startc, as_tuple=True)
+            cst = cycle[rows, cols]
+            for d in range(5):
+                forced[rows, cst + d] = lowv[rows, cols]
+            fq = torch.gather(forced, 1, cycle)
+            q = torch.where(fq > 0, fq, q)
+        ue = u64(es, r0 * Lmax, n * Lmax).reshape(n, Lmax)
+        err = lsr(ue, 32) < t_thr[q]
+        shift = 1 + (((ue & m32) * 3) >> 32)
+        obs = torch.where(err, (truth + shift) & 3, truth)
+        s_ascii = t_actg[obs]
+        q_ascii = (64 + q).to(torch.uint8)
+        s_ascii[~valid] = 0
+        q_ascii[~valid] = 0
+        seq[r0:r1].copy_(s_ascii, non_blocking=True)
+        qual[r0:r1].copy_(q_ascii, non_blocking=True)
+        refc = torch.where(valid, t_code[gpos], torch.full_like(gpos, -1))
+        mism[r0:r1].copy_(((obs != refc) & valid).sum(dim=1).to(torch.int32), non_blocking=True)
+    if pin:
+        torch.cuda.synchronize(dev)
+    return seq.numpy(), qual.numpy(), mism.numpy()
 
 
 # ---------------------------------------------------------------------------

@@ -122,6 +122,45 @@ GSNP_HD gsnp_dd gsnp_dd_div(gsnp_dd x, gsnp_dd y) {
 #define GSNP_INVLN10_LO 0x1.95355baaafad3p-57
 #define GSNP_INVLN2 0x1.71547652b82fep+0
 
+/* 1/(2k+1) for k = 0..21 as double-double pairs (atanh series of log) */
+#define GSNP_ATANH_COEF { \
+    {0x1.0000000000000p+0, 0x0.0p+0}, \
+    {0x1.5555555555555p-2, 0x1.5555555555555p-56}, \
+    {0x1.999999999999ap-3, -0x1.999999999999ap-57}, \
+    {0x1.2492492492492p-3, 0x1.2492492492492p-57}, \
+    {0x1.c71c71c71c71cp-4, 0x1.c71c71c71c71cp-58}, \
+    {0x1.745d1745d1746p-4, -0x1.745d1745d1746p-59}, \
+    {0x1.3b13b13b13b14p-4, -0x1.3b13b13b13b14p-58}, \
+    {0x1.1111111111111p-4, 0x1.1111111111111p-60}, \
+    {0x1.e1e1e1e1e1e1ep-5, 0x1.e1e1e1e1e1e1ep-61}, \
+    {0x1.af286bca1af28p-5, 0x1.af286bca1af28p-59}, \
+    {0x1.8618618618618p-5, 0x1.8618618618618p-59}, \
+    {0x1.642c8590b2164p-5, 0x1.642c8590b2164p-60}, \
+    {0x1.47ae147ae147bp-5, -0x1.eb851eb851eb8p-61}, \
+    {0x1.2f684bda12f68p-5, 0x1.2f684bda12f68p-59}, \
+    {0x1.1a7b9611a7b96p-5, 0x1.1a7b9611a7b96p-61}, \
+    {0x1.0842108421084p-5, 0x1.0842108421084p-60}, \
+    {0x1.f07c1f07c1f08p-6, -0x1.f07c1f07c1f08p-61}, \
+    {0x1.d41d41d41d41dp-6, 0x1.0750750750750p-60}, \
+    {0x1.bacf914c1bad0p-6, -0x1.bacf914c1bad0p-60}, \
+    {0x1.a41a41a41a41ap-6, 0x1.0690690690690p-60}, \
+    {0x1.8f9c18f9c18fap-6, -0x1.f3831f3831f38p-61}, \
+    {0x1.7d05f417d05f4p-6, 0x1.7d05f417d05f4p-62} \
+}
+/* 1/n for n = 0..9 (entries 0 and 1 unused) as double-double pairs (Taylor series of expm1) */
+#define GSNP_INV_N_COEF { \
+    {0.0, 0.0}, \
+    {0.0, 0.0}, \
+    {0x1.0000000000000p-1, 0.0}, \
+    {0x1.5555555555555p-2, 0x1.5555555555555p-56}, \
+    {0x1.0000000000000p-2, 0.0}, \
+    {0x1.999999999999ap-3, -0x1.999999999999ap-57}, \
+    {0x1.5555555555555p-3, 0x1.5555555555555p-57}, \
+    {0x1.2492492492492p-3, 0x1.2492492492492p-57}, \
+    {0x1.0000000000000p-3, 0.0}, \
+    {0x1.c71c71c71c71cp-4, 0x1.c71c71c71c71cp-58} \
+}
+
 GSNP_HD double gsnp_bits_to_double(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
 GSNP_HD uint64_t gsnp_double_to_bits(double d) { uint64_t u; memcpy(&u, &d, 8); return u; }
 
@@ -144,11 +183,12 @@ GSNP_HD double gsnp_cr_exp(double x) {
     r = gsnp_dd_sub(r, gsnp_dd_make(GSNP_DMUL(kd, GSNP_LN2_C), 0.0));
     /* r' = r / 2^10, |r'| < 3.4e-4; expm1(r') by its Taylor series to degree 9 */
     gsnp_dd rp = gsnp_dd_make(GSNP_DMUL(r.hi, 0x1p-10), GSNP_DMUL(r.lo, 0x1p-10));
+    const double inv_n[10][2] = GSNP_INV_N_COEF;
     gsnp_dd s = gsnp_dd_make(1.0, 0.0);
     for (int n = 9; n >= 2; --n) {
         /* s = 1 + r'/n * s */
         s = gsnp_dd_mul(s, rp);
-        s = gsnp_dd_div(s, gsnp_dd_make((double)n, 0.0));
+        s = gsnp_dd_mul(s, gsnp_dd_make(inv_n[n][0], inv_n[n][1]));
         s = gsnp_dd_add(gsnp_dd_make(1.0, 0.0), s);
     }
     s = gsnp_dd_mul(s, rp); /* expm1(r') */
@@ -185,10 +225,11 @@ GSNP_HD double gsnp_cr_log10(double x) {
     gsnp_dd den = gsnp_two_sum(m, 1.0);
     gsnp_dd s = gsnp_dd_div(num, den);
     gsnp_dd s2 = gsnp_dd_mul(s, s);
-    gsnp_dd acc = gsnp_dd_div(gsnp_dd_make(1.0, 0.0), gsnp_dd_make(43.0, 0.0));
+    const double coef[22][2] = GSNP_ATANH_COEF;
+    gsnp_dd acc = gsnp_dd_make(coef[21][0], coef[21][1]);
     for (int k = 20; k >= 0; --k) {
         acc = gsnp_dd_mul(acc, s2);
-        acc = gsnp_dd_add(acc, gsnp_dd_div(gsnp_dd_make(1.0, 0.0), gsnp_dd_make((double)(2 * k + 1), 0.0)));
+        acc = gsnp_dd_add(acc, gsnp_dd_make(coef[k][0], coef[k][1]));
     }
     gsnp_dd lm = gsnp_dd_mul(acc, s);
     lm = gsnp_dd_make(GSNP_DMUL(lm.hi, 2.0), GSNP_DMUL(lm.lo, 2.0));

@@ -143,9 +143,28 @@ int gsnp_fetch_sites(gsnp_context* ctx, int64_t first, int64_t count, gsnp_site_
  * bytes are written and *size receives the count. */
 int gsnp_format_cns(gsnp_context* ctx, const char* chr_name, char* buf, int64_t* size);
 
+/* One kernel launch of the last calling pass, timed with CUDA events on the
+ * context's stream. */
+typedef struct gsnp_launch_info {
+    int kind;          /* 0: tile classification, 1: calling kernel of one depth bin */
+    int slots;         /* record slots per site of the bin (calling kernels) */
+    int64_t tiles;     /* 128-site tiles processed */
+    int64_t sites;
+    float ms;          /* device time of the launch */
+} gsnp_launch_info;
+
+/* Launches of the last calling pass: copies up to *n entries, sets *n to the
+ * number of launches. */
+int gsnp_last_launches(gsnp_context* ctx, gsnp_launch_info* out, int* n);
+
+/* Host-to-device bytes of the last gsnp_call_chromosome and device-to-host
+ * bytes fetched since then. */
+int gsnp_transfer_bytes(gsnp_context* ctx, uint64_t* h2d, uint64_t* d2h);
+
 /* Diagnostics of the last call: [0] sites called, [1] sites that took the
- * FP64 fixup, [2] sites on the rank-sum normal path, [3] max |FP32 - FP64|
- * of type_likely over fixup-checked sites (as raw double bits). */
+ * FP64 fixup, [2] sites whose FP32 likelihood was also summed in FP64 (every
+ * 4096th site), [3] the largest |FP32 - FP64| type_likely difference over
+ * those sites (raw bits of a double). */
 int gsnp_get_stats(gsnp_context* ctx, uint64_t* stats4);
 
 #ifdef __cplusplus

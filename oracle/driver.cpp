@@ -24,6 +24,7 @@
 #include "oracle.h"
 
 #include <getopt.h>
+#include <sys/time.h>
 
 #include <cctype>
 #include <fstream>
@@ -862,7 +863,14 @@ int oracle_main(int argc, char** argv) {
     matrix_file.close();
     prior_gen(para, p_prior.data());
     rank_table_gen(p_rank.data());
+    struct timeval t0, t1;
+    gettimeofday(&t0, nullptr);
     soap2cns(para, rs, &genome, p_matrix.data(), p_prior.data(), p_rank.data(), cns, consensus_name);
     cns.close();
+    gettimeofday(&t1, nullptr);
+    /* wall time of the calling pass (window loop and output), for the CPU
+     * baseline of the benchmark */
+    if (getenv("GSNP_ORACLE_TIMING"))
+        fprintf(stderr, "pass2_seconds=%.6f\n", (t1.tv_sec - t0.tv_sec) + 1e-6 * (t1.tv_usec - t0.tv_usec));
     return 0;
 }

@@ -38,6 +38,30 @@ def test_cns_text_matches_oracle(name, scale, tmp_path, oracle_bin, native_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name,scale", [("c0", 0.1), ("c1", 0.004), ("c2", 0.01), ("c3", 0.004), ("c4", 0.0101)])
+def test_fp32_fixup_form_matches_oracle(name, scale, tmp_path, oracle_bin, native_lib):
+    """FP32 compensated sums with FP64 recomputation near decision boundaries
+    must give the same cns bytes as the FP64 form and the oracle."""
+    w = synth.make_workload(name, scale=scale)
+    paths = synth.write_inputs(w, str(tmp_path))
+    flags = flags_for(w, paths)
+    ref = oracle_outputs(oracle_bin, w, flags, str(tmp_path))
+    assert ref["rc"] == 0, ref["stderr"]
+    c, reads, pm = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
+    try:
+        got = c.format_cns(w.chr_name)
+        stats = c.stats()
+    finally:
+        c.close()
+    if got != ref["cns"]:
+        i, x, y = first_diff(got, ref["cns"])
+        pytest.fail(f"{name}: first differing row {i}:\n gpu   : {x!r}\n oracle: {y!r}")
+    max_err = np.frombuffer(np.uint64(stats[3]).tobytes(), dtype=np.float64)[0]
+    assert max_err < 1e-2, max_err
+    assert stats[1] < w.genome_len // 100, stats[1]
+
+
+@pytest.mark.gpu
 def test_calibration_matrix_matches_oracle(tmp_path, oracle_bin, native_lib):
     w = synth.make_workload("c0", scale=0.05)
     paths = synth.write_inputs(w, str(tmp_path))
