@@ -6,7 +6,9 @@ at 30x (15 M alignments, 1.5e9 bases), dbSNP rows on 1% of sites, flags
 -L 100 -t -u -2 -s.  The inputs are seeded synthetic data of that shape
 (gsnp_gb300.synth), generated on the GPU; there is no public dataset.
 
-A step is one calling pass over the whole chromosome.
+A step is one calling pass over the whole chromosome.  The headline form is
+the FP32 compensated likelihood with FP64 fixup; the plain FP64 form is timed
+beside it in the same run (the "compare" object).
   value : sites/s with the alignments resident in HBM (tile classification and
           the binned calling kernels, CUDA events on the launching stream);
           the alignments (3 GB) exceed L2, so no flush is needed between steps.
@@ -19,7 +21,8 @@ per-read start/length/strand, the 4-bit reference code, a 32-byte call).
 
 --impl reference times the reference's calling algorithm on the host cores:
 the CPU oracle (oracle/, a restatement of the reference's single-threaded
-calling code) on a bounded sample of the same workload.
+calling code) on a bounded sample of the same workload, one process per core.
+The cpu_baseline object of the GPU line is the same code on one core.
 """
 from __future__ import annotations
 
@@ -47,7 +50,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gsnp", "reference"], default="gsnp")
-    ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp32",
+                    help="headline form: fp32 = FP32 compensated sums with FP64 fixup, fp64 = plain FP64")
+    ap.add_argument("--no-compare", action="store_true", help="do not also time the other form")
     ap.add_argument("--scale", type=float, default=1.0, help="genome scale (1.0 = the named 50 Mbp workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -74,6 +79,8 @@ class ClockSampler:
         self.lines = []
 
     def __enter__(self):
+        if self.device < 0:
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
@@ -148,17 +155,33 @@ class OracleSample:
         self.sample = "%d-site c1-shaped sample (%d reads), calling pass (window loop + cns text), 1 thread" % (
             self.w.genome_len, self.w.num_reads)
 
-    def run(self) -> float:
-        d = self.dir.name
+    def start(self, out_dir: str) -> subprocess.Popen:
         env = dict(os.environ, GSNP_ORACLE_TIMING="1")
-        r = subprocess.run([self.oracle, "-i", self.paths["soap"], "-d", self.paths["ref"], "-o",
-                            os.path.join(d, "cns")] + self.flags, cwd=d, env=env, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("oracle failed: " + r.stderr[-500:])
-        for line in r.stderr.splitlines():
+        return subprocess.Popen([self.oracle, "-i", self.paths["soap"], "-d", self.paths["ref"], "-o",
+                                 os.path.join(out_dir, "cns")] + self.flags, cwd=out_dir, env=env,
+                                stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+
+    @staticmethod
+    def seconds(proc: subprocess.Popen) -> float:
+        _, err = proc.communicate()
+        if proc.returncode != 0:
+            raise RuntimeError("oracle failed: " + err[-500:])
+        for line in err.splitlines():
             if line.startswith("pass2_seconds="):
-                return self.w.genome_len / float(line.split("=")[1])
+                return float(line.split("=")[1])
         raise RuntimeError("oracle printed no timing")
+
+    def run(self) -> float:
+        """sites/s of one process (one core)."""
+        return self.w.genome_len / self.seconds(self.start(self.dir.name))
+
+    def run_parallel(self, procs: int) -> float:
+        """Aggregate sites/s of `procs` concurrent processes on the sample,
+        counted against the slowest one."""
+        dirs = [tempfile.mkdtemp(dir=self.dir.name) for _ in range(procs)]
+        running = [self.start(d) for d in dirs]
+        secs = [self.seconds(p) for p in running]
+        return procs * self.w.genome_len / max(secs)
 
 
 def cpu_baseline(sample_len: int):
@@ -166,24 +189,35 @@ def cpu_baseline(sample_len: int):
     return s.run(), s.sample
 
 
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def run_reference(args, rank, world):
+    """The reference's calling code (single-threaded per chromosome) on every
+    host core: one process per core, each calling its own copy of the sample."""
     if rank != 0:
         return
     sample_len = 600_000 if args.scale >= 1.0 else max(40_000, int(600_000 * args.scale))
     smp = OracleSample(sample_len)
+    cores = host_cores()
     vals = []
     for i in range(args.warmup + args.steps):
-        v = smp.run()
+        v = smp.run_parallel(cores)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
+    sample = "%s; %d concurrent processes, one per host core" % (smp.sample.replace(", 1 thread", ""), cores)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sample_len / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * cores * sample_len / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "c1: 50 Mbp, 100 bp reads at 30x, dbSNP 1%, -L 100 -t -u -2 -s",
-                   "sample_sites": sample_len},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp.sample},
+                   "sample_sites": sample_len, "processes": cores},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -207,18 +241,20 @@ def main():
         dist = None
 
     precision = api.PRECISION_FP64 if args.precision == "fp64" else api.PRECISION_FP32_FIXUP
+    other = api.PRECISION_FP32_FIXUP if precision == api.PRECISION_FP64 else api.PRECISION_FP64
     t0 = time.time()
     w = synth.make_workload(CONFIG, scale=args.scale, backend="torch", device="cuda:%d" % local)
     t_gen = time.time() - t0
     flags = w.cli_flags("dbsnp")   # the dbSNP rows are passed in memory
-    p = api.params_from_flags(flags, precision)
     codes = api.site_codes(w.ref, w.db_pos)
     caller = api.Caller(local)
     caller.load_reference(codes, api.snp_table(w))
     arrs = [np.ascontiguousarray(x) for x in (w.pos, w.length, w.hit, w.strand)] + [w.seq, w.qual]
     reads = api.Caller.reads_struct(*arrs)
+    p = api.params_from_flags(flags, precision)
     pm = caller.calibrate(p, reads)
-    caller.load_tables(p, pm, caller.prior_table(p), caller.rank_table())
+    prior, rank_tab = caller.prior_table(p), caller.rank_table()
+    caller.load_tables(p, pm, prior, rank_tab)
     stream = torch.cuda.current_stream()
     caller.set_stream(stream.cuda_stream)
     caller.call(reads)                       # uploads the alignments, first pass
@@ -228,31 +264,42 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    # ---- device-resident timing ----
-    for _ in range(args.warmup):
-        caller.recall_resident()
-    launches_per_step = len(caller.last_launches())
-    barrier()
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kernel_ms = {}
-    with ClockSampler(local) as clocks:
-        start.record(stream)
-        for _ in range(args.steps):
-            caller.recall_resident()
-            for li in caller.last_launches():
-                key = (li["kind"], li["slots"])
-                kernel_ms.setdefault(key, []).append((li["ms"], li["sites"], li["tiles"]))
-        end.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    ms_total = start.elapsed_time(end)
-    if dist is not None:
-        t = torch.tensor([ms_total], device="cuda")
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_step = ms_total / args.steps
-    value = world * sites / (ms_step / 1000.0)
+        return float(t.item())
+
+    def time_form(prec, sample_clocks):
+        """Warm up, then time exactly args.steps device-resident calling passes."""
+        caller.load_tables(api.params_from_flags(flags, prec), pm, prior, rank_tab)
+        for _ in range(args.warmup):
+            caller.recall_resident()
+        n_launch = len(caller.last_launches())
+        barrier()
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kernel_ms = {}
+        with ClockSampler(local if sample_clocks else -1) as clocks:
+            start.record(stream)
+            for _ in range(args.steps):
+                caller.recall_resident()
+                for li in caller.last_launches():
+                    key = (li["kind"], li["slots"])
+                    kernel_ms.setdefault(key, []).append((li["ms"], li["sites"], li["tiles"]))
+            end.record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        ms_step = max_over_ranks(start.elapsed_time(end)) / args.steps
+        return {"ms_step": ms_step, "value": world * sites / (ms_step / 1000.0), "launches": n_launch,
+                "kernel_ms": kernel_ms, "clocks": clocks.summary() if sample_clocks else None,
+                "stats": caller.stats()}
+
+    compare = time_form(other, False) if not args.no_compare else None
+    head = time_form(precision, True)
+    value, ms_step, kernel_ms = head["value"], head["ms_step"], head["kernel_ms"]
+    stats = head["stats"]
 
     # ---- end to end through the C ABI from pinned host buffers ----
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 3)
@@ -267,25 +314,23 @@ def main():
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t1)
     h2d, d2h = caller.transfer_bytes()
-    e2e_s = max(statistics.mean(e2e_times), 1e-9)
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(max(statistics.mean(e2e_times), 1e-9))
     e2e_value = world * sites / e2e_s
-    stats = caller.stats()
 
-    # ---- roofline of the dominant kernel (the calling bin with most device time) ----
+    # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
     bsite = site_bytes(w)
-    dom_key = max((k for k in kernel_ms if k[0] == 1), key=lambda k: sum(x[0] for x in kernel_ms[k]))
+    names = {1: "call_tiles_kernel", 2: "call_fast_kernel", 3: "call_tiles_kernel(deferred)"}
+    dom_key = max((k for k in kernel_ms if k[0] in (1, 2)), key=lambda k: sum(x[0] for x in kernel_ms[k]))
     dom = kernel_ms[dom_key]
     dom_ms = statistics.mean(x[0] for x in dom)
     dom_sites = dom[0][1]
     achieved = bsite * dom_sites / (dom_ms / 1000.0) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    kernels = {("classify" if k[0] == 0 else "call_%d" % k[1]): round(statistics.mean(x[0] for x in v), 4)
-               for k, v in kernel_ms.items()}
+
+    def kernel_table(km):
+        return {("classify" if k[0] == 0 else "%s<%d>" % (names[k[0]], k[1])):
+                round(statistics.mean(x[0] for x in v), 4) for k, v in sorted(km.items())}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -310,16 +355,22 @@ def main():
             "bases_per_s": value * depth,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps},
-            "gpu_launches": launches_per_step * args.steps,
-            "kernels_ms": kernels,
+            "gpu_launches": head["launches"] * args.steps,
+            "kernels_ms": kernel_table(kernel_ms),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "call_tiles_kernel<%d>" % dom_key[1], "sites_per_launch": dom_sites,
+                         "kernel": "%s<%d>" % (names[dom_key[0]], dom_key[1]), "sites_per_launch": dom_sites,
                          "bytes_per_site": bsite, "peak_source": peak_kind},
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
-            "stats": {"fixup_sites": int(stats[1]), "normal_path_sites": int(stats[2])},
+            "clocks": head["clocks"],
+            "stats": stats,
         }
+        if compare is not None:
+            line["compare"] = {
+                "form": "fp64 plain" if other == api.PRECISION_FP64 else "fp32+fp64 fixup",
+                "value": compare["value"], "ms_per_step": compare["ms_step"],
+                "bases_per_s": compare["value"] * depth, "kernels_ms": kernel_table(compare["kernel_ms"]),
+                "speedup_of_headline": value / compare["value"]}
         print(json.dumps(line), flush=True)
     caller.close()
     if dist is not None:

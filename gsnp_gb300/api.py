@@ -83,7 +83,7 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_recall_resident": (ctypes.c_int, [_P]),
         "gsnp_fetch_sites": (ctypes.c_int, [_P, _I64, _I64, _P]),
         "gsnp_format_cns": (ctypes.c_int, [_P, ctypes.c_char_p, _P, ctypes.POINTER(_I64)]),
-        "gsnp_get_stats": (ctypes.c_int, [_P, _P]),
+        "gsnp_get_stats": (ctypes.c_int, [_P, _P, ctypes.c_int]),
         "gsnp_last_launches": (ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_int)]),
         "gsnp_transfer_bytes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     }
@@ -258,21 +258,29 @@ class Caller:
         return buf.raw[:size.value]
 
     def last_launches(self) -> List[dict]:
-        n = ctypes.c_int(16)
-        arr = (LaunchInfo * 16)()
+        n = ctypes.c_int(32)
+        arr = (LaunchInfo * 32)()
         self._check(self.lib.gsnp_last_launches(self.ctx, arr, ctypes.byref(n)), "gsnp_last_launches")
         return [dict(kind=arr[i].kind, slots=arr[i].slots, tiles=arr[i].tiles, sites=arr[i].sites, ms=arr[i].ms)
-                for i in range(min(n.value, 16))]
+                for i in range(min(n.value, len(arr)))]
 
     def transfer_bytes(self):
         h, d = ctypes.c_uint64(), ctypes.c_uint64()
         self._check(self.lib.gsnp_transfer_bytes(self.ctx, ctypes.byref(h), ctypes.byref(d)), "gsnp_transfer_bytes")
         return h.value, d.value
 
-    def stats(self) -> np.ndarray:
-        out = np.zeros(4, dtype=np.uint64)
-        self._check(self.lib.gsnp_get_stats(self.ctx, out.ctypes.data), "gsnp_get_stats")
-        return out
+    def stats(self) -> dict:
+        """Diagnostics of the last call (gsnp_get_stats)."""
+        out = np.zeros(8, dtype=np.uint64)
+        self._check(self.lib.gsnp_get_stats(self.ctx, out.ctypes.data, 8), "gsnp_get_stats")
+        return {
+            "sites": int(out[0]),
+            "fixup_sites": int(out[1]),
+            "sampled_sites": int(out[2]),
+            "max_abs_err": float(np.frombuffer(out[3].tobytes(), dtype=np.float64)[0]),
+            "deferred_sites": int(out[4]),
+            "sample_mismatches": int(out[5]),
+        }
 
 
 def snp_table(w) -> np.ndarray:

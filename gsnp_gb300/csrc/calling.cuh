@@ -10,9 +10,20 @@
 
 namespace gsnp {
 
+constexpr int kNumStats = 8;
+
 constexpr int kTile = 128;        /* sites per tile (divides the window) */
+constexpr int kWarpsPerTile = kTile / 32;
 constexpr int kMaxStagedReads = 2048;
 constexpr int kNumBins = 4;       /* record slots 32 / 64 / 128 / 256 */
+
+/* calling kernels */
+enum CallKind : int {
+    kKindClassify = 0,
+    kKindFP64 = 1,      /* FP64 likelihood, every site of the tile */
+    kKindFast = 2,      /* FP32 likelihood and posterior, hard sites deferred */
+    kKindDeferred = 3,  /* the FP64 kernel over the deferred sites of a tile */
+};
 
 /* per-window calling mode, decided by the host replay of the reference's
  * window loop (cpp/call_genotype.cc:422-669) */
@@ -36,6 +47,7 @@ struct CallArgs {
     const DbSnpEntry* snp;       /* sorted by position */
     int64_t n_snp;
     const double* snp_lp;        /* [n_snp][16] log10 prior of each dbSNP site (refine mode) */
+    const float* snp_lp32;       /* [n_snp][12] the same in FP32, by table column */
     /* tables */
     const double* lik64;         /* [qa_rows][L][4][10] log10 genotype terms */
     const float* lik32;          /* same, rounded to FP32 */
@@ -44,6 +56,7 @@ struct CallArgs {
     int tmax, gmax;
     const double* p_prior;       /* [8][16] */
     const double* log_prior;     /* [8][16] correctly rounded log10 of p_prior */
+    const float* log_prior32;    /* [8][12] the same in FP32, by table column */
     const double* p_rank;        /* 64 x 64 x 2048 */
     /* parameters */
     int qmin;                    /* as a signed char */
@@ -54,12 +67,17 @@ struct CallArgs {
     /* windows */
     const uint8_t* win_flags;    /* per window */
     const int32_t* win_lik_src;  /* per window: window whose likelihood is used (-1: zeros) */
+    /* tiles */
+    int64_t n_tiles;
+    int64_t* warp_rng;           /* [n_tiles][4][2]: reads that can cover each warp's 32 sites */
+    int* fix_count;              /* [kNumBins] tiles with deferred sites, per bin */
+    int32_t* fix_tiles;          /* [kNumBins][n_tiles] */
     /* outputs */
     SiteCall* out;               /* [chr_len] */
     SiteCounts* counts;          /* [chr_len] or null */
     double* lik_keep;            /* [chr_len][10] or null */
     float* lik_err;              /* optional: max |FP32 - FP64| per tile (diagnostics) */
-    unsigned long long* stats;   /* [4]: fixup sites, normal-path sites, ... */
+    unsigned long long* stats;   /* [kNumStats], see gsnp_get_stats */
     int* error;                  /* nonzero on a capacity overflow */
 };
 

@@ -29,10 +29,10 @@
 
 namespace gsnp {
 
-cudaError_t launch_classify(const CallArgs& a, int pass, int64_t n_tiles, int* d_bin_count, int32_t* d_bin_tiles,
-                            cudaStream_t stream);
-cudaError_t launch_bin(const CallArgs& a, int bin, const int32_t* tiles, int count, cudaStream_t stream);
-cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, cudaStream_t stream);
+cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32_t* d_bin_tiles, cudaStream_t stream);
+cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
+cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
+int bin_slots(int bin);
 
 /* ---- device helpers ---- */
 
@@ -136,6 +136,7 @@ struct gsnp_context {
     uint8_t* d_qadj = nullptr;
     double* d_p_prior = nullptr;
     double* d_log_prior = nullptr;
+    float* d_log_prior32 = nullptr;
     double* d_p_rank = nullptr;
     /* reference */
     int64_t chr_len = 0;
@@ -144,6 +145,7 @@ struct gsnp_context {
     DbSnpEntry* d_snp = nullptr;
     int64_t n_snp = 0;
     double* d_snp_lp = nullptr;
+    float* d_snp_lp32 = nullptr;
     bool snp_lp_ready = false;
     /* resident reads (deposited, packed) */
     int64_t n_dep = 0;
@@ -167,14 +169,18 @@ struct gsnp_context {
     /* scratch */
     int* d_error = nullptr;
     unsigned long long* d_stats = nullptr;
-    int* d_bin_count = nullptr;
-    int32_t* d_bin_tiles = nullptr;
-    int64_t bin_tiles_cap = 0;
-    int h_bin_count[kNumBins] = {0, 0, 0, 0};
+    int* d_bin_count = nullptr;     /* [2 * kNumBins] FP64 bins, then fast bins */
+    int32_t* d_bin_tiles = nullptr; /* [2 * kNumBins][n_tiles] */
+    int* d_fix_count = nullptr;     /* [kNumBins] tiles with deferred sites */
+    int32_t* d_fix_tiles = nullptr; /* [kNumBins][n_tiles] */
+    int64_t* d_warp_rng = nullptr;  /* [n_tiles][4][2] */
+    int64_t tiles_cap = 0;
+    int h_bin_count[2 * kNumBins] = {};
+    int h_fix_count[kNumBins] = {};
     bool called = false;
-    uint64_t stats[4] = {0, 0, 0, 0};
+    uint64_t stats[kNumStats] = {};
     /* CUDA events around each launch of the last calling pass */
-    static const int kMaxLaunches = 16;
+    static const int kMaxLaunches = 32;
     cudaEvent_t ev[2 * kMaxLaunches] = {};
     gsnp_launch_info launches[kMaxLaunches];
     int n_launches = 0;
@@ -207,10 +213,11 @@ cudaError_t dev_alloc(T** p, size_t count) {
 }
 
 void free_all(gsnp_context* c) {
-    void* ptrs[] = {c->d_lik64, c->d_lik32, c->d_qadj, c->d_p_prior, c->d_log_prior, c->d_p_rank,
-                    c->d_codes, c->d_snp, c->d_snp_lp, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq,
-                    c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts, c->d_lik_keep,
-                    c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles};
+    void* ptrs[] = {c->d_lik64, c->d_lik32, c->d_qadj, c->d_p_prior, c->d_log_prior, c->d_log_prior32,
+                    c->d_p_rank, c->d_codes, c->d_snp, c->d_snp_lp, c->d_snp_lp32, c->d_pos, c->d_lenhit,
+                    c->d_len, c->d_strand, c->d_bq, c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts,
+                    c->d_lik_keep, c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles, c->d_fix_count,
+                    c->d_fix_tiles, c->d_warp_rng};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -229,6 +236,7 @@ CallArgs make_args(gsnp_context* c) {
     a.snp = c->d_snp;
     a.n_snp = c->n_snp;
     a.snp_lp = c->d_snp_lp;
+    a.snp_lp32 = c->d_snp_lp32;
     a.lik64 = c->d_lik64;
     a.lik32 = c->d_lik32;
     a.qa_rows = c->tables.qa_rows;
@@ -237,6 +245,7 @@ CallArgs make_args(gsnp_context* c) {
     a.gmax = c->tables.gmax;
     a.p_prior = c->d_p_prior;
     a.log_prior = c->d_log_prior;
+    a.log_prior32 = c->d_log_prior32;
     a.p_rank = c->d_p_rank;
     a.qmin = c->params.q_min;
     a.q_max_min = (int)(signed char)(c->params.q_max - c->params.q_min);
@@ -251,6 +260,10 @@ CallArgs make_args(gsnp_context* c) {
     a.precision = c->tables.all_nonpositive ? c->params.precision : GSNP_PRECISION_FP64;
     a.win_flags = c->d_win_flags;
     a.win_lik_src = c->d_win_lik_src;
+    a.n_tiles = (c->chr_len + kTile - 1) / kTile;
+    a.warp_rng = c->d_warp_rng;
+    a.fix_count = c->d_fix_count;
+    a.fix_tiles = c->d_fix_tiles;
     a.out = c->d_out;
     a.counts = c->d_counts;
     a.lik_keep = c->d_lik_keep;
@@ -263,22 +276,24 @@ int run_calling(gsnp_context* c) {
     const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
     if (!c->snp_lp_ready) {
         CK(dev_alloc(&c->d_snp_lp, (size_t)std::max<int64_t>(c->n_snp, 1) * 16), "cudaMalloc dbSNP priors");
+        CK(dev_alloc(&c->d_snp_lp32, (size_t)std::max<int64_t>(c->n_snp, 1) * 12), "cudaMalloc dbSNP priors");
         const CallArgs a0 = make_args(c);
-        CK(launch_snp_log_prior(a0, c->d_snp_lp, c->stream), "dbSNP prior kernel");
+        CK(launch_snp_log_prior(a0, c->d_snp_lp, c->d_snp_lp32, c->stream), "dbSNP prior kernel");
         c->snp_lp_ready = true;
     }
-    if (n_tiles > c->bin_tiles_cap) {
-        CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * kNumBins), "cudaMalloc bins");
-        c->bin_tiles_cap = n_tiles;
+    if (n_tiles > c->tiles_cap) {
+        CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * 2 * kNumBins), "cudaMalloc bins");
+        CK(dev_alloc(&c->d_fix_tiles, (size_t)n_tiles * kNumBins), "cudaMalloc bins");
+        CK(dev_alloc(&c->d_warp_rng, (size_t)n_tiles * kWarpsPerTile * 2), "cudaMalloc ranges");
+        c->tiles_cap = n_tiles;
     }
     if (!c->ev[0])
         for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i) CK(cudaEventCreate(&c->ev[i]), "cudaEventCreate");
     CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
-    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4, c->stream), "memset");
+    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * kNumStats, c->stream), "memset");
     const CallArgs a = make_args(c);
     bool any_external = false;
     for (int64_t w = 0; w < c->plan.n_windows; ++w) any_external |= (c->plan.flags[w] & kWinExternalLik) != 0;
-    static const int slots[kNumBins] = {32, 64, 128, 256};
     c->n_launches = 0;
     auto begin = [&](int kind, int sl, int64_t tiles) -> int {
         if (c->n_launches >= gsnp_context::kMaxLaunches) return -1;
@@ -295,16 +310,36 @@ int run_calling(gsnp_context* c) {
         if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], c->stream);
     };
     for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
-        int k = begin(0, 0, n_tiles);
-        CK(launch_classify(a, pass, n_tiles, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
+        int k = begin(kKindClassify, 0, n_tiles);
+        CK(launch_classify(a, pass, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
         end(k);
-        CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(int) * kNumBins, cudaMemcpyDeviceToHost, c->stream),
+        CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(c->h_bin_count), cudaMemcpyDeviceToHost,
+                           c->stream),
            "bin counts");
         CK(cudaStreamSynchronize(c->stream), "classify");
-        for (int b = 0; b < kNumBins; ++b) {
+        bool any_fast = false;
+        for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
+        if (any_fast) CK(cudaMemsetAsync(c->d_fix_count, 0, sizeof(int) * kNumBins, c->stream), "memset");
+        for (int b = 0; b < 2 * kNumBins; ++b) {
             if (c->h_bin_count[b] == 0) continue;
-            k = begin(1, slots[b], c->h_bin_count[b]);
-            CK(launch_bin(a, b, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b], c->stream), "calling kernel");
+            const int kind = b < kNumBins ? kKindFP64 : kKindFast;
+            k = begin(kind, bin_slots(b % kNumBins), c->h_bin_count[b]);
+            CK(launch_bin(a, kind, b % kNumBins, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b],
+                          c->stream),
+               "calling kernel");
+            end(k);
+        }
+        if (!any_fast) continue;
+        /* the FP64 pass over the tiles whose sites the fast kernel deferred */
+        CK(cudaMemcpyAsync(c->h_fix_count, c->d_fix_count, sizeof(c->h_fix_count), cudaMemcpyDeviceToHost,
+                           c->stream),
+           "deferred counts");
+        CK(cudaStreamSynchronize(c->stream), "fast calling");
+        for (int b = 0; b < kNumBins; ++b) {
+            if (c->h_fix_count[b] == 0) continue;
+            k = begin(kKindDeferred, bin_slots(b), c->h_fix_count[b]);
+            CK(launch_bin(a, kKindDeferred, b, c->d_fix_tiles + (int64_t)b * n_tiles, c->h_fix_count[b], c->stream),
+               "deferred calling kernel");
             end(k);
         }
     }
@@ -313,7 +348,8 @@ int run_calling(gsnp_context* c) {
     CK(cudaMemcpyAsync(c->stats, c->d_stats, sizeof(c->stats), cudaMemcpyDeviceToHost, c->stream), "stats");
     CK(cudaStreamSynchronize(c->stream), "calling");
     for (int k = 0; k < c->n_launches; ++k) cudaEventElapsedTime(&c->launches[k].ms, c->ev[2 * k], c->ev[2 * k + 1]);
-    if (err) return fail(c, GSNP_ERR_CAPACITY, "a site's count_all exceeds 65535");
+    if (err == 1) return fail(c, GSNP_ERR_CAPACITY, "a site's count_all exceeds 65535");
+    if (err) return fail(c, GSNP_ERR_STATE, "record slots of a tile overflowed its depth bin");
     c->stats[0] = (uint64_t)c->chr_len;
     c->called = true;
     return GSNP_OK;
@@ -331,8 +367,9 @@ int gsnp_context_create(int device, gsnp_context** out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_error, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_stats, sizeof(unsigned long long) * 4);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bin_count, sizeof(int) * kNumBins);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_stats, sizeof(unsigned long long) * kNumStats);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bin_count, sizeof(int) * 2 * kNumBins);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_fix_count, sizeof(int) * kNumBins);
     if (e != cudaSuccess) {
         free_all(c);
         delete c;
@@ -381,12 +418,14 @@ int gsnp_load_tables(gsnp_context* c, const gsnp_params* p, const double* p_matr
     CK(dev_alloc(&c->d_qadj, t.qadj.size()), "cudaMalloc");
     CK(dev_alloc(&c->d_p_prior, 128), "cudaMalloc");
     CK(dev_alloc(&c->d_log_prior, 128), "cudaMalloc");
+    CK(dev_alloc(&c->d_log_prior32, 96), "cudaMalloc");
     CK(dev_alloc(&c->d_p_rank, 64UL * 64UL * 2048UL), "cudaMalloc");
     CK(cudaMemcpy(c->d_lik64, t.lik64.data(), t.lik64.size() * 8, cudaMemcpyHostToDevice), "upload");
     CK(cudaMemcpy(c->d_lik32, t.lik32.data(), t.lik32.size() * 4, cudaMemcpyHostToDevice), "upload");
     CK(cudaMemcpy(c->d_qadj, t.qadj.data(), t.qadj.size(), cudaMemcpyHostToDevice), "upload");
     CK(cudaMemcpy(c->d_p_prior, p_prior, 128 * 8, cudaMemcpyHostToDevice), "upload");
     CK(cudaMemcpy(c->d_log_prior, t.log_prior.data(), 128 * 8, cudaMemcpyHostToDevice), "upload");
+    CK(cudaMemcpy(c->d_log_prior32, t.log_prior32.data(), 96 * 4, cudaMemcpyHostToDevice), "upload");
     CK(cudaMemcpy(c->d_p_rank, p_rank, 64UL * 64UL * 2048UL * 8, cudaMemcpyHostToDevice), "upload");
     c->have_tables = true;
     c->snp_lp_ready = false;
@@ -598,9 +637,9 @@ int gsnp_transfer_bytes(gsnp_context* c, uint64_t* h2d, uint64_t* d2h) {
     return GSNP_OK;
 }
 
-int gsnp_get_stats(gsnp_context* c, uint64_t* s) {
-    if (!c || !s) return GSNP_ERR_ARG;
-    memcpy(s, c->stats, sizeof(c->stats));
+int gsnp_get_stats(gsnp_context* c, uint64_t* s, int n) {
+    if (!c || !s || n < 0) return GSNP_ERR_ARG;
+    for (int i = 0; i < n; ++i) s[i] = i < kNumStats ? c->stats[i] : 0;
     return GSNP_OK;
 }
 

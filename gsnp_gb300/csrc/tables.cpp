@@ -87,7 +87,9 @@ int build_tables(const gsnp_params& p, const double* pm, const double* p_prior, 
                         const double x = pm[((unsigned long)q << 12) | ((unsigned long)c << 4) | (a1 << 2) | o];
                         const double y = pm[((unsigned long)q << 12) | ((unsigned long)c << 4) | (a2 << 2) | o];
                         row[k] = log10(0.5 * x + 0.5 * y);
-                        if (!(row[k] <= 0.0)) t->all_nonpositive = false;
+                        /* the FP32 error bound is relative: every term must be
+                         * <= 0 and round to 0 or to a normal FP32 number */
+                        if (!(row[k] <= 0.0) || (row[k] < 0.0 && row[k] > -0x1p-126)) t->all_nonpositive = false;
                         ++k;
                     }
             }
@@ -97,6 +99,10 @@ int build_tables(const gsnp_params& p, const double* pm, const double* p_prior, 
 
     t->log_prior.resize(128);
     for (int i = 0; i < 128; ++i) t->log_prior[i] = gsnp_cr_log10(p_prior[i]);
+    static const int col_genotype[10] = {0, 1, 2, 3, 5, 6, 7, 10, 11, 15};
+    t->log_prior32.assign(8 * 12, 0.0f);
+    for (int r = 0; r < 8; ++r)
+        for (int k = 0; k < 10; ++k) t->log_prior32[r * 12 + k] = (float)t->log_prior[r * 16 + col_genotype[k]];
     return 0;
 }
 

@@ -21,7 +21,8 @@ struct HostTables {
     std::vector<float> lik32;       /* [qa_rows][L][4][12], FP32, rows padded to 12 */
     std::vector<uint8_t> qadj;      /* [tmax][gmax][65] */
     std::vector<double> log_prior;  /* [128] correctly rounded log10 of p_prior */
-    bool all_nonpositive = true;    /* every lik64 entry <= 0 */
+    std::vector<float> log_prior32; /* [8][12] log_prior in FP32 by table column */
+    bool all_nonpositive = true;    /* every lik64 entry <= 0, none of them an FP32 subnormal */
 };
 
 /* Tables of the likelihood and posterior kernels, built from the reference's

@@ -146,7 +146,8 @@ int gsnp_format_cns(gsnp_context* ctx, const char* chr_name, char* buf, int64_t*
 /* One kernel launch of the last calling pass, timed with CUDA events on the
  * context's stream. */
 typedef struct gsnp_launch_info {
-    int kind;          /* 0: tile classification, 1: calling kernel of one depth bin */
+    int kind;          /* 0: tile classification; calling kernel of one depth bin: 1 FP64,
+                          2 FP32 fast form, 3 FP64 pass over the fast form's deferred sites */
     int slots;         /* record slots per site of the bin (calling kernels) */
     int64_t tiles;     /* 128-site tiles processed */
     int64_t sites;
@@ -161,11 +162,18 @@ int gsnp_last_launches(gsnp_context* ctx, gsnp_launch_info* out, int* n);
  * bytes fetched since then. */
 int gsnp_transfer_bytes(gsnp_context* ctx, uint64_t* h2d, uint64_t* d2h);
 
-/* Diagnostics of the last call: [0] sites called, [1] sites that took the
- * FP64 fixup, [2] sites whose FP32 likelihood was also summed in FP64 (every
- * 4096th site), [3] the largest |FP32 - FP64| type_likely difference over
- * those sites (raw bits of a double). */
-int gsnp_get_stats(gsnp_context* ctx, uint64_t* stats4);
+/* Diagnostics of the last call, n entries:
+ *   [0] sites called
+ *   [1] sites whose FP32 likelihood was recomputed in FP64 (fixups)
+ *   [2] sites whose FP32 likelihood was also summed in FP64 (every 4096th)
+ *   [3] the largest |FP32 - FP64| type_likely difference over those sites
+ *       (raw bits of a double)
+ *   [4] sites the FP32 kernel deferred to the FP64 pass (heterozygous calls,
+ *       which need the FP64 rank-sum, and calls its FP32 bounds did not prove)
+ *   [5] sampled sites whose FP32-kernel call differs from the FP64 call
+ *       (always 0 unless the error bound is wrong)
+ *   [6], [7] reserved, 0 */
+int gsnp_get_stats(gsnp_context* ctx, uint64_t* stats, int n);
 
 #ifdef __cplusplus
 }

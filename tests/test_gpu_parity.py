@@ -56,9 +56,35 @@ def test_fp32_fixup_form_matches_oracle(name, scale, tmp_path, oracle_bin, nativ
     if got != ref["cns"]:
         i, x, y = first_diff(got, ref["cns"])
         pytest.fail(f"{name}: first differing row {i}:\n gpu   : {x!r}\n oracle: {y!r}")
-    max_err = np.frombuffer(np.uint64(stats[3]).tobytes(), dtype=np.float64)[0]
-    assert max_err < 1e-2, max_err
-    assert stats[1] < w.genome_len // 100, stats[1]
+    assert stats["sample_mismatches"] == 0, stats
+    assert stats["sampled_sites"] > 0, stats
+    assert stats["max_abs_err"] < 1e-2, stats
+    assert stats["fixup_sites"] < w.genome_len // 100, stats
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,scale", [("c1", 0.05), ("c2", 0.05), ("c3", 0.05)])
+def test_fp32_form_equals_fp64_form(name, scale, native_lib):
+    """At sizes beyond the oracle's: every site call of the FP32 form equals
+    the FP64 form's, field for field."""
+    w = synth.make_workload(name, scale=scale)
+    flags = flags_for(w, {"ref": "ref.fa", "soap": "in.soap", "dbsnp": "db.txt"})
+    out = {}
+    for prec in (api.PRECISION_FP64, api.PRECISION_FP32_FIXUP):
+        c, reads, pm = api.run_workload(w, flags, precision=prec)
+        try:
+            calls = c.fetch(0, w.genome_len)
+            out[prec] = (calls, c.stats())
+        finally:
+            c.close()
+    a, b = out[api.PRECISION_FP64][0].copy(), out[api.PRECISION_FP32_FIXUP][0].copy()
+    a["flags"] = 0
+    b["flags"] = 0
+    bad = np.nonzero(a != b)[0]
+    assert bad.size == 0, f"{bad.size} sites differ, first {bad[:5]}"
+    st = out[api.PRECISION_FP32_FIXUP][1]
+    assert st["sample_mismatches"] == 0, st
+    assert st["deferred_sites"] < w.genome_len // 10, st
 
 
 @pytest.mark.gpu
