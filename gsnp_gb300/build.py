@@ -1,7 +1,11 @@
-"""Build the native library libgsnp_gb300.so (sm_103a kernels + host code).
+"""Build the native libraries (sm_103a kernels + host code).
 
 Every translation unit is compiled in parallel into gsnp_gb300/_build/ and
-linked into gsnp_gb300/_lib/libgsnp_gb300.so with a static CUDA runtime.
+linked with a static CUDA runtime into
+  gsnp_gb300/_lib/libgsnp_gb300.so   the C ABI of include/gsnp_gb300.h;
+  gsnp_gb300/_lib/libgsnp_backend.so the reference's C++ backend functions
+                                     (include/gsnp_backend.h) for host code
+                                     written against them.
 Floating point is pinned: device code with --fmad=false (no fused
 multiply-add the source does not spell out), host code with
 -ffp-contract=off.
@@ -20,6 +24,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgsnp_gb300.so")
+BACKEND_LIB = os.path.join(LIBDIR, "libgsnp_backend.so")
+# translation units of each library
+BACKEND_ONLY = {"compat.cu"}
+BACKEND_UNITS = {"compat.cu", "dict.cu", "tables.cpp"}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -87,11 +95,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 failed.append(cmd[-3])
     if failed:
         raise RuntimeError("compilation failed: " + ", ".join(failed))
-    if force or jobs or not os.path.exists(LIB):
-        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    for lib, units in ((LIB, [o for o in objs if os.path.basename(o)[:-2] not in BACKEND_ONLY]),
+                       (BACKEND_LIB, [o for o in objs if os.path.basename(o)[:-2] in BACKEND_UNITS])):
+        if force or jobs or not os.path.exists(lib):
+            cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", lib] + units
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     return LIB
 
 

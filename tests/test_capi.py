@@ -28,18 +28,39 @@ def test_library_exports_header_symbols(native_lib):
     assert not missing, missing
 
 
-def test_library_exports_reference_backend_symbols(native_lib):
-    """The 20 C++ entry points the reference's host objects link against."""
-    out = subprocess.run(["nm", "-DC", "--defined-only", native_lib], capture_output=True, text=True).stdout
-    want = ["GPUInit()", "GSNPKernelInit(", "cuda_init(", "cuda_updateSparse(", "cuda_likelihoodSparse(",
-            "cuda_posterior(", "cuda_recycle(", "cuda_quickRecycle(", "gold_pos_match(", "getNumBinWord(",
-            "encode(", "decode(", "dictComprStart(", "dictComprEnd()", "cuda_dictCompression(unsigned int*, unsigned long*, char*",
-            "cuda_dictCompression(unsigned int*, unsigned long*, int*", "cuda_dictCompression(unsigned int*, unsigned long*, unsigned int*",
-            "cuda_dictCompression(unsigned int*, unsigned long*, double*", "RLECompression(int*", "RLECompression(double*"]
-    if "GPUInit()" not in out:
-        pytest.skip("reference-compatible backend not built into this library")
-    for w in want:
-        assert w in out, w
+BACKEND_SYMBOLS = [
+    "GPUInit()", "GSNPKernelInit(", "cuda_init(", "cuda_updateSparse(", "cuda_likelihoodSparse(",
+    "cuda_posterior(", "cuda_recycle(", "cuda_quickRecycle(", "gold_pos_match(", "getNumBinWord(",
+    "encode(", "decode(", "dictComprStart(", "dictComprEnd()",
+    "cuda_dictCompression(unsigned int*, unsigned long*, char*",
+    "cuda_dictCompression(unsigned int*, unsigned long*, int*",
+    "cuda_dictCompression(unsigned int*, unsigned long*, unsigned int*",
+    "cuda_dictCompression(unsigned int*, unsigned long*, double*",
+    "RLECompression(int*", "RLECompression(double*", "RLECompression(char*"]
+
+
+def test_backend_library_exports_reference_symbols(native_lib):
+    """The 20 C++ entry points (with overloads) the reference's host objects link against."""
+    from gsnp_gb300 import build
+    out = subprocess.run(["nm", "-DC", "--defined-only", build.BACKEND_LIB], capture_output=True, text=True).stdout
+    exported = [ln.split(" T ", 1)[1] for ln in out.splitlines() if " T " in ln]
+    for w in BACKEND_SYMBOLS:
+        assert any(e.startswith(w) for e in exported), w
+    # the C ABI library does not export the reference's C++ names
+    out2 = subprocess.run(["nm", "-DC", "--defined-only", native_lib], capture_output=True, text=True).stdout
+    assert "GPUInit()" not in out2
+
+
+def test_reference_host_objects_link_against_backend(native_lib):
+    """The reference's own host objects (compiled in place from its sources)
+    link against libgsnp_backend.so with no unresolved symbol."""
+    ref = os.environ.get("GSNP_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "cpp")):
+        pytest.skip("reference sources not present")
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref-link", "REF=" + ref],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "gsnp_ref_gpu"))
 
 
 def test_host_tables_without_gpu(native_lib):
