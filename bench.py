@@ -320,7 +320,7 @@ def main():
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
     bsite = site_bytes(w)
-    names = {1: "call_tiles_kernel", 2: "call_fast_kernel", 3: "call_tiles_kernel(deferred)"}
+    names = {1: "call_tiles_kernel", 2: "call_fast_kernel", 3: "deferred_sites_kernel"}
     dom_key = max((k for k in kernel_ms if k[0] in (1, 2)), key=lambda k: sum(x[0] for x in kernel_ms[k]))
     dom = kernel_ms[dom_key]
     dom_ms = statistics.mean(x[0] for x in dom)
@@ -329,8 +329,11 @@ def main():
     peak = float(peaks.get("hbm_gbs", 6800.0))
 
     def kernel_table(km):
-        return {("classify" if k[0] == 0 else "%s<%d>" % (names[k[0]], k[1])):
-                round(statistics.mean(x[0] for x in v), 4) for k, v in sorted(km.items())}
+        def name(k):
+            if k[0] == 0:
+                return "classify"
+            return names[k[0]] if k[0] == 3 else "%s<%d>" % (names[k[0]], k[1])
+        return {name(k): round(statistics.mean(x[0] for x in v), 4) for k, v in sorted(km.items())}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

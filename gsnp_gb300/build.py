@@ -5,7 +5,9 @@ linked with a static CUDA runtime into
   gsnp_gb300/_lib/libgsnp_gb300.so   the C ABI of include/gsnp_gb300.h;
   gsnp_gb300/_lib/libgsnp_backend.so the reference's C++ backend functions
                                      (include/gsnp_backend.h) for host code
-                                     written against them.
+                                     written against them;
+  gsnp_gb300/_lib/gsnp               the command-line caller (cli.cpp) over
+                                     the C ABI.
 Floating point is pinned: device code with --fmad=false (no fused
 multiply-add the source does not spell out), host code with
 -ffp-contract=off.
@@ -28,6 +30,8 @@ BACKEND_LIB = os.path.join(LIBDIR, "libgsnp_backend.so")
 # translation units of each library
 BACKEND_ONLY = {"compat.cu"}
 BACKEND_UNITS = {"compat.cu", "dict.cu", "tables.cpp"}
+CLI_UNIT = "cli.cpp"
+CLI = os.path.join(LIBDIR, "gsnp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -95,13 +99,20 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 failed.append(cmd[-3])
     if failed:
         raise RuntimeError("compilation failed: " + ", ".join(failed))
-    for lib, units in ((LIB, [o for o in objs if os.path.basename(o)[:-2] not in BACKEND_ONLY]),
-                       (BACKEND_LIB, [o for o in objs if os.path.basename(o)[:-2] in BACKEND_UNITS])):
+    lib_objs = [o for o in objs if os.path.basename(o)[:-2] != CLI_UNIT]
+    for lib, units in ((LIB, [o for o in lib_objs if os.path.basename(o)[:-2] not in BACKEND_ONLY]),
+                       (BACKEND_LIB, [o for o in lib_objs if os.path.basename(o)[:-2] in BACKEND_UNITS])):
         if force or jobs or not os.path.exists(lib):
             cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", lib] + units
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    cli_obj = os.path.join(BUILD, CLI_UNIT + ".o")
+    if force or _newer(CLI, [cli_obj, LIB]):
+        cmd = ["g++", "-o", CLI, cli_obj, "-L" + LIBDIR, "-lgsnp_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     return LIB
 
 

@@ -23,13 +23,16 @@
  * read's row is read with one coalesced load per lane band.
  *
  * Two calling kernels share this structure:
- *   call_tiles_kernel  FP64 sums in the reference's order (the plain form);
- *                      also the second pass of the fast form over the sites
- *                      that form deferred;
+ *   call_tiles_kernel  FP64 sums in the reference's order (the plain form, and
+ *                      windows whose likelihood another window reuses);
  *   call_fast_kernel   FP32 compensated sums and an FP32 posterior for
  *                      homozygous calls that the error bound proves; every
- *                      other site is marked and its tile listed for the FP64
- *                      pass.  It runs no FP64 instruction.
+ *                      other site is deferred: its counts and sorted records
+ *                      are appended to a small pool.  It runs no FP64
+ *                      instruction.
+ *   deferred_sites_kernel  one thread per deferred site: the FP32 sums again
+ *                      with the double-precision bound checks, the FP64 sums
+ *                      where those fail, the rank-sum test.
  * Tiles are binned by their deepest site (kNumBins record-slot capacities) so
  * that shared memory is sized for the tile, not for the worst case.
  */
@@ -61,17 +64,21 @@ __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v)
  * that the column stays in ascending order.  Lanes with !active only keep the
  * warp's loop going. */
 template <int SLOTS>
-__device__ __forceinline__ void warp_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site, bool active,
-                                            uint32_t* recs, SitePileup& p) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) { p.cu[i] = 0; p.qs[i] = 0; p.ca[i] = 0; }
-    p.depth = 0;
-    p.repeat = 0;
-    p.dep_uni = 0;
-    p.num = 0;
+__device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
+                                                   bool active, uint32_t* recs) {
+    /* records are appended in pileup order, then each lane sorts its own
+     * column once: the lanes of a warp then diverge over one sort each rather
+     * than over every insertion */
     const int lane = threadIdx.x & 31;
     const int L = a.L;
     const signed char qmin = (signed char)a.qmin;
+    /* per-base counters packed: count_uni 4 x 8 bits (at most 255 unique
+     * bases), q_sum and count_all 4 x 16 bits (a site deeper than 65535 is a
+     * capacity error) */
+    uint32_t cu4 = 0;
+    uint64_t qs4 = 0, ca4 = 0;
+    uint32_t depth = 0, repeat = 0;
+    int dep_uni = 0, num = 0;
     bool overflow = false;
     for (int64_t rb = r_lo; rb < r_hi; rb += 32) {
         const int64_t r = rb + lane;
@@ -84,6 +91,7 @@ __device__ __forceinline__ void warp_pileup(const CallArgs& a, int64_t r_lo, int
             mminus = __ldg(a.strand + r) != '+';
         }
         const int cnt = (int)((r_hi - rb) < 32 ? (r_hi - rb) : 32);
+        const uint16_t* rows = a.bq + rb * L;
         for (int k = 0; k < cnt; ++k) {
             const int32_t start = __shfl_sync(kFull, mpos, k);
             const uint32_t lh = __shfl_sync(kFull, mlh, k);
@@ -91,42 +99,127 @@ __device__ __forceinline__ void warp_pileup(const CallArgs& a, int64_t r_lo, int
             const int coord = (int)(site - start);
             const int rlen = (int)(lh >> 16);
             if (!active || coord < 0 || coord >= rlen) continue;
-            const int hit = (int)(lh & 0xffffu);
-            const uint16_t bq = __ldg(a.bq + (rb + k) * L + coord);
+            const uint32_t hit = lh & 0xffffu;
+            const uint32_t bq = __ldg(rows + k * L + coord);
             const signed char base = (signed char)(bq & 0xff);
             const signed char qual = (signed char)(bq >> 8);
-            p.depth += 1;
-            p.repeat += (uint32_t)hit;
-            if (base == 'N' || qual < qmin || p.dep_uni >= 0xFF) continue;
-            const int b = (base >> 1) & 3;
+            depth += 1;
+            repeat += hit;
+            if (base == 'N' || qual < qmin || dep_uni >= 0xFF) continue;
+            const int sh = ((base >> 1) & 3) * 16;
             if (hit == 1) {
-                p.dep_uni += 1;
+                dep_uni += 1;
+                const int q = qual - qmin;
                 const uint32_t coord_val = minus ? (uint32_t)(rlen - 1 - coord) : (uint32_t)coord;
-                const uint32_t w = make_record(base, qual - qmin, coord_val, minus ? 1u : 0u);
-                if (p.num < SLOTS) {
-                    int j = p.num;
-                    while (j > 0) {
-                        const uint32_t prev = recs[(j - 1) * kTile];
-                        if (prev <= w) break;
-                        recs[j * kTile] = prev;
-                        --j;
-                    }
-                    recs[j * kTile] = w;
-                    p.num += 1;
+                const uint32_t w = make_record(base, q, coord_val, (uint32_t)minus);
+                if (num < SLOTS) {
+                    recs[num * kTile] = w;
+                    num += 1;
                 } else {
                     overflow = true;
                 }
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (i == b) { p.cu[i] += 1; p.qs[i] += qual - qmin; }
+                cu4 += 1u << (sh >> 1);
+                qs4 += (uint64_t)(uint32_t)q << sh;
             }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (i == b) p.ca[i] += 1;
+            ca4 += 1ull << sh;
         }
     }
     if (overflow) atomicExch(a.error, 2);
-    if (p.ca[0] > 0xffff || p.ca[1] > 0xffff || p.ca[2] > 0xffff || p.ca[3] > 0xffff) atomicExch(a.error, 1);
+    if (depth > 0xffff) atomicExch(a.error, 1);
+    /* ascending insertion sort of the column */
+    for (int i = 1; i < num; ++i) {
+        const uint32_t w = recs[i * kTile];
+        int j = i;
+        while (j > 0) {
+            const uint32_t prev = recs[(j - 1) * kTile];
+            if (prev <= w) break;
+            recs[j * kTile] = prev;
+            --j;
+        }
+        recs[j * kTile] = w;
+    }
+    PackedPileup pk;
+    pk.cu4 = cu4;
+    pk.qs4 = qs4;
+    pk.ca4 = ca4;
+    pk.depth = depth;
+    pk.repeat = repeat;
+    pk.dep_uni = (uint16_t)dep_uni;
+    pk.num = (uint16_t)num;
+    return pk;
+}
+
+/* dbSNP row of each flagged site of a tile: the rows before the tile plus the
+ * flagged sites before it in the tile (the rows are the flagged sites in
+ * position order).  Every thread of the CTA calls it. */
+__device__ __forceinline__ int32_t tile_snp_row(const CallArgs& a, int64_t tile, bool flagged, int* s_cnt) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned b = __ballot_sync(kFull, flagged);
+    if (lane == 0) s_cnt[warp] = __popc(b);
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += s_cnt[w];
+    return flagged ? a.tile_snp[tile] + before + __popc(b & ((1u << lane) - 1u)) : -1;
+}
+
+/* Shared state of a tile after its pileup, re-dealt to the threads in order of
+ * record count so that the lanes of a warp walk columns of similar depth.  The
+ * packed counts of the tile's sites (kTile entries) are passed through the
+ * pcr-bitset area of the dynamic shared memory, which is free until the
+ * record walk. */
+template <int SLOTS>
+struct TileDeal {
+    int32_t snp_row[kTile];
+    int hist[SLOTS + 2];
+    int perm[kTile];
+    uint8_t ori[kTile];
+    int cnt[kWarpsPerTile];
+};
+
+/* Returns the tile column (site offset) this thread calls from here on and
+ * its pileup counts; the pcr-bitset area may be written once it returns. */
+template <int SLOTS>
+__device__ __forceinline__ int deal_by_depth(TileDeal<SLOTS>& d, PackedPileup* pk_area, const PackedPileup& pk,
+                                             bool active, uint8_t ori, int32_t snp_row, SitePileup* p) {
+    const int t = threadIdx.x;
+    for (int i = t; i < SLOTS + 2; i += kTile) d.hist[i] = 0;
+    pk_area[t] = pk;
+    d.snp_row[t] = snp_row;
+    d.ori[t] = ori;
+    __syncthreads();
+    const int key = active ? (int)pk.num + 1 : 0;
+    atomicAdd(&d.hist[key], 1);
+    __syncthreads();
+    if (t < 32) {
+        /* exclusive scan of the SLOTS + 2 counts by one warp */
+        constexpr int per = (SLOTS + 2 + 31) / 32;
+        int v[per], sum = 0;
+#pragma unroll
+        for (int k = 0; k < per; ++k) {
+            const int i = t * per + k;
+            v[k] = i < SLOTS + 2 ? d.hist[i] : 0;
+            sum += v[k];
+        }
+        int x = sum;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(kFull, x, off);
+            if (t >= off) x += y;
+        }
+        int run = x - sum;
+#pragma unroll
+        for (int k = 0; k < per; ++k) {
+            const int i = t * per + k;
+            if (i < SLOTS + 2) d.hist[i] = run;
+            run += v[k];
+        }
+    }
+    __syncthreads();
+    d.perm[atomicAdd(&d.hist[key], 1)] = t;
+    __syncthreads();
+    const int me = d.perm[t];
+    *p = pk_area[me].unpack();
+    __syncthreads();
+    return me;
 }
 
 __device__ __forceinline__ void store_counts(const CallArgs& a, int64_t site, const SitePileup& p) {
@@ -172,9 +265,11 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
 /* tile classification                                                       */
 /* ------------------------------------------------------------------------ */
 
+__constant__ int c_slots[kNumBins] = {32, 48, 64, 96, 128, 256};
+
 /* Per tile: the deepest site's record need (reads starting in [site - L + 1,
  * site], capped at 255) picks the depth bin; the window's mode picks the FP64
- * kernel (bins 0..3) or the fast one (bins 4..7).  Each warp's read range is
+ * kernel (bins 0 .. kNumBins-1) or the fast one (the next kNumBins).  Each warp's read range is
  * stored for the calling kernels. */
 __global__ void __launch_bounds__(kTile) classify_tiles_kernel(CallArgs a, int pass, int* bin_count,
                                                                int32_t* bin_tiles) {
@@ -219,7 +314,9 @@ __global__ void __launch_bounds__(kTile) classify_tiles_kernel(CallArgs a, int p
         int m = 0;
         for (int i = 0; i < kWarpsPerTile; ++i) m = max(m, smax[i]);
         const bool fast = a.precision == 1 && !(wflags & (kWinKeepLik | kWinExternalLik));
-        const int bin = (m <= 32 ? 0 : m <= 64 ? 1 : m <= 128 ? 2 : 3) + (fast ? kNumBins : 0);
+        int bin = 0;
+        while (bin < kNumBins - 1 && m > c_slots[bin]) ++bin;
+        bin += fast ? kNumBins : 0;
         const int idx = atomicAdd(&bin_count[bin], 1);
         bin_tiles[(int64_t)bin * a.n_tiles + idx] = (int32_t)tile;
     }
@@ -268,49 +365,43 @@ cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, c
 /* the FP64 calling kernel                                                   */
 /* ------------------------------------------------------------------------ */
 
-/* deferred != 0: only the sites the fast kernel marked (pending or sampled)
- * are called; their FP32 sums are tried first with the double-precision
- * bound checks, then recomputed in FP64 when those fail. */
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles,
-                                                              int deferred) {
+__global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t* recs = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;        /* [SLOTS][kTile] */
-    uint32_t* seen = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile + threadIdx.x;  /* [nw][kTile] */
+    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);                   /* [SLOTS][kTile] */
+    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;    /* [nw][kTile] */
 
+    __shared__ TileDeal<SLOTS> deal;
     const int t = threadIdx.x, warp = t >> 5;
     const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
     const int win = (int)(s0 / kWin);
     const uint8_t wflags = a.win_flags[win];
-    const int64_t site = s0 + t;
-    bool active = site < a.chr_len;
-    uint8_t f0 = 0;
-    if (deferred) {
-        if (active) f0 = a.out[site].flags;
-        active = active && (f0 & (kCallPending | kCallSampled));
-        if (!__any_sync(kFull, active)) return;
-    }
     const int64_t r_lo = a.warp_rng[(tile * kWarpsPerTile + warp) * 2];
     const int64_t r_hi = a.warp_rng[(tile * kWarpsPerTile + warp) * 2 + 1];
+    const bool active_t = s0 + t < a.chr_len;
+    const uint8_t ori_t = active_t ? __ldg(a.ori + s0 + t) : 0;
+    const int32_t row_t = tile_snp_row(a, tile, (ori_t & 8) != 0, deal.cnt);
+    const PackedPileup pk = warp_pileup<SLOTS>(a, r_lo, r_hi, s0 + t, active_t, recs_all + t);
     SitePileup p;
-    warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs, p);
-    if (!active) return;
+    const int me = deal_by_depth<SLOTS>(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t,
+                                        &p);
+    const int64_t site = s0 + me;
+    if (site >= a.chr_len) return;
+    const uint8_t ori = deal.ori[me];
+    uint32_t* recs = recs_all + me;
+    uint32_t* seen = seen_all + me;
 
-    double tl[16], eps[16];
+    double tl[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) { tl[i] = 0.0; eps[i] = 0.0; }
-    const bool external = (wflags & kWinExternalLik) != 0;
-    const bool fp32 = deferred && a.precision == 1;
-    if (external) {
+    for (int i = 0; i < 16; ++i) tl[i] = 0.0;
+    if (wflags & kWinExternalLik) {
         const int src = a.win_lik_src[win];
         if (src >= 0) {
             const double* srcp = a.lik_keep + ((int64_t)src * kWin + (site - (int64_t)win * kWin)) * 10;
 #pragma unroll
             for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = srcp[i];
         }
-    } else if (fp32) {
-        likelihood_fp32(a, recs, seen, kTile, p.num, tl, eps);
     } else {
         likelihood_fp64(a, recs, seen, kTile, p.num, tl);
         if (wflags & kWinKeepLik) {
@@ -319,40 +410,13 @@ __global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const 
             for (int i = 0; i < 10; ++i) dst[i] = tl[genotype_of(i)];
         }
     }
-    if ((wflags & kWinKeepCounts) && !deferred) store_counts(a, site, p);
+    if (wflags & kWinKeepCounts) store_counts(a, site, p);
 
-    const uint8_t ori = __ldg(a.ori + site);
     double lp[16];
-    load_log_prior(a, site, ori, lp);
+    load_log_prior(a, deal.snp_row[me], ori, lp);
     auto nq = [&](int b) { return neighbour_qsum(a, site, b); };
-    if (fp32 && (f0 & kCallSampled)) {
-        /* sampled accuracy of the FP32 sums against the FP64 ones */
-        double t64[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) t64[i] = 0.0;
-        likelihood_fp64(a, recs, seen, kTile, p.num, t64);
-        double m = 0.0;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) m = fmax(m, fabs(t64[i] - tl[i]));
-        atomicMax(a.stats + 3, (unsigned long long)__double_as_longlong(m));
-        atomicAdd(a.stats + 2, 1ull);
-    }
     SiteCall call;
-    if (!site_posterior(a, ori, p, tl, fp32 ? eps : nullptr, lp, recs, kTile, nq, &call)) {
-        /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
-        likelihood_fp64(a, recs, seen, kTile, p.num, tl);
-        site_posterior(a, ori, p, tl, nullptr, lp, recs, kTile, nq, &call);
-        call.flags |= kCallFixup;
-        atomicAdd(a.stats + 1, 1ull);
-    }
-    if (deferred) {
-        if (f0 & kCallPending) {
-            atomicAdd(a.stats + 4, 1ull);
-        } else if (!same_call(a.out[site], call)) {
-            /* a sampled site the fast kernel decided differs from the FP64 call */
-            atomicAdd(a.stats + 5, 1ull);
-        }
-    }
+    site_posterior(a, ori, p, tl, nullptr, lp, recs, kTile, nq, &call);
     a.out[site] = call;
 }
 
@@ -360,75 +424,189 @@ __global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const 
 /* the fast calling kernel                                                   */
 /* ------------------------------------------------------------------------ */
 
+/* Sites whose call is not proven in FP32 (and every 4096th site, sampled for
+ * the FP32 accuracy figure) are appended to the deferred pool: counts and the
+ * sorted records with their occurrence byte restored.  The append counters
+ * keep counting past the capacities so that the host can size the pool and
+ * run the pass again. */
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, 6) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles, int bin) {
+__global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t* recs = reinterpret_cast<uint32_t*>(smem) + threadIdx.x;
-    uint32_t* seen = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile + threadIdx.x;
+    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;
+    __shared__ TileDeal<SLOTS> deal;
 
-    const int t = threadIdx.x, warp = t >> 5;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
     const int win = (int)(s0 / kWin);
     const uint8_t wflags = a.win_flags[win];
-    const int64_t site = s0 + t;
-    const bool active = site < a.chr_len;
     const int64_t r_lo = a.warp_rng[(tile * kWarpsPerTile + warp) * 2];
     const int64_t r_hi = a.warp_rng[(tile * kWarpsPerTile + warp) * 2 + 1];
+    const bool active_t = s0 + t < a.chr_len;
+    const uint8_t ori_t = active_t ? __ldg(a.ori + s0 + t) : 0;
+    const int32_t row_t = tile_snp_row(a, tile, (ori_t & 8) != 0, deal.cnt);
+    const PackedPileup pk = warp_pileup<SLOTS>(a, r_lo, r_hi, s0 + t, active_t, recs_all + t);
     SitePileup p;
-    warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs, p);
+    const int me = deal_by_depth<SLOTS>(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t,
+                                        &p);
+    const int64_t site = s0 + me;
+    const bool active = site < a.chr_len;
+    uint32_t* recs = recs_all + me;
+    uint32_t* seen = seen_all + me;
 
-    bool listed = false;
+    uint8_t dflags = 0;
     if (active) {
         if (wflags & kWinKeepCounts) store_counts(a, site, p);
         /* adjusted quality of each record, written over its occurrence byte */
         walk_records<true>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
             recs[i * kTile] = (recs[i * kTile] & ~0xffu) | (uint32_t)qa;
         });
-        /* FP32 sums, two records per step (the pairing of likelihood_fp32) */
+        /* FP32 sums, four records per compensated step (the grouping of
+         * likelihood_fp32) */
         Kahan10 k;
         k.init();
-        for (int i = 0; i < p.num; i += 2) {
-            const uint32_t w0 = recs[i * kTile];
-            const bool two = i + 1 < p.num;
-            const uint32_t w1 = two ? recs[(i + 1) * kTile] : w0;
+        for (int i = 0; i < p.num; i += 4) {
             float x[10], y[10];
-            lik32_row(a, (int)(w0 & 0xffu), rec_coord(w0), rec_base(w0), x);
-            lik32_row(a, (int)(w1 & 0xffu), rec_coord(w1), rec_base(w1), y);
-            if (two) {
+            uint32_t w = recs[i * kTile];
+            lik32_row(a, (int)(w & 0xffu), rec_coord(w), rec_base(w), x);
+            if (i + 1 < p.num) {
+                w = recs[(i + 1) * kTile];
+                lik32_row(a, (int)(w & 0xffu), rec_coord(w), rec_base(w), y);
+#pragma unroll
+                for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
+            }
+            if (i + 2 < p.num) {
+                float z[10];
+                w = recs[(i + 2) * kTile];
+                lik32_row(a, (int)(w & 0xffu), rec_coord(w), rec_base(w), y);
+                if (i + 3 < p.num) {
+                    w = recs[(i + 3) * kTile];
+                    lik32_row(a, (int)(w & 0xffu), rec_coord(w), rec_base(w), z);
+#pragma unroll
+                    for (int v = 0; v < 10; ++v) y[v] = __fadd_rn(y[v], z[v]);
+                }
 #pragma unroll
                 for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
             }
             k.add(x);
         }
-        const uint8_t ori = __ldg(a.ori + site);
+        const uint8_t ori = deal.ori[me];
         SiteCall call;
-        const bool sampled = (site & 4095) == 0 && a.stats;
-        if (fast_posterior(a, site, ori, p, k.s, p.num, &call)) {
-            if (sampled) call.flags |= kCallSampled;
-            listed = sampled;
+        if ((site & 4095) == 0 && a.stats) dflags = kCallSampled;
+        if (fast_posterior(a, deal.snp_row[me], ori, p, k.s, p.num, &call)) {
+            call.flags |= dflags;
         } else {
             call = SiteCall{};
-            call.flags = kCallPending | (sampled ? kCallSampled : 0);
-            listed = true;
+            dflags |= kCallPending;
+            call.flags = dflags;
         }
         a.out[site] = call;
     }
-    if (__syncthreads_or(listed) && t == 0) {
-        const int idx = atomicAdd(a.fix_count + bin, 1);
-        a.fix_tiles[(int64_t)bin * a.n_tiles + idx] = (int32_t)tile;
+    /* append the deferred sites of the warp */
+    const unsigned m = __ballot_sync(kFull, dflags != 0);
+    if (m == 0) return;
+    unsigned long long base = 0;
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) base = atomicAdd(a.dcount, (unsigned long long)__popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    if (!dflags) return;
+    const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+    const unsigned long long off = atomicAdd(a.dcount + 1, (unsigned long long)p.num);
+    if ((int64_t)slot >= a.dsite_cap || (int64_t)(off + p.num) > a.dpool_cap) return;
+    DeferredSite d;
+    d.site = site;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        d.cu[i] = (uint16_t)p.cu[i];
+        d.qs[i] = (uint16_t)p.qs[i];
+        d.ca[i] = p.ca[i];
     }
+    d.depth = p.depth;
+    d.repeat = p.repeat;
+    d.rec_off = (uint32_t)off;
+    d.num = (uint16_t)p.num;
+    d.dep_uni = (uint16_t)p.dep_uni;
+    d.snp_row = deal.snp_row[me];
+    d.flags = dflags;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) d.pad[i] = 0;
+    a.dsites[slot] = d;
+    uint32_t* dst = a.dpool + off;
+    for (int i = 0; i < p.num; ++i) dst[i] = (recs[i * kTile] & ~0xffu) | 1u;
+}
+
+/* The FP64 pass over the deferred sites, one thread per site: the FP32 sums
+ * again (the same pairing, hence the same values) with the double-precision
+ * bound checks, then the FP64 sums where those fail.  Sampled sites also get
+ * the FP64 sums for the accuracy figure, and when the fast kernel had decided
+ * them its call is compared with this one. */
+__global__ void __launch_bounds__(128) deferred_sites_kernel(CallArgs a, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DeferredSite d = a.dsites[i];
+    const int64_t site = d.site;
+    const uint32_t* recs = a.dpool + d.rec_off;
+    uint32_t seen[16];
+    SitePileup p;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        p.cu[b] = d.cu[b];
+        p.qs[b] = d.qs[b];
+        p.ca[b] = d.ca[b];
+    }
+    p.depth = d.depth;
+    p.repeat = d.repeat;
+    p.dep_uni = d.dep_uni;
+    p.num = d.num;
+    double tl[16], eps[16];
+#pragma unroll
+    for (int g = 0; g < 16; ++g) { tl[g] = 0.0; eps[g] = 0.0; }
+    likelihood_fp32(a, recs, seen, 1, p.num, tl, eps);
+    if (d.flags & kCallSampled) {
+        double t64[16];
+#pragma unroll
+        for (int g = 0; g < 16; ++g) t64[g] = 0.0;
+        likelihood_fp64(a, recs, seen, 1, p.num, t64);
+        double m = 0.0;
+#pragma unroll
+        for (int g = 0; g < 16; ++g) m = fmax(m, fabs(t64[g] - tl[g]));
+        atomicMax(a.stats + 3, (unsigned long long)__double_as_longlong(m));
+        atomicAdd(a.stats + 2, 1ull);
+    }
+    const uint8_t ori = __ldg(a.ori + site);
+    double lp[16];
+    load_log_prior(a, d.snp_row, ori, lp);
+    auto nq = [&](int b) { return neighbour_qsum(a, site, b); };
+    SiteCall call;
+    if (!site_posterior(a, ori, p, tl, eps, lp, recs, 1, nq, &call)) {
+        /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
+        likelihood_fp64(a, recs, seen, 1, p.num, tl);
+        site_posterior(a, ori, p, tl, nullptr, lp, recs, 1, nq, &call);
+        call.flags |= kCallFixup;
+        atomicAdd(a.stats + 1, 1ull);
+    }
+    if (d.flags & kCallPending) {
+        atomicAdd(a.stats + 4, 1ull);
+    } else if (!same_call(a.out[site], call)) {
+        /* a sampled site the fast kernel decided differs from the FP64 call */
+        atomicAdd(a.stats + 5, 1ull);
+    }
+    a.out[site] = call;
 }
 
 /* ------------------------------------------------------------------------ */
 /* launchers                                                                 */
 /* ------------------------------------------------------------------------ */
 
-static const int kSlots[kNumBins] = {32, 64, 128, 256};
+static const int kSlots[kNumBins] = {32, 48, 64, 96, 128, 256};
 
 size_t call_smem_bytes(int slots, int L) {
-    const int nw = (2 * L + 31) >> 5;
-    return ((size_t)slots + nw) * kTile * 4;
+    /* records [slots][kTile], then the pcr bitsets [nw][kTile], which first
+     * hold the tile's packed pileup counts */
+    const size_t nw = (2 * L + 31) >> 5;
+    const size_t bits = nw * kTile * 4, packed = sizeof(PackedPileup) * kTile;
+    return (size_t)slots * kTile * 4 + (bits > packed ? bits : packed);
 }
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32_t* d_bin_tiles, cudaStream_t stream) {
@@ -439,27 +617,35 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32
 }
 
 template <int SLOTS>
-static cudaError_t launch_one(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count,
-                              cudaStream_t stream) {
+static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles, int count, cudaStream_t stream) {
     const int smem = (int)call_smem_bytes(SLOTS, a.L);
     if (kind == kKindFast) {
         cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        call_fast_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles, bin);
+        call_fast_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
     } else {
         cudaFuncSetAttribute(call_tiles_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        call_tiles_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles, kind == kKindDeferred ? 1 : 0);
+        call_tiles_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
     }
     return cudaGetLastError();
 }
 
-/* Launch a calling kernel over the `count` tiles of depth bin `bin` (0..3). */
+/* Launch the FP64 or the fast calling kernel over the `count` tiles of depth
+ * bin `bin`. */
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream) {
     switch (bin) {
-        case 0: return launch_one<32>(a, kind, bin, tiles, count, stream);
-        case 1: return launch_one<64>(a, kind, bin, tiles, count, stream);
-        case 2: return launch_one<128>(a, kind, bin, tiles, count, stream);
-        default: return launch_one<256>(a, kind, bin, tiles, count, stream);
+        case 0: return launch_one<32>(a, kind, tiles, count, stream);
+        case 1: return launch_one<48>(a, kind, tiles, count, stream);
+        case 2: return launch_one<64>(a, kind, tiles, count, stream);
+        case 3: return launch_one<96>(a, kind, tiles, count, stream);
+        case 4: return launch_one<128>(a, kind, tiles, count, stream);
+        default: return launch_one<256>(a, kind, tiles, count, stream);
     }
+}
+
+cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    deferred_sites_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a, n);
+    return cudaGetLastError();
 }
 
 int bin_slots(int bin) { return kSlots[bin]; }

@@ -15,15 +15,30 @@ constexpr int kNumStats = 8;
 constexpr int kTile = 128;        /* sites per tile (divides the window) */
 constexpr int kWarpsPerTile = kTile / 32;
 constexpr int kMaxStagedReads = 2048;
-constexpr int kNumBins = 4;       /* record slots 32 / 64 / 128 / 256 */
+constexpr int kNumBins = 6;       /* record slots 32 / 48 / 64 / 96 / 128 / 256 */
 
 /* calling kernels */
 enum CallKind : int {
     kKindClassify = 0,
     kKindFP64 = 1,      /* FP64 likelihood, every site of the tile */
     kKindFast = 2,      /* FP32 likelihood and posterior, hard sites deferred */
-    kKindDeferred = 3,  /* the FP64 kernel over the deferred sites of a tile */
+    kKindDeferred = 3,  /* FP64 pass over the sites the fast kernel deferred */
 };
+
+/* A site the fast kernel left to the FP64 pass: its pileup counts and the
+ * offset of its sorted records in the deferred record pool. */
+struct DeferredSite {
+    int64_t site;
+    uint16_t cu[4], qs[4];
+    uint32_t ca[4];
+    uint32_t depth, repeat;
+    uint32_t rec_off;
+    uint16_t num, dep_uni;
+    int32_t snp_row;             /* dbSNP row of the site, -1 if none */
+    uint8_t flags;               /* kCallPending and/or kCallSampled */
+    uint8_t pad[3];
+};
+static_assert(sizeof(DeferredSite) == 64, "DeferredSite is 64 bytes");
 
 /* per-window calling mode, decided by the host replay of the reference's
  * window loop (cpp/call_genotype.cc:422-669) */
@@ -44,8 +59,9 @@ struct CallArgs {
     /* reference */
     const uint8_t* ori;          /* 4-bit site code per position */
     int64_t chr_len;
-    const DbSnpEntry* snp;       /* sorted by position */
+    const DbSnpEntry* snp;       /* sorted by position, one row per site flagged in ori */
     int64_t n_snp;
+    const int32_t* tile_snp;     /* [n_tiles]: dbSNP rows before each 128-site tile */
     const double* snp_lp;        /* [n_snp][16] log10 prior of each dbSNP site (refine mode) */
     const float* snp_lp32;       /* [n_snp][12] the same in FP32, by table column */
     /* tables */
@@ -70,8 +86,11 @@ struct CallArgs {
     /* tiles */
     int64_t n_tiles;
     int64_t* warp_rng;           /* [n_tiles][4][2]: reads that can cover each warp's 32 sites */
-    int* fix_count;              /* [kNumBins] tiles with deferred sites, per bin */
-    int32_t* fix_tiles;          /* [kNumBins][n_tiles] */
+    /* sites deferred by the fast kernel */
+    DeferredSite* dsites;        /* [dsite_cap] */
+    uint32_t* dpool;             /* [dpool_cap] sorted records of the deferred sites */
+    unsigned long long* dcount;  /* [2]: sites and record words requested (may exceed the capacities) */
+    int64_t dsite_cap, dpool_cap;
     /* outputs */
     SiteCall* out;               /* [chr_len] */
     SiteCounts* counts;          /* [chr_len] or null */

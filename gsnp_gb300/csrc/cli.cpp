@@ -1,0 +1,444 @@
+/*
+ * cli.cpp - the `gsnp` command: SOAPsnp/GSNP consensus calling on one GB300.
+ *
+ * Same options, inputs and outputs as the reference's command line
+ * (cpp/main.cc:85-420): a sorted SOAP alignment file (-i), the reference
+ * FASTA (-d), the consensus output (-o, cns text, or the -C compressed
+ * files), optional dbSNP priors (-s, -2), calibration matrix output/input
+ * (-M/-I) and the model parameters.  One extra option, -P fp64|fp32, picks
+ * the likelihood form (default fp32: FP32 compensated sums with FP64 fixup;
+ * both forms give identical output).
+ *
+ * The whole chromosome is resident on the device: the alignments are parsed
+ * on every host core, uploaded once, calibrated and called by the kernels of
+ * libgsnp_gb300.so behind include/gsnp_gb300.h.  As in the reference, the
+ * called chromosome is the one named by the last alignment, and all
+ * alignments must be on it.
+ */
+#include <fcntl.h>
+#include <getopt.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gsnp_gb300.h"
+
+namespace {
+
+struct Options {
+    std::string soap, fasta, out, dbsnp, matrix_out, matrix_in;
+    gsnp_params p{};
+    bool compress = false;
+};
+
+[[noreturn]] void usage() {
+    std::cerr << "GSNP (GB300)\n"
+                 "Compulsory Parameters:\n"
+                 "-i <FILE> Input SORTED Soap Result\n"
+                 "-d <FILE> Reference Sequence in fasta format\n"
+                 "-o <FILE> Output consensus file\n"
+                 "Optional Parameters:\n"
+                 "-z <Char> ASCII chracter standing for quality==0 [@]\n"
+                 "-g <Double> Global Error Dependency Coefficient, 0.0(complete dependent)~1.0(complete independent)[0.9]\n"
+                 "-p <Double> PCR Error Dependency Coefficient, 0.0(complete dependent)~1.0(complete independent)[0.5]\n"
+                 "-r <Double> novel altHOM prior probability [0.0005]\n"
+                 "-e <Double> novel HET prior probability [0.0010]\n"
+                 "-t set transition/transversion ratio to 2:1 in prior probability\n"
+                 "-s <FILE> Pre-formated dbSNP information\n"
+                 "-2 specify this option will REFINE SNPs using dbSNPs information [Off]\n"
+                 "-a <Double> Validated HET prior, if no allele frequency known [0.1]\n"
+                 "-b <Double> Validated altHOM prior, if no allele frequency known[0.05]\n"
+                 "-j <Double> Unvalidated HET prior, if no allele frequency known [0.02]\n"
+                 "-k <Double> Unvalidated altHOM rate, if no allele frequency known[0.01]\n"
+                 "-u Enable rank sum test to give HET further penalty for better accuracy. [Off]\n"
+                 "-m Enable monoploid calling mode, this will ensure all consensus as HOM and you MUST specify "
+                 "this option for male chrX\n"
+                 "-M <FILE> Output the quality calibration matrix\n"
+                 "-I <FILE> Input previous quality calibration matrix\n"
+                 "-L <short> maximum length of read [45]\n"
+                 "-Q <short> maximum FASTQ quality score [40]\n"
+                 "-C Output compressed consensus files\n"
+                 "-P fp64|fp32 likelihood form on the GPU [fp32]\n";
+    exit(1);
+}
+
+void parse_args(int argc, char** argv, Options* o) {
+    gsnp_params& p = o->p;
+    p.q_min = 64;
+    p.q_max = 64 + 40;
+    p.read_length = 45;
+    p.pcr_dependency = log10(0.5);
+    p.global_dependency = log10(0.9);
+    p.het_novel = 0.0010;
+    p.althom_novel = 0.0005;
+    p.het_val = 0.10;
+    p.althom_val = 0.05;
+    p.het_unval = 0.02;
+    p.althom_unval = 0.01;
+    p.precision = GSNP_PRECISION_FP32_FIXUP;
+    int c;
+    while ((c = getopt(argc, argv, "i:d:o:z:g:p:r:e:ts:2a:b:j:k:unmqM:I:L:Q:S:F:E:T:h:CP:")) != -1) {
+        switch (c) {
+            case 'i': o->soap = optarg; break;
+            case 'd': o->fasta = optarg; break;
+            case 'o': o->out = optarg; break;
+            case 'z': p.q_min = (signed char)optarg[0]; p.q_max = (signed char)(p.q_min + 40); break;
+            case 'g': p.global_dependency = log10(atof(optarg)); break;
+            case 'p': p.pcr_dependency = log10(atof(optarg)); break;
+            case 'r': p.althom_novel = atof(optarg); break;
+            case 'e': p.het_novel = atof(optarg); break;
+            case 't': p.transition_dominant = 1; break;
+            case 's': o->dbsnp = optarg; break;
+            case '2': p.refine = 1; break;
+            /* the reference stores -a/-b and -j/-k crosswise to its usage text
+             * (cpp/main.cc:194-213); kept so that the same command line gives
+             * the same output */
+            case 'a': p.althom_val = atof(optarg); break;
+            case 'b': p.het_val = atof(optarg); break;
+            case 'j': p.althom_unval = atof(optarg); break;
+            case 'k': p.het_unval = atof(optarg); break;
+            case 'u': p.rank_sum = 1; break;
+            case 'n': break;
+            case 'm': p.monoploid = 1; break;
+            case 'q': printf("ERROR: The -q parameter currently is not supported.\n"); exit(0);
+            case 'M': o->matrix_out = optarg; break;
+            case 'I': o->matrix_in = optarg; break;
+            case 'S': break;
+            case 'L': p.read_length = (unsigned char)atoi(optarg); break;
+            case 'Q':
+                p.q_max = (signed char)optarg[0];
+                if (p.q_max < p.q_min) std::cerr << "FASTQ quality character error: Q_MAX > Q_MIN" << std::endl;
+                break;
+            case 'F': printf("ERROR: The -F parameter currently is not supported.\n"); exit(0);
+            case 'E': printf("ERROR: The -E parameter currently is not supported.\n"); break;
+            case 'T': printf("ERROR: the -T parameter currently is not supported.\n"); exit(0);
+            case 'C': o->compress = true; break;
+            case 'P':
+                if (!strcmp(optarg, "fp64")) p.precision = GSNP_PRECISION_FP64;
+                else if (!strcmp(optarg, "fp32")) p.precision = GSNP_PRECISION_FP32_FIXUP;
+                else usage();
+                break;
+            default: usage();
+        }
+    }
+    if (o->out.empty() || o->fasta.empty() || o->soap.empty()) usage();
+}
+
+[[noreturn]] void die(const std::string& msg, int code = EXIT_FAILURE) {
+    std::cerr << msg << std::endl;
+    exit(code);
+}
+
+/* ---- reference and dbSNP (cpp/chromosome.cc:28-220) ---- */
+
+struct Chromosome {
+    std::vector<uint8_t> codes;   /* (base >> 1) & 7, bit 3 = dbSNP */
+    std::map<uint32_t, gsnp_snp> snp;
+};
+
+void load_fasta(const std::string& path, std::map<std::string, Chromosome>* chrs) {
+    std::ifstream in(path);
+    if (!in) die("No such file or directory:" + path, 1);
+    std::string line, name;
+    Chromosome* cur = nullptr;
+    while (std::getline(in, line)) {
+        if (!line.empty() && line[0] == '>') {
+            std::string::size_type i = 1;
+            while (i != line.size() && !isspace((unsigned char)line[i])) ++i;
+            name = line.substr(1, i - 1);
+            auto r = chrs->emplace(name, Chromosome());
+            /* a repeated name keeps the entry and takes the later sequence,
+             * as the reference's loader does */
+            if (!r.second) std::cerr << "Insert Chromosome " << name << " Failed!\n";
+            cur = &r.first->second;
+            cur->codes.clear();
+        } else if (cur) {
+            for (char ch : line) cur->codes.push_back((uint8_t)((((unsigned char)ch) >> 1) & 7));
+        }
+    }
+}
+
+void load_dbsnp(const std::string& path, std::map<std::string, Chromosome>* chrs) {
+    std::ifstream in(path);
+    if (!in) die("No such file or directory:" + path, 1);
+    std::string line;
+    bool hapmap = false, validated = false, indel = false;
+    double f[4] = {0, 0, 0, 0};
+    while (std::getline(in, line)) {
+        std::istringstream s(line);
+        std::string name;
+        std::string::size_type pos = 0;
+        s >> name >> pos;
+        s >> hapmap >> validated >> indel >> f[0] >> f[1] >> f[2] >> f[3];
+        auto it = chrs->find(name);
+        if (it == chrs->end()) continue;
+        pos -= 1;
+        Chromosome& c = it->second;
+        if (pos >= c.codes.size()) continue;
+        gsnp_snp r{};
+        r.pos = (uint32_t)pos;
+        r.validated = validated;
+        r.hapmap = hapmap;
+        r.indel = indel;
+        for (int i = 0; i < 4; ++i) r.freq[i] = f[i];
+        if (c.snp.emplace((uint32_t)pos, r).second) c.codes[pos] |= 8;
+    }
+}
+
+/* ---- SOAP alignments (cpp/soap_snp.h:132-169) ---- */
+
+struct Reads {
+    std::vector<int32_t> pos, len, hit;
+    std::vector<uint8_t> strand;
+    std::vector<uint8_t> seq, qual;   /* L bytes per alignment */
+    std::vector<std::string> chr;     /* distinct chromosome names, in order of first use */
+    std::vector<uint16_t> chr_id;
+    std::string bad;                  /* first error */
+};
+
+bool next_token(const char*& p, const char* end, const char** tok, size_t* len) {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    if (p >= end) return false;
+    *tok = p;
+    while (p < end && *p != ' ' && *p != '\t' && *p != '\r') ++p;
+    *len = (size_t)(p - *tok);
+    return true;
+}
+
+bool to_int(const char* t, size_t n, int* v) {
+    char buf[32];
+    if (n == 0 || n >= sizeof(buf)) return false;
+    memcpy(buf, t, n);
+    buf[n] = 0;
+    char* e = nullptr;
+    errno = 0;
+    const long x = strtol(buf, &e, 10);
+    if (e == buf || errno) return false;
+    *v = (int)x;
+    return true;
+}
+
+/* Parse lines [begin, end) into r; the reference's stream extraction skips a
+ * line whose fields do not parse. */
+void parse_chunk(const char* begin, const char* end, int L, Reads* r) {
+    std::string read, qual;
+    const char* p = begin;
+    while (p < end) {
+        const char* eol = (const char*)memchr(p, '\n', (size_t)(end - p));
+        if (!eol) eol = end;
+        const char* q = p;
+        p = eol + 1;
+        const char* tok[11];
+        size_t tl[11];
+        int nt = 0;
+        while (nt < 11 && next_token(q, eol, &tok[nt], &tl[nt])) ++nt;
+        if (nt < 10) continue;
+        int hit, read_len, position, mismatch;
+        if (!to_int(tok[3], tl[3], &hit) || !to_int(tok[5], tl[5], &read_len) || !to_int(tok[8], tl[8], &position) ||
+            !to_int(tok[9], tl[9], &mismatch))
+            continue;
+        read.assign(tok[1], tl[1]);
+        qual.assign(tok[2], tl[2]);
+        if (mismatch > 100) {
+            int indel_pos;
+            if (nt < 11 || !to_int(tok[10], tl[10], &indel_pos)) continue;
+            if (mismatch > 200) {
+                const int n = mismatch - 200;
+                const std::string ns(n > 0 ? n : 0, 'N');
+                read = read.substr(0, indel_pos) + ns + read.substr(indel_pos, read_len - indel_pos);
+                qual = qual.substr(0, indel_pos) + ns + qual.substr(indel_pos, read_len - indel_pos);
+            } else {
+                const int n = mismatch - 100;
+                read = read.substr(0, indel_pos) + read.substr(indel_pos + n, read_len - indel_pos - n);
+                qual = qual.substr(0, indel_pos) + qual.substr(indel_pos + n, read_len - indel_pos - n);
+            }
+        }
+        if (read_len < 0 || read_len > L || (int)read.size() < read_len || (int)qual.size() < read_len) {
+            if (r->bad.empty()) r->bad = "alignment longer than -L or than its sequence field";
+            continue;
+        }
+        const std::string chr(tok[7], tl[7]);
+        size_t cid = 0;
+        while (cid < r->chr.size() && r->chr[cid] != chr) ++cid;
+        if (cid == r->chr.size()) r->chr.push_back(chr);
+        r->chr_id.push_back((uint16_t)cid);
+        r->pos.push_back(position - 1);
+        r->len.push_back(read_len);
+        r->hit.push_back(hit);
+        r->strand.push_back((uint8_t)tok[6][0]);
+        const size_t off = r->seq.size();
+        r->seq.resize(off + L, 'A');
+        r->qual.resize(off + L, 0);
+        memcpy(&r->seq[off], read.data(), (size_t)read_len);
+        memcpy(&r->qual[off], qual.data(), (size_t)read_len);
+    }
+}
+
+void load_soap(const std::string& path, int L, Reads* out) {
+    const int fd = open(path.c_str(), O_RDONLY);
+    if (fd < 0) die("No such file or directory:" + path, 1);
+    struct stat st;
+    fstat(fd, &st);
+    const size_t size = (size_t)st.st_size;
+    if (size == 0) {
+        close(fd);
+        return;
+    }
+    const char* data = (const char*)mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+    if (data == MAP_FAILED) die("cannot map " + path);
+    const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<const char*> cut(nt + 1);
+    cut[0] = data;
+    cut[nt] = data + size;
+    for (unsigned t = 1; t < nt; ++t) {
+        const char* c = data + size * t / nt;
+        if (c < cut[t - 1]) c = cut[t - 1];
+        const char* nl = (const char*)memchr(c, '\n', (size_t)(data + size - c));
+        cut[t] = nl ? nl + 1 : data + size;
+    }
+    std::vector<Reads> part(nt);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t) th.emplace_back(parse_chunk, cut[t], cut[t + 1], L, &part[t]);
+    for (auto& x : th) x.join();
+    munmap((void*)data, size);
+    close(fd);
+    for (Reads& r : part) {
+        if (out->bad.empty() && !r.bad.empty()) out->bad = r.bad;
+        std::vector<uint16_t> remap(r.chr.size());
+        for (size_t i = 0; i < r.chr.size(); ++i) {
+            size_t k = 0;
+            while (k < out->chr.size() && out->chr[k] != r.chr[i]) ++k;
+            if (k == out->chr.size()) out->chr.push_back(r.chr[i]);
+            remap[i] = (uint16_t)k;
+        }
+        for (uint16_t id : r.chr_id) out->chr_id.push_back(remap[id]);
+        out->pos.insert(out->pos.end(), r.pos.begin(), r.pos.end());
+        out->len.insert(out->len.end(), r.len.begin(), r.len.end());
+        out->hit.insert(out->hit.end(), r.hit.begin(), r.hit.end());
+        out->strand.insert(out->strand.end(), r.strand.begin(), r.strand.end());
+        out->seq.insert(out->seq.end(), r.seq.begin(), r.seq.end());
+        out->qual.insert(out->qual.end(), r.qual.begin(), r.qual.end());
+        std::vector<uint8_t>().swap(r.seq);
+        std::vector<uint8_t>().swap(r.qual);
+    }
+}
+
+/* ---- calibration matrix files (cpp/matrix.cc:215-241) ---- */
+
+void write_matrix(const std::string& path, const gsnp_params& p, const double* pm) {
+    FILE* f = fopen(path.c_str(), "w");
+    if (!f) die("Cannot creat file :" + path, 1);
+    for (int q = p.q_min; q <= p.q_max; ++q)
+        for (unsigned long coord = 0; coord != p.read_length; ++coord) {
+            fprintf(f, "%llu\t%lu", (unsigned long long)(long long)q - (unsigned long long)(long long)p.q_min, coord);
+            for (int t = 0; t != 16; ++t)
+                fprintf(f, "\t%.16e", pm[((unsigned long long)(q - p.q_min) << 12) | (coord << 4) | (unsigned)t]);
+            fprintf(f, "\n");
+        }
+    fclose(f);
+}
+
+void read_matrix(const std::string& path, double* pm) {
+    std::ifstream in(path);
+    if (!in) die("No such file or directory:" + path, 1);
+    for (std::string line; std::getline(in, line);) {
+        std::istringstream s(line);
+        int q = 0;
+        std::string::size_type coord = 0;
+        s >> q >> coord;
+        for (int t = 0; t != 16; ++t) s >> pm[((unsigned long long)q << 12) | (coord << 4) | (unsigned)t];
+    }
+}
+
+void check(gsnp_context* ctx, int rc, const char* what) {
+    if (rc == GSNP_OK) return;
+    const std::string msg = gsnp_context_error(ctx);
+    if (rc == GSNP_ERR_UNSORTED) die(msg, 255);
+    if (rc == GSNP_ERR_INPUT && msg.find("unknown base") != std::string::npos) {
+        printf("!!!ERROR@encode: unknown base when encoding.\n");
+        exit(EXIT_FAILURE);
+    }
+    die(std::string(what) + ": " + msg);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Options o;
+    parse_args(argc, argv, &o);
+    gsnp_params& p = o.p;
+
+    std::ofstream cns(o.out.c_str());
+    if (!cns) die("Cannot creat file:" + o.out, 1);
+    std::map<std::string, Chromosome> chrs;
+    load_fasta(o.fasta, &chrs);
+    if (!o.dbsnp.empty()) load_dbsnp(o.dbsnp, &chrs);
+
+    Reads reads;
+    load_soap(o.soap, p.read_length, &reads);
+    if (!reads.bad.empty()) die("!!!ERROR: " + reads.bad);
+    if (reads.pos.empty()) die("!!!ERROR: no usable alignment.");
+    const std::string chr_name = reads.chr[reads.chr_id.back()];
+    auto it = chrs.find(chr_name);
+    if (it == chrs.end()) die("Assertion Failed: Chromosome: !" + chr_name + "! NOT found", 255);
+    for (size_t i = 0; i < reads.pos.size(); ++i)
+        if (reads.chr_id[i] != reads.chr_id.back() && reads.pos[i] >= 0)
+            die("!!!ERROR: alignments on more than one chromosome (" + reads.chr[reads.chr_id[i]] + ", " + chr_name +
+                "); call one chromosome per run");
+    Chromosome& chr = it->second;
+
+    gsnp_context* ctx = nullptr;
+    if (gsnp_context_create(0, &ctx) != GSNP_OK) die("!!!ERROR: no CUDA device");
+    std::vector<gsnp_snp> snp;
+    snp.reserve(chr.snp.size());
+    for (const auto& kv : chr.snp) snp.push_back(kv.second);
+    check(ctx, gsnp_load_reference(ctx, chr.codes.data(), (int64_t)chr.codes.size(), snp.data(), (int64_t)snp.size()),
+          "reference");
+
+    const int64_t n = (int64_t)reads.pos.size();
+    gsnp_reads r{};
+    r.n = n;
+    r.pos = reads.pos.data();
+    r.len = reads.len.data();
+    r.hit = reads.hit.data();
+    r.strand = reads.strand.data();
+    r.seq = reads.seq.data();
+    r.qual = reads.qual.data();
+    r.pitch = p.read_length;
+
+    std::vector<double> pm(256UL * 256UL * 16UL, 1.0), prior(128), rank(64UL * 64UL * 2048UL);
+    if (o.matrix_in.empty()) {
+        check(ctx, gsnp_calibrate(ctx, &p, &r, pm.data()), "calibration");
+        if (!o.matrix_out.empty()) write_matrix(o.matrix_out, p, pm.data());
+    } else {
+        read_matrix(o.matrix_in, pm.data());
+    }
+    gsnp_prior_table(&p, prior.data());
+    gsnp_rank_table(rank.data());
+    check(ctx, gsnp_load_tables(ctx, &p, pm.data(), prior.data(), rank.data()), "tables");
+    check(ctx, gsnp_call_chromosome(ctx, &r), "calling");
+
+    cns.close();
+    if (o.compress) {
+        check(ctx, gsnp_write_columns(ctx, chr_name.c_str(), o.out.c_str()), "-C output");
+    } else {
+        check(ctx, gsnp_write_cns(ctx, chr_name.c_str(), o.out.c_str()), "cns text");
+        check(ctx, gsnp_write_columns(ctx, nullptr, o.out.c_str()), "column files");
+    }
+    gsnp_context_destroy(ctx);
+    return 0;
+}

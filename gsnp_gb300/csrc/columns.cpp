@@ -1,0 +1,325 @@
+/*
+ * columns.cpp - the -C compressed output (cpp/compress.h:86-1312,
+ * cpp/dict_compression.h:40-296).
+ *
+ * Six files per run, one block per called window, byte-compatible with the
+ * reference's writers and its decompressor (cpp/decompression.cpp):
+ *   <out>.1_2             window table: count, then "chr start size" lines
+ *   <out>.3_4_6           reference base 2-bit packed, N ids, genotype and
+ *                         best-base differences from the reference base
+ *   <out>.5_7_8_9_14_16   six per-site columns, each run-length encoded and
+ *                         both run values and run lengths dictionary coded
+ *   <out>.10              second base 2-bit packed, N ids
+ *   <out>.11_12_13        second-base quality/count columns: common entries
+ *                         dictionary coded, the rest as sparse id/value lists
+ *   <out>.15_17           sparse rank-sum values and dbSNP site ids
+ * The dictionary codec runs on the GPU (dict.cu); run-length encoding, 2-bit
+ * packing and the sparse lists are single passes on the host.
+ */
+#include "columns.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rows.h"
+
+namespace gsnp {
+
+const char kAbbv[17] = {'A', 'M', 'W', 'R', 'M', 'C', 'Y', 'S', 'W', 'Y', 'T', 'K', 'R', 'S', 'K', 'G', 'N'};
+const char kActgN[9] = "ACTGNNNN";
+
+namespace {
+
+constexpr unsigned long kDictCap = 32UL * 8192UL;   /* the reference's dictionary capacity */
+
+struct Files {
+    FILE* f346 = nullptr;
+    FILE* frle = nullptr;
+    FILE* f10 = nullptr;
+    FILE* f111213 = nullptr;
+    FILE* f1517 = nullptr;
+    bool ok = true;
+    void put(FILE* f, const void* p, size_t bytes) {
+        if (bytes && fwrite(p, 1, bytes, f) != bytes) ok = false;
+    }
+};
+
+int base_bits(char c) {
+    switch (c) {
+        case 'A': return 0;
+        case 'C': return 1;
+        case 'G': return 2;
+        case 'T': return 3;
+        default: return -1;
+    }
+}
+
+/* 2-bit packing, first base in the high bits, the last word right-aligned
+ * (kernel/compress_kernel.cu:85-160) */
+std::vector<uint32_t> pack2(const std::vector<char>& c) {
+    const size_t n = c.size(), nw = (n + 15) / 16;
+    std::vector<uint32_t> code(nw, 0);
+    for (size_t w = 0; w < nw; ++w) {
+        const size_t nb = (w == nw - 1) ? n - w * 16 : 16;
+        uint32_t word = 0;
+        for (size_t i = 0; i < nb; ++i) word = (word << 2) | (uint32_t)base_bits(c[w * 16 + i]);
+        code[w] = word;
+    }
+    return code;
+}
+
+template <class T>
+unsigned rle(std::vector<T>& data, std::vector<uint32_t>& runs) {
+    const size_t n = data.size();
+    runs.assign(n, 0);
+    if (n == 0) return 0;
+    size_t r = 0, start = 0;
+    for (size_t i = 1; i <= n; ++i)
+        if (i == n || !(data[i] == data[start])) {
+            data[r] = data[start];
+            runs[r] = (uint32_t)(i - start);
+            ++r;
+            start = i;
+        }
+    return (unsigned)r;
+}
+
+class Writer {
+public:
+    Writer(const DictCodec& dict, Files& f) : dict_(dict), f_(f) {}
+
+    bool window(const std::vector<CnsRow>& rows, std::string* err) {
+        const size_t n = rows.size();
+        bool all_n = true;
+        for (const CnsRow& r : rows) all_n = all_n && r.nflag;
+        col_3_4_6(rows, all_n);
+        if (!col_rle(rows, all_n, err)) return false;
+        col_10(rows, all_n);
+        if (!col_11_12_13(rows, all_n, err)) return false;
+        col_15_17(rows, all_n);
+        (void)n;
+        return f_.ok;
+    }
+
+private:
+    const DictCodec& dict_;
+    Files& f_;
+
+    /* Column_3_4_6 (cpp/compress.h:171-409) */
+    void col_3_4_6(const std::vector<CnsRow>& rows, bool all_n) {
+        const unsigned long n = rows.size();
+        unsigned long param[7] = {1, 0, n, 0, 0, 0, 0};
+        if (all_n) {
+            f_.put(f_.f346, param, sizeof(param));
+            return;
+        }
+        std::vector<char> c3(n);
+        std::vector<int> id4, id6, idn;
+        std::vector<char> v4, v6;
+        for (unsigned long i = 0; i < n; ++i) {
+            const CnsRow& r = rows[i];
+            char a = 'N', b = 'N', c = 'N';
+            if (r.called()) {
+                a = kActgN[r.ori & 7];
+                b = kAbbv[r.type1];
+                c = kActgN[r.base1];
+            }
+            if (b != a) { id4.push_back((int)i); v4.push_back(b); }
+            if (c != a) { id6.push_back((int)i); v6.push_back(c); }
+            if (a == 'N') { idn.push_back((int)i); a = 'A'; }
+            c3[i] = a;
+        }
+        const std::vector<uint32_t> code = pack2(c3);
+        param[0] = 0;
+        param[3] = code.size();
+        param[4] = idn.size();
+        param[5] = id4.size();
+        param[6] = id6.size();
+        param[1] = 5 * id4.size() + 5 * id6.size() + 4 * idn.size() + 4 * code.size();
+        f_.put(f_.f346, param, sizeof(param));
+        f_.put(f_.f346, id4.data(), 4 * id4.size());
+        f_.put(f_.f346, v4.data(), v4.size());
+        f_.put(f_.f346, id6.data(), 4 * id6.size());
+        f_.put(f_.f346, v6.data(), v6.size());
+        f_.put(f_.f346, idn.data(), 4 * idn.size());
+        f_.put(f_.f346, code.data(), 4 * code.size());
+    }
+
+    /* one column of Column_RLEDict (cpp/compress.h:495-868) */
+    template <class T>
+    bool rle_dict(std::vector<T>& col, std::string* err) {
+        std::vector<uint32_t> runlen;
+        const unsigned runs = rle(col, runlen);
+        std::vector<uint32_t> cval(runs + 1), clen(runs + 1);
+        std::vector<T> dval(runs + 1);
+        std::vector<uint32_t> dlen(runs + 1);
+        unsigned long nwv = runs, ndv = kDictCap, nwl = runs, ndl = kDictCap;
+        if (!dict_.compress(col.data(), runs, cval.data(), &nwv, dval.data(), &ndv, err)) return false;
+        if (!dict_.compress(runlen.data(), runs, clen.data(), &nwl, dlen.data(), &ndl, err)) return false;
+        unsigned long param[6] = {runs, nwv, nwl, ndv, ndl, 4 * nwv + 4 * nwl + sizeof(T) * ndv + 4 * ndl};
+        f_.put(f_.frle, param, sizeof(param));
+        f_.put(f_.frle, cval.data(), 4 * nwv);
+        f_.put(f_.frle, clen.data(), 4 * nwl);
+        f_.put(f_.frle, dval.data(), sizeof(T) * ndv);
+        f_.put(f_.frle, dlen.data(), 4 * ndl);
+        return true;
+    }
+
+    bool col_rle(const std::vector<CnsRow>& rows, bool all_n, std::string* err) {
+        const int flag = all_n ? 1 : 0;
+        f_.put(f_.frle, &flag, sizeof(int));
+        if (flag) return true;
+        const size_t n = rows.size();
+        std::vector<int> col(n);
+        std::vector<double> dcol(n);
+        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].q_cns : 0;
+        if (!rle_dict(col, err)) return false;
+        col.resize(n);
+        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].avg1 : 0;
+        if (!rle_dict(col, err)) return false;
+        col.resize(n);
+        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].cu1 : 0;
+        if (!rle_dict(col, err)) return false;
+        col.resize(n);
+        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].ca1 : 0;
+        if (!rle_dict(col, err)) return false;
+        col.resize(n);
+        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? (int)rows[j].depth : 0;
+        if (!rle_dict(col, err)) return false;
+        for (size_t j = 0; j < n; ++j) {
+            const CnsRow& r = rows[j];
+            dcol[j] = r.called() ? (r.depth == 0 ? 255 : (double)r.repeat / r.depth) : 255.0;
+        }
+        return rle_dict(dcol, err);
+    }
+
+    /* Column_10 (cpp/compress.h:759-897) */
+    void col_10(const std::vector<CnsRow>& rows, bool all_n) {
+        const int flag = all_n ? 1 : 0;
+        f_.put(f_.f10, &flag, sizeof(int));
+        if (flag) return;
+        const size_t n = rows.size();
+        std::vector<char> c(n);
+        std::vector<uint32_t> nid;
+        for (size_t j = 0; j < n; ++j) {
+            const CnsRow& r = rows[j];
+            c[j] = (r.called() && r.base2 < 4) ? kActgN[r.base2] : 'N';
+            if (c[j] == 'N') { nid.push_back((uint32_t)j); c[j] = 'A'; }
+        }
+        const std::vector<uint32_t> code = pack2(c);
+        unsigned long param[3] = {nid.size(), code.size(), n};
+        f_.put(f_.f10, param, sizeof(param));
+        f_.put(f_.f10, code.data(), 4 * code.size());
+        f_.put(f_.f10, nid.data(), 4 * nid.size());
+    }
+
+    /* Column_11_12_13 (cpp/compress.h:947-1172).  The reference writes a
+     * window whose common list is empty by failing an assert in its
+     * dictionary code (cpp/dict_compression.h:140-143); here such a list is
+     * the pair {0, 0} with no payload. */
+    bool col_11_12_13(const std::vector<CnsRow>& rows, bool all_n, std::string* err) {
+        const int flag = all_n ? 1 : 0;
+        f_.put(f_.f111213, &flag, sizeof(int));
+        if (flag) return true;
+        const size_t n = rows.size();
+        std::vector<int> cid, c11, c12, c13, e12id, e12, e13id, e13;
+        for (size_t j = 0; j < n; ++j) {
+            const CnsRow& r = rows[j];
+            int v11 = 0, v12 = 0, v13 = 0;
+            if (r.called() && r.base2 < 4) {
+                v11 = r.avg2;
+                v12 = r.cu2;
+                v13 = r.ca2;
+            }
+            if (v11 != 0) { cid.push_back((int)j); c11.push_back(v11); c12.push_back(v12); c13.push_back(v13); }
+            else if (v11 != v12) { e12id.push_back((int)j); e12.push_back(v12); }
+            else if (v11 != v13) { e13id.push_back((int)j); e13.push_back(v13); }
+        }
+        unsigned long param[4] = {n, cid.size(), e12id.size(), e13id.size()};
+        f_.put(f_.f111213, param, sizeof(param));
+        f_.put(f_.f111213, e12id.data(), 4 * e12id.size());
+        f_.put(f_.f111213, e12.data(), 4 * e12.size());
+        f_.put(f_.f111213, e13id.data(), 4 * e13id.size());
+        f_.put(f_.f111213, e13.data(), 4 * e13.size());
+        f_.put(f_.f111213, cid.data(), 4 * cid.size());
+        for (std::vector<int>* v : {&c11, &c12, &c13}) {
+            std::vector<uint32_t> words(kWin);
+            std::vector<int> dict(kWin);
+            unsigned long dp[2] = {(unsigned long)kWin, (unsigned long)kWin};
+            if (!dict_.compress(v->data(), v->size(), words.data(), &dp[0], dict.data(), &dp[1], err)) return false;
+            f_.put(f_.f111213, dp, sizeof(dp));
+            f_.put(f_.f111213, words.data(), 4 * dp[0]);
+            f_.put(f_.f111213, dict.data(), 4 * dp[1]);
+        }
+        return true;
+    }
+
+    /* Column_15_17 (cpp/compress.h:1175-1312) */
+    void col_15_17(const std::vector<CnsRow>& rows, bool all_n) {
+        const int flag = all_n ? 1 : 0;
+        f_.put(f_.f1517, &flag, sizeof(int));
+        if (flag) return;
+        const size_t n = rows.size();
+        std::vector<int> id;
+        std::vector<double> val;
+        for (size_t j = 0; j < n; ++j)
+            if (rows[j].called() && rows[j].rank_sum != 1.0) { id.push_back((int)j); val.push_back(rows[j].rank_sum); }
+        int cnt = (int)id.size();
+        f_.put(f_.f1517, &cnt, sizeof(int));
+        f_.put(f_.f1517, id.data(), 4 * id.size());
+        f_.put(f_.f1517, val.data(), 8 * val.size());
+        id.clear();
+        for (size_t j = 0; j < n; ++j)
+            if (rows[j].called() && (rows[j].ori & 8)) id.push_back((int)j);
+        cnt = (int)id.size();
+        f_.put(f_.f1517, &cnt, sizeof(int));
+        f_.put(f_.f1517, id.data(), 4 * id.size());
+    }
+};
+
+FILE* open_file(const std::string& path, const char* mode, std::string* err) {
+    FILE* f = fopen(path.c_str(), mode);
+    if (!f) *err = "cannot create " + path;
+    return f;
+}
+
+}  // namespace
+
+int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* calls, const SiteCounts* counts,
+                  const char* chr_name, const std::string& base, const DictCodec& dict, std::string* err) {
+    Files f;
+    f.f346 = open_file(base + ".3_4_6", "wb", err);
+    f.frle = open_file(base + ".5_7_8_9_14_16", "wb", err);
+    f.f10 = open_file(base + ".10", "wb", err);
+    f.f111213 = open_file(base + ".11_12_13", "wb", err);
+    f.f1517 = open_file(base + ".15_17", "wb", err);
+    FILE* f12 = open_file(base + ".1_2", "w", err);
+    int rc = 0;
+    if (!f.f346 || !f.frle || !f.f10 || !f.f111213 || !f.f1517 || !f12) rc = 1;
+    if (rc == 0 && calls) {
+        fprintf(f12, "%lu\n", (unsigned long)plan.n_windows);
+        Writer wr(dict, f);
+        std::vector<CnsRow> rows;
+        for (int64_t w = 0; w < plan.n_windows && rc == 0; ++w) {
+            const int64_t len = plan.call_len[w];
+            fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1), (unsigned long)len);
+            rows.resize((size_t)len);
+            for (int64_t j = 0; j < len; ++j) rows[(size_t)j] = resolve_row(plan, w, j, codes, calls, counts);
+            if (!wr.window(rows, err)) rc = err->empty() ? (*err = "write failed", 1) : 1;
+        }
+    } else if (rc == 0) {
+        /* text mode: the column files exist and are empty, the table says 0 windows */
+        fprintf(f12, "0\n");
+    }
+    for (FILE* x : {f.f346, f.frle, f.f10, f.f111213, f.f1517, f12})
+        if (x && fclose(x) != 0 && rc == 0) {
+            *err = "write failed";
+            rc = 1;
+        }
+    return rc;
+}
+
+}  // namespace gsnp

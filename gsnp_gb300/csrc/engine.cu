@@ -23,6 +23,9 @@
 #include <vector>
 
 #include "calling.cuh"
+#include "columns.h"
+#include "dict.h"
+#include "emit.h"
 #include "gsnp_gb300.h"
 #include "plan.h"
 #include "tables.h"
@@ -32,6 +35,7 @@ namespace gsnp {
 cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32_t* d_bin_tiles, cudaStream_t stream);
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
+cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
 int bin_slots(int bin);
 
 /* ---- device helpers ---- */
@@ -146,6 +150,7 @@ struct gsnp_context {
     int64_t n_snp = 0;
     double* d_snp_lp = nullptr;
     float* d_snp_lp32 = nullptr;
+    int32_t* d_tile_snp = nullptr;
     bool snp_lp_ready = false;
     /* resident reads (deposited, packed) */
     int64_t n_dep = 0;
@@ -159,6 +164,7 @@ struct gsnp_context {
     WindowPlan plan;
     uint8_t* d_win_flags = nullptr;
     int32_t* d_win_lik_src = nullptr;
+    int32_t* d_win_host_src = nullptr;
     int64_t n_win_alloc = 0;
     /* outputs */
     SiteCall* d_out = nullptr;
@@ -171,12 +177,14 @@ struct gsnp_context {
     unsigned long long* d_stats = nullptr;
     int* d_bin_count = nullptr;     /* [2 * kNumBins] FP64 bins, then fast bins */
     int32_t* d_bin_tiles = nullptr; /* [2 * kNumBins][n_tiles] */
-    int* d_fix_count = nullptr;     /* [kNumBins] tiles with deferred sites */
-    int32_t* d_fix_tiles = nullptr; /* [kNumBins][n_tiles] */
+    DeferredSite* d_dsites = nullptr;        /* sites the fast kernel deferred */
+    uint32_t* d_dpool = nullptr;             /* their sorted records */
+    unsigned long long* d_dcount = nullptr;  /* [2] requested sites, record words */
+    int64_t dsite_cap = 0, dpool_cap = 0;
     int64_t* d_warp_rng = nullptr;  /* [n_tiles][4][2] */
     int64_t tiles_cap = 0;
     int h_bin_count[2 * kNumBins] = {};
-    int h_fix_count[kNumBins] = {};
+    unsigned long long h_dcount[2] = {0, 0};
     bool called = false;
     uint64_t stats[kNumStats] = {};
     /* CUDA events around each launch of the last calling pass */
@@ -185,6 +193,17 @@ struct gsnp_context {
     gsnp_launch_info launches[kMaxLaunches];
     int n_launches = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
+    /* dictionary codec scratch (-C output) */
+    void* d_dict = nullptr;
+    size_t dict_bytes = 0;
+    /* cns text emission */
+    void* d_emit = nullptr;
+    size_t emit_bytes = 0;
+    char* d_text = nullptr;
+    size_t text_bytes = 0;
+    char* d_chr = nullptr;
+    char* h_text = nullptr;      /* pinned staging of one chunk */
+    size_t h_text_bytes = 0;
 };
 
 namespace {
@@ -216,8 +235,9 @@ void free_all(gsnp_context* c) {
     void* ptrs[] = {c->d_lik64, c->d_lik32, c->d_qadj, c->d_p_prior, c->d_log_prior, c->d_log_prior32,
                     c->d_p_rank, c->d_codes, c->d_snp, c->d_snp_lp, c->d_snp_lp32, c->d_pos, c->d_lenhit,
                     c->d_len, c->d_strand, c->d_bq, c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts,
-                    c->d_lik_keep, c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles, c->d_fix_count,
-                    c->d_fix_tiles, c->d_warp_rng};
+                    c->d_lik_keep, c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles, c->d_dsites,
+                    c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_dict, c->d_win_host_src, c->d_emit,
+                    c->d_text, c->d_chr, c->d_tile_snp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -235,6 +255,7 @@ CallArgs make_args(gsnp_context* c) {
     a.chr_len = c->chr_len;
     a.snp = c->d_snp;
     a.n_snp = c->n_snp;
+    a.tile_snp = c->d_tile_snp;
     a.snp_lp = c->d_snp_lp;
     a.snp_lp32 = c->d_snp_lp32;
     a.lik64 = c->d_lik64;
@@ -262,8 +283,11 @@ CallArgs make_args(gsnp_context* c) {
     a.win_lik_src = c->d_win_lik_src;
     a.n_tiles = (c->chr_len + kTile - 1) / kTile;
     a.warp_rng = c->d_warp_rng;
-    a.fix_count = c->d_fix_count;
-    a.fix_tiles = c->d_fix_tiles;
+    a.dsites = c->d_dsites;
+    a.dpool = c->d_dpool;
+    a.dcount = c->d_dcount;
+    a.dsite_cap = c->dsite_cap;
+    a.dpool_cap = c->dpool_cap;
     a.out = c->d_out;
     a.counts = c->d_counts;
     a.lik_keep = c->d_lik_keep;
@@ -283,9 +307,15 @@ int run_calling(gsnp_context* c) {
     }
     if (n_tiles > c->tiles_cap) {
         CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * 2 * kNumBins), "cudaMalloc bins");
-        CK(dev_alloc(&c->d_fix_tiles, (size_t)n_tiles * kNumBins), "cudaMalloc bins");
         CK(dev_alloc(&c->d_warp_rng, (size_t)n_tiles * kWarpsPerTile * 2), "cudaMalloc ranges");
         c->tiles_cap = n_tiles;
+    }
+    if (c->dsite_cap == 0) {
+        /* deferred sites: about 0.1% of a 30x genome; grown on demand */
+        c->dsite_cap = std::max<int64_t>(1 << 16, c->chr_len / 256);
+        c->dpool_cap = c->dsite_cap * 48;
+        CK(dev_alloc(&c->d_dsites, (size_t)c->dsite_cap), "cudaMalloc deferred");
+        CK(dev_alloc(&c->d_dpool, (size_t)c->dpool_cap), "cudaMalloc deferred");
     }
     if (!c->ev[0])
         for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i) CK(cudaEventCreate(&c->ev[i]), "cudaEventCreate");
@@ -319,28 +349,45 @@ int run_calling(gsnp_context* c) {
         CK(cudaStreamSynchronize(c->stream), "classify");
         bool any_fast = false;
         for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
-        if (any_fast) CK(cudaMemsetAsync(c->d_fix_count, 0, sizeof(int) * kNumBins, c->stream), "memset");
-        for (int b = 0; b < 2 * kNumBins; ++b) {
+        for (int b = 0; b < kNumBins; ++b) {
             if (c->h_bin_count[b] == 0) continue;
-            const int kind = b < kNumBins ? kKindFP64 : kKindFast;
-            k = begin(kind, bin_slots(b % kNumBins), c->h_bin_count[b]);
-            CK(launch_bin(a, kind, b % kNumBins, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b],
-                          c->stream),
+            k = begin(kKindFP64, bin_slots(b), c->h_bin_count[b]);
+            CK(launch_bin(a, kKindFP64, b, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b], c->stream),
                "calling kernel");
             end(k);
         }
         if (!any_fast) continue;
-        /* the FP64 pass over the tiles whose sites the fast kernel deferred */
-        CK(cudaMemcpyAsync(c->h_fix_count, c->d_fix_count, sizeof(c->h_fix_count), cudaMemcpyDeviceToHost,
-                           c->stream),
-           "deferred counts");
-        CK(cudaStreamSynchronize(c->stream), "fast calling");
-        for (int b = 0; b < kNumBins; ++b) {
-            if (c->h_fix_count[b] == 0) continue;
-            k = begin(kKindDeferred, bin_slots(b), c->h_fix_count[b]);
-            CK(launch_bin(a, kKindDeferred, b, c->d_fix_tiles + (int64_t)b * n_tiles, c->h_fix_count[b], c->stream),
-               "deferred calling kernel");
-            end(k);
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            const CallArgs af = make_args(c);
+            const int first = c->n_launches;
+            CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+            for (int b = 0; b < kNumBins; ++b) {
+                const int nb = c->h_bin_count[kNumBins + b];
+                if (nb == 0) continue;
+                k = begin(kKindFast, bin_slots(b), nb);
+                CK(launch_bin(af, kKindFast, b, c->d_bin_tiles + (int64_t)(kNumBins + b) * n_tiles, nb, c->stream),
+                   "fast calling kernel");
+                end(k);
+            }
+            CK(cudaMemcpyAsync(c->h_dcount, c->d_dcount, sizeof(c->h_dcount), cudaMemcpyDeviceToHost, c->stream),
+               "deferred counts");
+            CK(cudaStreamSynchronize(c->stream), "fast calling");
+            const int64_t ns = (int64_t)c->h_dcount[0], nw = (int64_t)c->h_dcount[1];
+            if (ns <= c->dsite_cap && nw <= c->dpool_cap) {
+                k = begin(kKindDeferred, 0, (ns + kTile - 1) / kTile);
+                if (k >= 0) c->launches[k].sites = ns;
+                CK(launch_deferred(af, ns, c->stream), "deferred calling kernel");
+                end(k);
+                break;
+            }
+            if (attempt == 1) return fail(c, GSNP_ERR_STATE, "deferred-site pool overflow");
+            /* grow the pool to what the pass asked for and run it again */
+            c->dsite_cap = std::max(c->dsite_cap, ns + ns / 8 + 1024);
+            c->dpool_cap = std::max(c->dpool_cap, nw + nw / 8 + 65536);
+            CK(dev_alloc(&c->d_dsites, (size_t)c->dsite_cap), "cudaMalloc deferred");
+            CK(dev_alloc(&c->d_dpool, (size_t)c->dpool_cap), "cudaMalloc deferred");
+            CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * kNumStats, c->stream), "memset");
+            c->n_launches = first;
         }
     }
     int err = 0;
@@ -348,7 +395,7 @@ int run_calling(gsnp_context* c) {
     CK(cudaMemcpyAsync(c->stats, c->d_stats, sizeof(c->stats), cudaMemcpyDeviceToHost, c->stream), "stats");
     CK(cudaStreamSynchronize(c->stream), "calling");
     for (int k = 0; k < c->n_launches; ++k) cudaEventElapsedTime(&c->launches[k].ms, c->ev[2 * k], c->ev[2 * k + 1]);
-    if (err == 1) return fail(c, GSNP_ERR_CAPACITY, "a site's count_all exceeds 65535");
+    if (err == 1) return fail(c, GSNP_ERR_CAPACITY, "a site is covered by more than 65535 alignments");
     if (err) return fail(c, GSNP_ERR_STATE, "record slots of a tile overflowed its depth bin");
     c->stats[0] = (uint64_t)c->chr_len;
     c->called = true;
@@ -369,7 +416,7 @@ int gsnp_context_create(int device, gsnp_context** out) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_error, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_stats, sizeof(unsigned long long) * kNumStats);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bin_count, sizeof(int) * 2 * kNumBins);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_fix_count, sizeof(int) * kNumBins);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_dcount, sizeof(unsigned long long) * 2);
     if (e != cudaSuccess) {
         free_all(c);
         delete c;
@@ -385,6 +432,7 @@ void gsnp_context_destroy(gsnp_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_all(c);
+    if (c->h_text) cudaFreeHost(c->h_text);
     for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -442,6 +490,22 @@ int gsnp_load_reference(gsnp_context* c, const uint8_t* codes, int64_t length, c
     CK(dev_alloc(&c->d_codes, (size_t)length), "cudaMalloc codes");
     CK(cudaMemcpy(c->d_codes, codes, (size_t)length, cudaMemcpyHostToDevice), "upload codes");
     static_assert(sizeof(gsnp_snp) == sizeof(DbSnpEntry), "dbSNP row layout");
+    /* the rows are the flagged sites in position order: the kernels find a
+     * site's row from the rows before its tile */
+    int64_t flagged = 0;
+    for (int64_t i = 0; i < length; ++i) flagged += (codes[i] & 8) != 0;
+    if (flagged != n_snp) return fail(c, GSNP_ERR_ARG, "dbSNP rows and flagged site codes differ in number");
+    const int64_t n_tiles = (length + kTile - 1) / kTile;
+    std::vector<int32_t> tile_snp((size_t)n_tiles + 1, 0);
+    for (int64_t k = 0; k < n_snp; ++k) {
+        const int64_t pos = snp[k].pos;
+        if (pos >= length || !(codes[pos] & 8) || (k > 0 && pos <= (int64_t)snp[k - 1].pos))
+            return fail(c, GSNP_ERR_ARG, "dbSNP rows must be ascending, unique and on flagged sites");
+        tile_snp[(size_t)(pos / kTile) + 1] += 1;
+    }
+    for (int64_t t = 0; t < n_tiles; ++t) tile_snp[(size_t)t + 1] += tile_snp[(size_t)t];
+    CK(dev_alloc(&c->d_tile_snp, (size_t)n_tiles + 1), "cudaMalloc tiles");
+    CK(cudaMemcpy(c->d_tile_snp, tile_snp.data(), ((size_t)n_tiles + 1) * 4, cudaMemcpyHostToDevice), "upload");
     c->n_snp = n_snp;
     CK(dev_alloc(&c->d_snp, (size_t)std::max<int64_t>(n_snp, 1)), "cudaMalloc dbsnp");
     if (n_snp > 0) CK(cudaMemcpy(c->d_snp, snp, sizeof(gsnp_snp) * n_snp, cudaMemcpyHostToDevice), "upload dbsnp");
@@ -472,10 +536,13 @@ int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
     if (P.n_windows > c->n_win_alloc) {
         CK(dev_alloc(&c->d_win_flags, (size_t)P.n_windows), "cudaMalloc");
         CK(dev_alloc(&c->d_win_lik_src, (size_t)P.n_windows), "cudaMalloc");
+        CK(dev_alloc(&c->d_win_host_src, (size_t)P.n_windows), "cudaMalloc");
         c->n_win_alloc = P.n_windows;
     }
     CK(cudaMemcpyAsync(c->d_win_flags, P.flags.data(), P.n_windows, cudaMemcpyHostToDevice, c->stream), "upload");
     CK(cudaMemcpyAsync(c->d_win_lik_src, P.lik_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
+       "upload");
+    CK(cudaMemcpyAsync(c->d_win_host_src, P.host_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
        "upload");
     bool need_counts = false, need_lik = false;
     for (int64_t w = 0; w < P.n_windows; ++w) {
@@ -645,32 +712,197 @@ int gsnp_get_stats(gsnp_context* c, uint64_t* s, int n) {
 
 }  // extern "C"
 
-/* cns text: cpp/call_genotype.cc:353-411.  Exposed to format.cpp. */
+/* -C output (columns.cpp) and cns text (emit.cu) */
 namespace gsnp {
-int format_cns_host(const WindowPlan& plan, const std::vector<uint8_t>& codes, const SiteCall* calls,
-                    const SiteCounts* counts, const char* chr_name, std::string* out);
+namespace {
+
+/* the dictionary codec of the -C output on the context's device */
+class GpuDict : public DictCodec {
+public:
+    explicit GpuDict(gsnp_context* c) : c_(c) {}
+    bool compress(const int* in, size_t n, uint32_t* w, unsigned long* nw, int* d, unsigned long* nd,
+                  std::string* err) const override {
+        return run(in, n, w, nw, d, nd, err);
+    }
+    bool compress(const uint32_t* in, size_t n, uint32_t* w, unsigned long* nw, uint32_t* d, unsigned long* nd,
+                  std::string* err) const override {
+        return run(in, n, w, nw, d, nd, err);
+    }
+    bool compress(const double* in, size_t n, uint32_t* w, unsigned long* nw, double* d, unsigned long* nd,
+                  std::string* err) const override {
+        return run(in, n, w, nw, d, nd, err);
+    }
+
+private:
+    gsnp_context* c_;
+    template <class T>
+    bool run(const T* in, size_t n, uint32_t* w, unsigned long* nw, T* d, unsigned long* nd, std::string* err) const {
+        const size_t in_bytes = ((n * sizeof(T) + 255) / 256) * 256;
+        const size_t need = in_bytes + dict_scratch_bytes(n);
+        if (need > c_->dict_bytes) {
+            if (c_->d_dict) cudaFree(c_->d_dict);
+            c_->d_dict = nullptr;
+            c_->dict_bytes = 0;
+            const cudaError_t e = cudaMalloc(&c_->d_dict, need);
+            if (e != cudaSuccess) {
+                *err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+                return false;
+            }
+            c_->dict_bytes = need;
+        }
+        if (n) {
+            const cudaError_t e = cudaMemcpyAsync(c_->d_dict, in, n * sizeof(T), cudaMemcpyHostToDevice, c_->stream);
+            if (e != cudaSuccess) {
+                *err = std::string("upload: ") + cudaGetErrorString(e);
+                return false;
+            }
+        }
+        return dict_compress_device<T>(reinterpret_cast<const T*>(c_->d_dict), n,
+                                       reinterpret_cast<char*>(c_->d_dict) + in_bytes, c_->dict_bytes - in_bytes,
+                                       c_->stream, w, nw, d, nd, err) == 0;
+    }
+};
+
+int fetch_results(gsnp_context* c, std::vector<SiteCall>* calls, std::vector<SiteCounts>* counts) {
+    calls->resize((size_t)c->chr_len);
+    CK(cudaMemcpy(calls->data(), c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost), "fetch");
+    if (c->have_counts) {
+        counts->resize((size_t)c->chr_len);
+        CK(cudaMemcpy(counts->data(), c->d_counts, (size_t)c->chr_len * sizeof(SiteCounts), cudaMemcpyDeviceToHost),
+           "fetch");
+    }
+    return GSNP_OK;
 }
+
+}  // namespace
+}  // namespace gsnp
+
+namespace gsnp {
+namespace {
+
+constexpr int64_t kEmitChunk = 16 * (int64_t)kWin;   /* sites per emission step */
+
+/* Emit the cns text chunk by chunk; sink(text, bytes) receives each chunk's
+ * text in host memory (pinned).  With sink == nullptr only the total size is
+ * computed. */
+template <class Sink>
+int emit_cns(gsnp_context* c, const char* chr_name, uint64_t* total, Sink&& sink, bool write) {
+    const size_t chr_n = strlen(chr_name);
+    if (chr_n > 255) return fail(c, GSNP_ERR_ARG, "chromosome name longer than 255 bytes");
+    if (!c->d_chr) CK(cudaMalloc((void**)&c->d_chr, 256), "cudaMalloc");
+    CK(cudaMemcpyAsync(c->d_chr, chr_name, chr_n, cudaMemcpyHostToDevice, c->stream), "upload");
+    const size_t need = emit_scratch_bytes(std::min<int64_t>(kEmitChunk, c->chr_len));
+    if (need > c->emit_bytes) {
+        if (c->d_emit) cudaFree(c->d_emit);
+        c->d_emit = nullptr;
+        c->emit_bytes = 0;
+        CK(cudaMalloc(&c->d_emit, need), "cudaMalloc emit");
+        c->emit_bytes = need;
+    }
+    CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
+    *total = 0;
+    for (int64_t s0 = 0; s0 < c->chr_len; s0 += kEmitChunk) {
+        EmitArgs e;
+        memset(&e, 0, sizeof(e));
+        e.calls = c->d_out;
+        e.counts = c->have_counts ? c->d_counts : nullptr;
+        e.codes = c->d_codes;
+        e.host_src = c->d_win_host_src;
+        e.chr = c->d_chr;
+        e.chr_n = (int)chr_n;
+        e.site0 = s0;
+        e.n = std::min<int64_t>(kEmitChunk, c->chr_len - s0);
+        e.error = c->d_error;
+        uint64_t bytes = 0;
+        CK(emit_lengths(e, c->d_emit, c->stream, &bytes), "cns text lengths");
+        *total += bytes;
+        if (!write) continue;
+        if (bytes > c->text_bytes) {
+            if (c->d_text) cudaFree(c->d_text);
+            c->d_text = nullptr;
+            c->text_bytes = 0;
+            CK(cudaMalloc((void**)&c->d_text, bytes), "cudaMalloc text");
+            c->text_bytes = bytes;
+        }
+        if (bytes > c->h_text_bytes) {
+            if (c->h_text) cudaFreeHost(c->h_text);
+            c->h_text = nullptr;
+            c->h_text_bytes = 0;
+            CK(cudaMallocHost((void**)&c->h_text, bytes), "cudaMallocHost text");
+            c->h_text_bytes = bytes;
+        }
+        e.text = c->d_text;
+        CK(emit_text(e, c->stream), "cns text");
+        CK(cudaMemcpyAsync(c->h_text, c->d_text, bytes, cudaMemcpyDeviceToHost, c->stream), "download text");
+        CK(cudaStreamSynchronize(c->stream), "cns text");
+        c->d2h_bytes += bytes;
+        if (!sink(c->h_text, bytes)) return fail(c, GSNP_ERR_INPUT, "write failed");
+    }
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
+    CK(cudaStreamSynchronize(c->stream), "cns text");
+    if (err) return fail(c, GSNP_ERR_STATE, "a cns value is outside the text formatter's range");
+    return GSNP_OK;
+}
+
+}  // namespace
+}  // namespace gsnp
 
 extern "C" int gsnp_format_cns(gsnp_context* c, const char* chr_name, char* buf, int64_t* size) {
     if (!c || !chr_name || !size) return fail(c, GSNP_ERR_ARG, "null argument");
     if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
     cudaSetDevice(c->device);
-    std::vector<SiteCall> calls((size_t)c->chr_len);
-    CK(cudaMemcpy(calls.data(), c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost), "fetch");
-    std::vector<SiteCounts> counts;
-    if (c->have_counts) {
-        counts.resize((size_t)c->chr_len);
-        CK(cudaMemcpy(counts.data(), c->d_counts, (size_t)c->chr_len * sizeof(SiteCounts), cudaMemcpyDeviceToHost),
-           "fetch");
-    }
-    std::string text;
-    format_cns_host(c->plan, c->h_codes, calls.data(), c->have_counts ? counts.data() : nullptr, chr_name, &text);
+    uint64_t total = 0;
     if (!buf) {
-        *size = (int64_t)text.size();
+        const int rc = emit_cns(c, chr_name, &total, [](const char*, uint64_t) { return true; }, false);
+        if (rc == GSNP_OK) *size = (int64_t)total;
+        return rc;
+    }
+    const int64_t cap = *size;
+    int64_t at = 0;
+    const int rc = emit_cns(c, chr_name, &total, [&](const char* t, uint64_t n) {
+        const int64_t k = std::min<int64_t>((int64_t)n, cap - at);
+        if (k > 0) memcpy(buf + at, t, (size_t)k);
+        at += std::max<int64_t>(k, 0);
+        return true;
+    }, true);
+    if (rc == GSNP_OK) *size = at;
+    return rc;
+}
+
+extern "C" int gsnp_write_cns(gsnp_context* c, const char* chr_name, const char* path) {
+    if (!c || !chr_name || !path) return fail(c, GSNP_ERR_ARG, "null argument");
+    if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
+    cudaSetDevice(c->device);
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, GSNP_ERR_INPUT, std::string("cannot create ") + path);
+    uint64_t total = 0;
+    const int rc = emit_cns(c, chr_name, &total, [&](const char* t, uint64_t n) {
+        return fwrite(t, 1, n, f) == n;
+    }, true);
+    if (fclose(f) != 0 && rc == GSNP_OK) return fail(c, GSNP_ERR_INPUT, "write failed");
+    return rc;
+}
+
+extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const char* base_path) {
+    if (!c || !base_path) return fail(c, GSNP_ERR_ARG, "null argument");
+    cudaSetDevice(c->device);
+    std::vector<SiteCall> calls;
+    std::vector<SiteCounts> counts;
+    std::string err;
+    GpuDict dict(c);
+    if (!chr_name) {
+        /* text-mode companion files */
+        WindowPlan none;
+        if (write_columns(none, nullptr, nullptr, nullptr, "", base_path, dict, &err) != 0)
+            return fail(c, GSNP_ERR_INPUT, err);
         return GSNP_OK;
     }
-    const int64_t n = std::min<int64_t>(*size, (int64_t)text.size());
-    memcpy(buf, text.data(), (size_t)n);
-    *size = n;
+    if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
+    const int rc = fetch_results(c, &calls, &counts);
+    if (rc != GSNP_OK) return rc;
+    if (write_columns(c->plan, c->h_codes.data(), calls.data(), c->have_counts ? counts.data() : nullptr, chr_name,
+                      base_path, dict, &err) != 0)
+        return fail(c, GSNP_ERR_INPUT, err);
     return GSNP_OK;
 }

@@ -27,7 +27,7 @@ constexpr uint8_t kCallPending = 4;  /* transient: left to the FP64 pass */
 constexpr uint8_t kCallSampled = 8;  /* transient: FP32 accuracy sample */
 
 /* Error bound factor of the FP32 likelihood sums (likelihood_fp32). */
-#define GSNP_FP32_K(n) (5.0 * 0x1p-24 + (double)(n) * 0x1p-45)
+#define GSNP_FP32_K(n) (6.0 * 0x1p-24 + (double)(n) * 0x1p-45)
 
 __device__ __forceinline__ int64_t lower_bound_g(const int32_t* a, int64_t n, int64_t v) {
     int64_t lo = 0, hi = n;
@@ -45,6 +45,28 @@ struct SitePileup {
     uint32_t depth, repeat;
     int dep_uni, num;
 };
+
+/* The pileup counts of one site in 32 bytes: count_uni 4 x 8 bits (at most
+ * 255 unique bases), q_sum and count_all 4 x 16 bits. */
+struct PackedPileup {
+    uint64_t qs4, ca4;
+    uint32_t cu4, depth, repeat;
+    uint16_t dep_uni, num;
+    __host__ __device__ SitePileup unpack() const {
+        SitePileup p;
+        for (int i = 0; i < 4; ++i) {
+            p.cu[i] = (int)((cu4 >> (8 * i)) & 0xff);
+            p.qs[i] = (int)((qs4 >> (16 * i)) & 0xffff);
+            p.ca[i] = (uint32_t)((ca4 >> (16 * i)) & 0xffff);
+        }
+        p.depth = depth;
+        p.repeat = repeat;
+        p.dep_uni = dep_uni;
+        p.num = num;
+        return p;
+    }
+};
+static_assert(sizeof(PackedPileup) == 32, "PackedPileup is 32 bytes");
 
 /* ------------------------------------------------------------------------ */
 /* record walk (kernel/likelihood_kernel.cu:187-255)                          */
@@ -116,11 +138,13 @@ __device__ __forceinline__ void likelihood_fp64(const CallArgs& a, const uint32_
     for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = s[i];
 }
 
-/* FP32 compensated sums: consecutive terms are added in pairs and each pair is
- * Kahan-summed.  Every term is <= 0 (the host checks the table), so sum|x| =
- * |S|, and |S32 - S64| <= |S32| * GSNP_FP32_K(n): the rounding of each term to
- * FP32 (u), of each pair (u), the compensated sum (2u + O(n u^2)) and the FP64
- * sum's own rounding (n 2^-53), u = 2^-24, with a quarter of slack. */
+/* FP32 compensated sums: groups of four consecutive terms are added pairwise,
+ * ((x0 + x1) + (x2 + x3)), and each group sum is Kahan-summed.  Every term is
+ * <= 0 (the host checks the table), so sum|x| = |S|, and
+ * |S32 - S64| <= |S32| * GSNP_FP32_K(n): the rounding of each term to FP32
+ * (u), of the two levels of each group (2u), the compensated sum
+ * (2u + O(n u^2)) and the FP64 sum's own rounding (n 2^-53), u = 2^-24, with
+ * one u of slack. */
 struct Kahan10 {
     float s[10], c[10];
     __device__ __forceinline__ void init() {
@@ -150,22 +174,37 @@ __device__ __forceinline__ void likelihood_fp32(const CallArgs& a, const uint32_
                                                 int num, double* tl, double* eps) {
     Kahan10 k;
     k.init();
-    float h[10];
-    bool half = false;
+    float g0[10], g1[10];
+    int pos = 0;   /* position of the next term in its group of four */
     walk_records<false>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
         float x[10];
         lik32_row(a, qa, coord, o, x);
-        if (!half) {
+        switch (pos) {
+            case 0:
 #pragma unroll
-            for (int v = 0; v < 10; ++v) h[v] = x[v];
-        } else {
+                for (int v = 0; v < 10; ++v) g0[v] = x[v];
+                break;
+            case 1:
 #pragma unroll
-            for (int v = 0; v < 10; ++v) h[v] = __fadd_rn(h[v], x[v]);
-            k.add(h);
+                for (int v = 0; v < 10; ++v) g0[v] = __fadd_rn(g0[v], x[v]);
+                break;
+            case 2:
+#pragma unroll
+                for (int v = 0; v < 10; ++v) g1[v] = x[v];
+                break;
+            default:
+#pragma unroll
+                for (int v = 0; v < 10; ++v) g0[v] = __fadd_rn(g0[v], __fadd_rn(g1[v], x[v]));
+                k.add(g0);
+                break;
         }
-        half = !half;
+        pos = (pos + 1) & 3;
     });
-    if (half) k.add(h);
+    if (pos == 3) {
+#pragma unroll
+        for (int v = 0; v < 10; ++v) g0[v] = __fadd_rn(g0[v], g1[v]);
+    }
+    if (pos != 0) k.add(g0);
     const double kk = GSNP_FP32_K(num);
 #pragma unroll
     for (int i = 0; i < 10; ++i) {
@@ -254,16 +293,6 @@ __device__ __noinline__ double rank_test(const double* p_rank, int q_max_min, co
 /* posterior (kernel/posterior_kernel.cu:680-864)                             */
 /* ------------------------------------------------------------------------ */
 
-__device__ __forceinline__ int64_t find_snp(const CallArgs& a, int64_t site) {
-    int64_t lo = 0, hi = a.n_snp;
-    while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if ((int64_t)a.snp[mid].pos < site) lo = mid + 1;
-        else hi = mid;
-    }
-    return (lo < a.n_snp && (int64_t)a.snp[lo].pos == site) ? lo : -1;
-}
-
 /* base1/base2: the two largest q_sum (count_all when no unique base passed),
  * later base winning ties; the reference base fills in for zero counts */
 struct TopBases {
@@ -348,13 +377,11 @@ __device__ __forceinline__ bool same_call(const SiteCall& x, const SiteCall& y) 
 }
 
 /* log10 genotype priors of a site by genotype code: the prior table of the
- * reference base, or the dbSNP row's (precomputed by snp_log_prior_kernel) */
-__device__ __forceinline__ void load_log_prior(const CallArgs& a, int64_t site, uint8_t ori, double* lp) {
+ * reference base, or, for a dbSNP site in refine mode, its row's
+ * (precomputed by snp_log_prior_kernel; snp_row is the row of the site) */
+__device__ __forceinline__ void load_log_prior(const CallArgs& a, int64_t snp_row, uint8_t ori, double* lp) {
     const double2* src = reinterpret_cast<const double2*>(a.log_prior + ((ori & 7) << 4));
-    if ((ori & 0x8) && a.refine) {
-        const int64_t k = find_snp(a, site);
-        if (k >= 0) src = reinterpret_cast<const double2*>(a.snp_lp + k * 16);
-    }
+    if ((ori & 0x8) && a.refine) src = reinterpret_cast<const double2*>(a.snp_lp + snp_row * 16);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const double2 v = __ldg(src + i);
@@ -446,19 +473,19 @@ __device__ bool site_posterior(const CallArgs& a, uint8_t ori, const SitePileup&
  * homozygous (the rank-sum value is then 1 and its log10 0).  s holds the FP32
  * likelihood sums by table column, num the record count.  Returns false,
  * writing nothing, when the best genotype is heterozygous or when the FP32
- * values do not prove the FP64 decisions: with E_g a bound of |tp32[g] -
- * tp64[g]| (the likelihood bound, the FP32 rounding of the prior and of the
- * addition), type1 must lead every other genotype and type2 every remaining
- * one by more than the sum of their bounds, and the truncated, clamped quality
- * must be the same at both ends of the interval that holds the FP64 value. */
-__device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t site, uint8_t ori, const SitePileup& p,
+ * values do not prove the FP64 decisions.  With E_g a bound of
+ * |tp32[g] - tp64[g]| (the likelihood bound, the FP32 rounding of the prior
+ * and of the addition) and E one bound for every genotype:
+ *   - type1 must lead the runner-up value v2 by more than E1 + E, so that it
+ *     leads every other genotype in FP64 too;
+ *   - the consensus quality depends on tp64[type1] minus the largest other
+ *     tp64, which lies within E1 + E of v1 - v2; the truncated, clamped
+ *     quality must be the same at both ends of that interval. */
+__device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t snp_row, uint8_t ori, const SitePileup& p,
                                                const float* s, int num, SiteCall* out) {
     const int ori7 = ori & 7;
     const float* src = a.log_prior32 + ori7 * 12;
-    if ((ori & 0x8) && a.refine) {
-        const int64_t k = find_snp(a, site);
-        if (k >= 0) src = a.snp_lp32 + k * 12;
-    }
+    if ((ori & 0x8) && a.refine) src = a.snp_lp32 + snp_row * 12;
     float lp[10];
     {
         const float4* s4 = reinterpret_cast<const float4*>(src);
@@ -467,36 +494,35 @@ __device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t site, 
         lp[4] = x1.x; lp[5] = x1.y; lp[6] = x1.z; lp[7] = x1.w;
         lp[8] = x2.x; lp[9] = x2.y;
     }
-    const float kk = __fadd_rn(5.0f * 0x1p-24f, __fmul_rn((float)num, 0x1p-45f));
-    const float grow = 1.0f + 0x1p-20f;
-    float tp[10], E[10];
-    int g1 = -1, g2 = -1;
-    float v1 = 0.f, v2 = 0.f, e1 = 0.f, e2 = 0.f;
+    int g1 = -1;
+    float v1 = 0.f, v2 = -INFINITY, s1 = 0.f, l1 = 0.f, smax = 0.f, lmax = 0.f;
 #pragma unroll
     for (int t = 0; t < 10; ++t) {
         const int g = genotype_of(t);
-        tp[t] = __fadd_rn(s[t], lp[t]);
-        E[t] = isinf(tp[t]) ? 0.f
-                            : __fmul_rn(__fadd_rn(__fmul_rn(fabsf(s[t]), kk),
-                                                  __fmul_rn(__fadd_rn(fabsf(lp[t]), fabsf(tp[t])), 0x1p-23f)),
-                                        grow);
         if (a.monoploid && (g >> 2) != (g & 3)) continue;
-        if (g1 < 0 || tp[t] >= v1) { g2 = g1; v2 = v1; e2 = e1; g1 = g; v1 = tp[t]; e1 = E[t]; }
-        else if (g2 < 0 || tp[t] >= v2) { g2 = g; v2 = tp[t]; e2 = E[t]; }
+        const float tp = __fadd_rn(s[t], lp[t]);
+        smax = fmaxf(smax, fabsf(s[t]));
+        lmax = fmaxf(lmax, fabsf(lp[t]));
+        if (g1 < 0 || tp >= v1) {
+            if (g1 >= 0) v2 = v1;
+            g1 = g; v1 = tp; s1 = s[t]; l1 = lp[t];
+        } else {
+            v2 = fmaxf(v2, tp);
+        }
     }
     if ((g1 >> 2) != (g1 & 3)) return false;
-#pragma unroll
-    for (int t = 0; t < 10; ++t) {
-        const int g = genotype_of(t);
-        if ((a.monoploid && (g >> 2) != (g & 3)) || g == g1) continue;
-        if (!(__fsub_rn(v1, tp[t]) > __fmul_rn(__fadd_rn(e1, E[t]), grow))) return false;
-        if (g == g2) continue;
-        if (!(__fsub_rn(v2, tp[t]) > __fmul_rn(__fadd_rn(e2, E[t]), grow))) return false;
-    }
+    /* |s - S64| <= |s| k; the prior's rounding <= 2^-24 |lp|; the addition's
+     * <= 2^-24 |tp| <= 2^-24 (|s| + |lp|) */
+    const float kk = __fadd_rn(6.0f * 0x1p-24f, __fmul_rn((float)num, 0x1p-45f));
+    const float grow = 1.0f + 0x1p-20f;
+    const float kk1 = __fadd_rn(kk, 0x1p-23f);
+    const float e1 = __fmul_rn(__fadd_rn(__fmul_rn(fabsf(s1), kk1), __fmul_rn(fabsf(l1), 0x1p-22f)), grow);
+    const float e = __fmul_rn(__fadd_rn(__fmul_rn(smax, kk1), __fmul_rn(lmax, 0x1p-22f)), grow);
+    const float margin = __fmul_rn(__fadd_rn(e1, e), grow);
+    if (!(__fsub_rn(v1, v2) > margin)) return false;
     const TopBases tb = top_bases(p, ori7);
     const float raw = __fmul_rn(10.f, __fsub_rn(v1, v2));
-    const float delta = __fadd_rn(__fmul_rn(__fmul_rn(10.f, __fadd_rn(e1, e2)), grow),
-                                  __fmul_rn(__fadd_rn(fabsf(raw), 1.f), 0x1p-20f));
+    const float delta = __fadd_rn(__fmul_rn(10.f, margin), __fmul_rn(__fadd_rn(fabsf(raw), 1.f), 0x1p-20f));
     const int q = finalize_q(__float2int_rz(__fsub_rn(raw, delta)), true, false, tb, g1);
     if (q != finalize_q(__float2int_rz(__fadd_rn(raw, delta)), true, false, tb, g1)) return false;
     fill_call(out, p, tb, g1, q, false, 1.0);

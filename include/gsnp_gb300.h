@@ -7,9 +7,10 @@
  * device state lives in the context until gsnp_context_destroy().
  *
  * Two ways in:
- *   1. Whole chromosome (this build's fast path): gsnp_load_tables,
- *      gsnp_load_reference, gsnp_call_chromosome, then gsnp_fetch_sites or
- *      gsnp_format_cns.  One call replaces the reference's window loop
+ *   1. Whole chromosome (this library): gsnp_load_reference,
+ *      gsnp_calibrate, gsnp_load_tables, gsnp_call_chromosome, then
+ *      gsnp_fetch_sites, gsnp_write_cns / gsnp_format_cns or
+ *      gsnp_write_columns.  One call replaces the reference's window loop
  *      Call_win::new_soap2cns (cpp/call_genotype.cc:422-669) and, per window,
  *      cuda_updateSparse / cuda_likelihoodSparse / cuda_posterior
  *      (kernel/update_kernel.cu:328, kernel/likelihood_kernel.cu:262,
@@ -17,8 +18,9 @@
  *      host arrays in gap windows, the dropped last read, the reused
  *      likelihood) are reproduced, so the output bytes are the reference's.
  *   2. Window by window, the reference's own entry points, declared with
- *      their original C++ names in gsnp_backend.h and implemented on top of
- *      this context (gsnp_gb300/csrc/compat.cu).
+ *      their original C++ names in gsnp_backend.h and implemented with the
+ *      window state resident on the device in a separate library,
+ *      libgsnp_backend.so (gsnp_gb300/csrc/compat.cu).
  */
 #ifndef GSNP_GB300_H
 #define GSNP_GB300_H
@@ -110,7 +112,9 @@ int gsnp_load_tables(gsnp_context* ctx, const gsnp_params* params, const double*
 
 /* Reference of the called chromosome: one 4-bit site code per byte
  * (bit 3 dbSNP, bit 2 N, bits 1:0 base ACTG; cpp/chromosome.cc:28-64) and its
- * dbSNP rows sorted by position. */
+ * dbSNP rows: one row per flagged site, ascending by position, as the
+ * reference's loader builds them (cpp/chromosome.cc:197-216).  Rows that do
+ * not match the flags are GSNP_ERR_ARG. */
 int gsnp_load_reference(gsnp_context* ctx, const uint8_t* site_codes, int64_t length, const gsnp_snp* snp,
                         int64_t n_snp);
 
@@ -138,10 +142,22 @@ int gsnp_recall_resident(gsnp_context* ctx);
 /* Copy calls for sites [first, first + count) to host memory. */
 int gsnp_fetch_sites(gsnp_context* ctx, int64_t first, int64_t count, gsnp_site_call* out);
 
-/* Format the cns text of the whole chromosome (cpp/call_genotype.cc:353-411).
- * With buf == NULL, *size receives the number of bytes; otherwise up to *size
- * bytes are written and *size receives the count. */
+/* Format the cns text of the whole chromosome (cpp/call_genotype.cc:353-411)
+ * on the device.  With buf == NULL, *size receives the number of bytes;
+ * otherwise up to *size bytes are written and *size receives the count. */
 int gsnp_format_cns(gsnp_context* ctx, const char* chr_name, char* buf, int64_t* size);
+
+/* Write the cns text of the whole chromosome to the file at path, formatted
+ * on the device chunk by chunk. */
+int gsnp_write_cns(gsnp_context* ctx, const char* chr_name, const char* path);
+
+/* Write the -C compressed output of the last call (cpp/compress.h:86-1312,
+ * written by cpp/call_genotype.cc:440-452,616-660): the six files
+ * <base_path>.1_2, .3_4_6, .5_7_8_9_14_16, .10, .11_12_13 and .15_17, byte for
+ * byte as the reference writes them, the dictionary codec running on the
+ * device.  With chr_name == NULL the files a text-mode run leaves are written
+ * instead (.1_2 holding "0", the others empty). */
+int gsnp_write_columns(gsnp_context* ctx, const char* chr_name, const char* base_path);
 
 /* One kernel launch of the last calling pass, timed with CUDA events on the
  * context's stream. */

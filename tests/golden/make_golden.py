@@ -1,0 +1,99 @@
+#!/usr/bin/env python
+"""Generate tests/golden/golden.json: SHA-256 digests of the reference's own
+outputs on seeded inputs.
+
+Each case writes a seeded synthetic workload (gsnp_gb300.synth) as the
+reference's input files and runs oracle/_ref/gsnp_ref on them.  That binary is
+the reference's own host code (cpp/main.cc, call_genotype.cc, matrix.cc,
+prior.cc, rank_sum.cc, chromosome.cc, normal_dis.cc, compiled in place from
+the reference tree by `make -C oracle ref`) over the restated backend. The
+digests of the inputs and of every output file (cns text, the -C files, the
+-M matrix) are recorded.  The reference tree is needed to run this script;
+the tests that read golden.json are not.
+
+    python tests/golden/make_golden.py [--ref /path/to/reference]
+"""
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+# (case id, config, scale, -C)
+CASES = [
+    ("c0_text", "c0", 0.1, False),
+    ("c0_C", "c0", 0.1, True),
+    ("c1_text", "c1", 0.004, False),
+    ("c1_C", "c1", 0.004, True),
+    ("c2_text", "c2", 0.01, False),
+    ("c3_text", "c3", 0.004, False),
+    ("c4_text", "c4", 0.0101, False),   # -C aborts in the reference here (empty dictionary assert)
+]
+
+
+def sha(data: bytes) -> str:
+    return hashlib.sha256(data).hexdigest()
+
+
+def case_flags(w, paths, compress):
+    flags = [f for f in w.cli_flags(paths.get("dbsnp")) if f != "-C"]
+    if compress:
+        flags.append("-C")
+    return flags
+
+
+def inputs(name, scale, directory):
+    from gsnp_gb300 import synth
+    w = synth.make_workload(name, scale=scale)
+    paths = synth.write_inputs(w, directory)
+    digests = {}
+    for k, p in sorted(paths.items()):
+        with open(p, "rb") as f:
+            digests[k] = sha(f.read())
+    return w, paths, digests
+
+
+def run_and_digest(binary, paths, flags, out_dir):
+    os.makedirs(out_dir, exist_ok=True)
+    r = subprocess.run([binary, "-i", paths["soap"], "-d", paths["ref"], "-o", os.path.join(out_dir, "cns"),
+                        "-M", os.path.join(out_dir, "mat")] + flags, cwd=out_dir, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    out = {}
+    for f in sorted(os.listdir(out_dir)):
+        if f.startswith("cns") or f == "mat":
+            with open(os.path.join(out_dir, f), "rb") as fh:
+                out[f] = sha(fh.read())
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + args.ref])
+    if r.returncode:
+        sys.exit("cannot build the reference host code")
+    ref_bin = os.path.join(ROOT, "oracle", "_ref", "gsnp_ref")
+    golden = {}
+    for cid, name, scale, compress in CASES:
+        with tempfile.TemporaryDirectory() as d:
+            w, paths, in_digests = inputs(name, scale, d)
+            flags = case_flags(w, paths, compress)
+            outs = run_and_digest(ref_bin, paths, flags, os.path.join(d, "out"))
+        golden[cid] = {"config": name, "scale": scale, "compress": compress,
+                       "flags": [f if not os.path.isabs(f) else os.path.basename(f) for f in flags],
+                       "inputs": in_digests, "outputs": outs}
+        print(cid, len(outs), "files")
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump(golden, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()
