@@ -66,9 +66,8 @@ __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v)
 template <int SLOTS>
 __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
                                                    bool active, uint32_t* recs) {
-    /* records are appended in pileup order, then each lane sorts its own
-     * column once: the lanes of a warp then diverge over one sort each rather
-     * than over every insertion */
+    /* records are appended in pileup order; sort_column puts them in
+     * ascending order once the tile's columns are dealt to the threads */
     const int lane = threadIdx.x & 31;
     const int L = a.L;
     const signed char qmin = (signed char)a.qmin;
@@ -126,7 +125,19 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
     }
     if (overflow) atomicExch(a.error, 2);
     if (depth > 0xffff) atomicExch(a.error, 1);
-    /* ascending insertion sort of the column */
+    PackedPileup pk;
+    pk.cu4 = cu4;
+    pk.qs4 = qs4;
+    pk.ca4 = ca4;
+    pk.depth = depth;
+    pk.repeat = repeat;
+    pk.dep_uni = (uint16_t)dep_uni;
+    pk.num = (uint16_t)num;
+    return pk;
+}
+
+/* ascending insertion sort of one site's record column */
+__device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
     for (int i = 1; i < num; ++i) {
         const uint32_t w = recs[i * kTile];
         int j = i;
@@ -138,15 +149,6 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
         }
         recs[j * kTile] = w;
     }
-    PackedPileup pk;
-    pk.cu4 = cu4;
-    pk.qs4 = qs4;
-    pk.ca4 = ca4;
-    pk.depth = depth;
-    pk.repeat = repeat;
-    pk.dep_uni = (uint16_t)dep_uni;
-    pk.num = (uint16_t)num;
-    return pk;
 }
 
 /* dbSNP row of each flagged site of a tile: the rows before the tile plus the
@@ -162,15 +164,16 @@ __device__ __forceinline__ int32_t tile_snp_row(const CallArgs& a, int64_t tile,
     return flagged ? a.tile_snp[tile] + before + __popc(b & ((1u << lane) - 1u)) : -1;
 }
 
-/* Shared state of a tile after its pileup, re-dealt to the threads in order of
- * record count so that the lanes of a warp walk columns of similar depth.  The
- * packed counts of the tile's sites (kTile entries) are passed through the
- * pcr-bitset area of the dynamic shared memory, which is free until the
- * record walk. */
-template <int SLOTS>
+/* Shared state of a tile after its pileup, re-dealt to the threads by record
+ * count.  The columns c, c+32, c+64, c+96 share shared-memory banks; the four
+ * sites of each such class go to the four warps in order of record count, so
+ * that each warp walks columns of similar depth while a warp's lanes still
+ * touch 32 distinct banks.  The packed counts of the tile's sites pass
+ * through the pcr-bitset area of the dynamic shared memory, which is free
+ * until the record walk. */
 struct TileDeal {
     int32_t snp_row[kTile];
-    int hist[SLOTS + 2];
+    int num[kTile];
     int perm[kTile];
     uint8_t ori[kTile];
     int cnt[kWarpsPerTile];
@@ -178,43 +181,23 @@ struct TileDeal {
 
 /* Returns the tile column (site offset) this thread calls from here on and
  * its pileup counts; the pcr-bitset area may be written once it returns. */
-template <int SLOTS>
-__device__ __forceinline__ int deal_by_depth(TileDeal<SLOTS>& d, PackedPileup* pk_area, const PackedPileup& pk,
-                                             bool active, uint8_t ori, int32_t snp_row, SitePileup* p) {
-    const int t = threadIdx.x;
-    for (int i = t; i < SLOTS + 2; i += kTile) d.hist[i] = 0;
+__device__ __forceinline__ int deal_by_depth(TileDeal& d, PackedPileup* pk_area, const PackedPileup& pk, bool active,
+                                             uint8_t ori, int32_t snp_row, SitePileup* p) {
+    const int t = threadIdx.x, lane = t & 31;
     pk_area[t] = pk;
     d.snp_row[t] = snp_row;
     d.ori[t] = ori;
+    const int key = active ? (int)pk.num : -1;
+    d.num[t] = key;
     __syncthreads();
-    const int key = active ? (int)pk.num + 1 : 0;
-    atomicAdd(&d.hist[key], 1);
-    __syncthreads();
-    if (t < 32) {
-        /* exclusive scan of the SLOTS + 2 counts by one warp */
-        constexpr int per = (SLOTS + 2 + 31) / 32;
-        int v[per], sum = 0;
+    int rank = 0;
 #pragma unroll
-        for (int k = 0; k < per; ++k) {
-            const int i = t * per + k;
-            v[k] = i < SLOTS + 2 ? d.hist[i] : 0;
-            sum += v[k];
-        }
-        int x = sum;
-        for (int off = 1; off < 32; off <<= 1) {
-            const int y = __shfl_up_sync(kFull, x, off);
-            if (t >= off) x += y;
-        }
-        int run = x - sum;
-#pragma unroll
-        for (int k = 0; k < per; ++k) {
-            const int i = t * per + k;
-            if (i < SLOTS + 2) d.hist[i] = run;
-            run += v[k];
-        }
+    for (int k = 0; k < kWarpsPerTile; ++k) {
+        const int c = k * 32 + lane;
+        const int kc = d.num[c];
+        rank += (kc < key || (kc == key && c < t)) ? 1 : 0;
     }
-    __syncthreads();
-    d.perm[atomicAdd(&d.hist[key], 1)] = t;
+    d.perm[rank * 32 + lane] = t;
     __syncthreads();
     const int me = d.perm[t];
     *p = pk_area[me].unpack();
@@ -371,7 +354,7 @@ __global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const 
     uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);                   /* [SLOTS][kTile] */
     uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;    /* [nw][kTile] */
 
-    __shared__ TileDeal<SLOTS> deal;
+    __shared__ TileDeal deal;
     const int t = threadIdx.x, warp = t >> 5;
     const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
@@ -384,13 +367,13 @@ __global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const 
     const int32_t row_t = tile_snp_row(a, tile, (ori_t & 8) != 0, deal.cnt);
     const PackedPileup pk = warp_pileup<SLOTS>(a, r_lo, r_hi, s0 + t, active_t, recs_all + t);
     SitePileup p;
-    const int me = deal_by_depth<SLOTS>(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t,
-                                        &p);
+    const int me = deal_by_depth(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t, &p);
     const int64_t site = s0 + me;
     if (site >= a.chr_len) return;
     const uint8_t ori = deal.ori[me];
     uint32_t* recs = recs_all + me;
     uint32_t* seen = seen_all + me;
+    sort_column(recs, p.num);
 
     double tl[16];
 #pragma unroll
@@ -434,7 +417,7 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
     extern __shared__ __align__(16) uint8_t smem[];
     uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);
     uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;
-    __shared__ TileDeal<SLOTS> deal;
+    __shared__ TileDeal deal;
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t tile = tiles[blockIdx.x];
@@ -448,12 +431,12 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
     const int32_t row_t = tile_snp_row(a, tile, (ori_t & 8) != 0, deal.cnt);
     const PackedPileup pk = warp_pileup<SLOTS>(a, r_lo, r_hi, s0 + t, active_t, recs_all + t);
     SitePileup p;
-    const int me = deal_by_depth<SLOTS>(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t,
-                                        &p);
+    const int me = deal_by_depth(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t, &p);
     const int64_t site = s0 + me;
     const bool active = site < a.chr_len;
     uint32_t* recs = recs_all + me;
     uint32_t* seen = seen_all + me;
+    if (active) sort_column(recs, p.num);
 
     uint8_t dflags = 0;
     if (active) {

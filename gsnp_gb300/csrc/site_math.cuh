@@ -239,7 +239,8 @@ __device__ __forceinline__ double normal_value(double z) {
                  b5 = 1.330274429, p = 0.2316419, c2 = 0.39894228;
     const double aa = fabs(z);
     const double t = GSNP_DDIV(1.0, GSNP_DADD(1.0, GSNP_DMUL(aa, p)));
-    const double b = GSNP_DMUL(c2, gsnp_cr_exp(GSNP_DMUL(-z, GSNP_DDIV(z, 2.0))));
+    /* z / 2 is computed as z * 0.5: halving is exact, so the value is the same */
+    const double b = GSNP_DMUL(c2, gsnp_cr_exp(GSNP_DMUL(-z, GSNP_DMUL(z, 0.5))));
     double n = GSNP_DADD(GSNP_DMUL(b5, t), b4);
     n = GSNP_DADD(GSNP_DMUL(n, t), b3);
     n = GSNP_DADD(GSNP_DMUL(n, t), b2);
@@ -278,7 +279,10 @@ __device__ __noinline__ double rank_test(const double* p_rank, int q_max_min, co
     const int top = min(64, q_max_min + 1);
     for (int q = 0; q <= top; ++q) {
         const int c = ca[q] + cb[q];
-        const double ra = GSNP_DADD((double)rank, GSNP_DDIV((double)(1 + c), 2.0));
+        /* an empty bin adds +0.0 to the non-negative sums: skipping it is
+         * exact; (1 + c) / 2 is computed as (1 + c) * 0.5, which is exact */
+        if (c == 0) continue;
+        const double ra = GSNP_DADD((double)rank, GSNP_DMUL((double)(1 + c), 0.5));
         Ta = GSNP_DADD(Ta, GSNP_DMUL(ra, (double)ca[q]));
         Tb = GSNP_DADD(Tb, GSNP_DMUL(ra, (double)cb[q]));
         rank += c;
@@ -473,14 +477,18 @@ __device__ bool site_posterior(const CallArgs& a, uint8_t ori, const SitePileup&
  * homozygous (the rank-sum value is then 1 and its log10 0).  s holds the FP32
  * likelihood sums by table column, num the record count.  Returns false,
  * writing nothing, when the best genotype is heterozygous or when the FP32
- * values do not prove the FP64 decisions.  With E_g a bound of
- * |tp32[g] - tp64[g]| (the likelihood bound, the FP32 rounding of the prior
- * and of the addition) and E one bound for every genotype:
- *   - type1 must lead the runner-up value v2 by more than E1 + E, so that it
- *     leads every other genotype in FP64 too;
- *   - the consensus quality depends on tp64[type1] minus the largest other
- *     tp64, which lies within E1 + E of v1 - v2; the truncated, clamped
- *     quality must be the same at both ends of that interval. */
+ * values do not prove the FP64 decisions.
+ *
+ * E_g bounds |tp32[g] - tp64[g]| (the likelihood bound, the FP32 rounding of
+ * the prior and of the addition).  With v1 = tp32[type1], v2 the largest
+ * other tp32 (genotype g2), d = v1 - v2 and B = max over the others of
+ * tp32[g] - v2 + E_g:
+ *   tp64[type1] - max(other tp64) lies in [d - E1 - B, d + E1 + E_g2],
+ * so type1 is the FP64 best when d > E1 + B, and the truncated, clamped
+ * quality is proven when it is the same at both ends of that interval.
+ * Every quantity is formed as a difference first, so that each FP32 rounding
+ * is relative to these small values; the bounds are then grown to cover
+ * those roundings. */
 __device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t snp_row, uint8_t ori, const SitePileup& p,
                                                const float* s, int num, SiteCall* out) {
     const int ori7 = ori & 7;
@@ -494,37 +502,57 @@ __device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t snp_ro
         lp[4] = x1.x; lp[5] = x1.y; lp[6] = x1.z; lp[7] = x1.w;
         lp[8] = x2.x; lp[9] = x2.y;
     }
-    int g1 = -1;
-    float v1 = 0.f, v2 = -INFINITY, s1 = 0.f, l1 = 0.f, smax = 0.f, lmax = 0.f;
+    /* |s - S64| <= |s| k; the prior's rounding <= 2^-24 |lp|; the addition's
+     * <= 2^-24 |tp| <= 2^-24 (|s| + |lp|); grown by 2^-20 for the rounding of
+     * the bound itself */
+    const float kk1 = __fadd_rn(__fadd_rn(6.0f * 0x1p-24f, __fmul_rn((float)num, 0x1p-45f)), 0x1p-23f);
+    const float grow = 1.0f + 0x1p-20f;
+    float tp[10], E[10];
+    int t1 = -1;
+    float v1 = 0.f;
+#pragma unroll
+    for (int t = 0; t < 10; ++t) {
+        const int g = genotype_of(t);
+        tp[t] = __fadd_rn(s[t], lp[t]);
+        E[t] = __fmul_rn(__fadd_rn(__fmul_rn(fabsf(s[t]), kk1), __fmul_rn(fabsf(lp[t]), 0x1p-22f)), grow);
+        if (a.monoploid && (g >> 2) != (g & 3)) continue;
+        if (t1 < 0 || tp[t] >= v1) { t1 = t; v1 = tp[t]; }
+    }
+    const int g1 = genotype_of(t1);
+    if ((g1 >> 2) != (g1 & 3)) return false;
+    float e1 = 0.f, v2 = -INFINITY, e2 = 0.f, emax = 0.f;
 #pragma unroll
     for (int t = 0; t < 10; ++t) {
         const int g = genotype_of(t);
         if (a.monoploid && (g >> 2) != (g & 3)) continue;
-        const float tp = __fadd_rn(s[t], lp[t]);
-        smax = fmaxf(smax, fabsf(s[t]));
-        lmax = fmaxf(lmax, fabsf(lp[t]));
-        if (g1 < 0 || tp >= v1) {
-            if (g1 >= 0) v2 = v1;
-            g1 = g; v1 = tp; s1 = s[t]; l1 = lp[t];
-        } else {
-            v2 = fmaxf(v2, tp);
+        if (t == t1) {
+            e1 = E[t];
+            continue;
         }
+        if (tp[t] >= v2) { v2 = tp[t]; e2 = E[t]; }
+        emax = fmaxf(emax, E[t]);
     }
-    if ((g1 >> 2) != (g1 & 3)) return false;
-    /* |s - S64| <= |s| k; the prior's rounding <= 2^-24 |lp|; the addition's
-     * <= 2^-24 |tp| <= 2^-24 (|s| + |lp|) */
-    const float kk = __fadd_rn(6.0f * 0x1p-24f, __fmul_rn((float)num, 0x1p-45f));
-    const float grow = 1.0f + 0x1p-20f;
-    const float kk1 = __fadd_rn(kk, 0x1p-23f);
-    const float e1 = __fmul_rn(__fadd_rn(__fmul_rn(fabsf(s1), kk1), __fmul_rn(fabsf(l1), 0x1p-22f)), grow);
-    const float e = __fmul_rn(__fadd_rn(__fmul_rn(smax, kk1), __fmul_rn(lmax, 0x1p-22f)), grow);
-    const float margin = __fmul_rn(__fadd_rn(e1, e), grow);
-    if (!(__fsub_rn(v1, v2) > margin)) return false;
+    float B = 0.f;
+#pragma unroll
+    for (int t = 0; t < 10; ++t) {
+        const int g = genotype_of(t);
+        if ((a.monoploid && (g >> 2) != (g & 3)) || t == t1) continue;
+        B = fmaxf(B, __fadd_rn(__fsub_rn(tp[t], v2), E[t]));
+    }
+    /* |fl(tp - v2 + E) - (tp - v2 + E)| <= 2^-23 (|tp - v2| + E) <= 2^-22 E at
+     * the maximum, which is covered by emax 2^-21 */
+    B = __fmul_rn(__fadd_rn(B, __fmul_rn(emax, 0x1p-21f)), grow);
+    if (!(isfinite(v1) && isfinite(v2) && isfinite(B))) return false;
+    const float d = __fsub_rn(v1, v2);                       /* error <= 2^-24 |d| */
+    const float below = __fmul_rn(__fadd_rn(e1, B), grow);   /* >= E1 + B */
+    const float above = __fmul_rn(__fadd_rn(e1, e2), grow);  /* >= E1 + E_g2 */
+    if (!(__fsub_rn(__fmul_rn(d, 1.0f - 0x1p-22f), below) > 0.f)) return false;
     const TopBases tb = top_bases(p, ori7);
-    const float raw = __fmul_rn(10.f, __fsub_rn(v1, v2));
-    const float delta = __fadd_rn(__fmul_rn(10.f, margin), __fmul_rn(__fadd_rn(fabsf(raw), 1.f), 0x1p-20f));
-    const int q = finalize_q(__float2int_rz(__fsub_rn(raw, delta)), true, false, tb, g1);
-    if (q != finalize_q(__float2int_rz(__fadd_rn(raw, delta)), true, false, tb, g1)) return false;
+    const float raw_lo = __fmul_rn(10.f, __fsub_rn(d, below));
+    const float raw_hi = __fmul_rn(10.f, __fadd_rn(d, above));
+    const float slack = __fmul_rn(__fadd_rn(fabsf(raw_hi), 1.f), 0x1p-19f);
+    const int q = finalize_q(__float2int_rz(__fsub_rn(raw_lo, slack)), true, false, tb, g1);
+    if (q != finalize_q(__float2int_rz(__fadd_rn(raw_hi, slack)), true, false, tb, g1)) return false;
     fill_call(out, p, tb, g1, q, false, 1.0);
     return true;
 }
