@@ -253,6 +253,124 @@ int dict_compress_device(const T* d_in, size_t n, void* d_scratch, size_t scratc
     return 0;
 }
 
+/* ---- the same codec over caller-provided scratch, with no allocation ---- */
+
+namespace {
+
+template <class T> __device__ T dev_value(uint64_t k, bool negzero);
+template <> __device__ char dev_value<char>(uint64_t k, bool) { return (char)(signed char)((int64_t)k - 128); }
+template <> __device__ int dev_value<int>(uint64_t k, bool) { return (int)((int64_t)k - 2147483648LL); }
+template <> __device__ unsigned int dev_value<unsigned int>(uint64_t k, bool) { return (unsigned int)k; }
+template <> __device__ double dev_value<double>(uint64_t k, bool negzero) {
+    uint64_t b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+    if (b == 0 && negzero) b = 0x8000000000000000ULL;
+    return __longlong_as_double((long long)b);
+}
+
+template <class T>
+__global__ void values_kernel(const uint64_t* __restrict__ keys, size_t d, const int* __restrict__ flags,
+                              T* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d) out[i] = dev_value<T>(keys[i], (*flags & 1) != 0);
+}
+
+size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+void static_layout(size_t n, size_t elem, size_t* cap, size_t* m, size_t offs[7]) {
+    *cap = 1;
+    while (*cap < 2 * n) *cap <<= 1;
+    *m = 1;
+    while (*m < n) *m <<= 1;
+    offs[0] = 0;                                   /* input values */
+    offs[1] = offs[0] + round256(n * elem);        /* hash table [cap] */
+    offs[2] = offs[1] + round256(*cap * 8);        /* sorted keys [m] */
+    offs[3] = offs[2] + round256(*m * 8);          /* indices [n] */
+    offs[4] = offs[3] + round256(n * 4);           /* packed words [n] */
+    offs[5] = offs[4] + round256(n * 4);           /* count, flags */
+    offs[6] = offs[5] + 256;                       /* dictionary values [n] */
+}
+
+}  // namespace
+
+size_t dict_static_bytes(size_t n, size_t elem) {
+    size_t cap, m, offs[7];
+    static_layout(n, elem, &cap, &m, offs);
+    return offs[6] + round256(n * elem);
+}
+
+template <class T>
+int dict_compress_prealloc(const T* h_in, size_t n, void* d_scratch, size_t scratch_bytes, cudaStream_t stream,
+                           uint32_t* h_words, unsigned long* n_words, T* h_dict, unsigned long* n_dict) {
+    if (*n_dict < n) return 4;
+    if (n == 0) {
+        *n_dict = 0;
+        *n_words = 0;
+        return 0;
+    }
+    size_t cap, m, offs[7];
+    static_layout(n, sizeof(T), &cap, &m, offs);
+    if (offs[6] + round256(n * sizeof(T)) > scratch_bytes) return 4;
+    uint8_t* p = (uint8_t*)d_scratch;
+    T* in = (T*)(p + offs[0]);
+    uint64_t* table = (uint64_t*)(p + offs[1]);
+    uint64_t* keys = (uint64_t*)(p + offs[2]);
+    uint32_t* idx = (uint32_t*)(p + offs[3]);
+    uint32_t* words = (uint32_t*)(p + offs[4]);
+    unsigned long long* count = (unsigned long long*)(p + offs[5]);
+    int* flags = (int*)(count + 1);
+    T* vals = (T*)(p + offs[6]);
+    cudaError_t e = cudaMemcpyAsync(in, h_in, n * sizeof(T), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(table, 0xff, cap * 8, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, 16, stream);
+    if (e != cudaSuccess) return 1;
+    insert_kernel<T><<<blocks(n, 256), 256, 0, stream>>>(in, n, table, cap - 1, flags);
+    compact_kernel<<<blocks(cap, 256), 256, 0, stream>>>(table, cap, keys, count);
+    unsigned long long d = 0;
+    int hflags = 0;
+    e = cudaMemcpyAsync(&d, count, 8, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hflags, flags, 4, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return 1;
+    if (hflags & 2) return 4;
+    size_t md = 1;
+    while (md < d) md <<= 1;
+    if (md > d && cudaMemsetAsync(keys + d, 0xff, (md - d) * 8, stream) != cudaSuccess) return 1;
+    if (md <= 8192) {
+        if (cudaFuncSetAttribute(bitonic_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 8) !=
+            cudaSuccess)
+            return 1;
+        bitonic_smem_kernel<<<1, 1024, md * 8, stream>>>(keys, (int)md);
+    } else {
+        for (size_t k = 2; k <= md; k <<= 1)
+            for (size_t j = k >> 1; j > 0; j >>= 1)
+                bitonic_global_kernel<<<blocks(md, 256), 256, 0, stream>>>(keys, md, k, j);
+    }
+    index_kernel<T><<<blocks(n, 256), 256, 0, stream>>>(in, n, keys, d, idx);
+    const int bits = dict_bits((unsigned long)d);
+    const int per_word = (int)floor(32 / (double)bits);
+    const unsigned long nw = (unsigned long)ceil(n / (double)per_word);
+    if (*n_words < nw) return 4;
+    pack_kernel<<<blocks(nw, 256), 256, 0, stream>>>(idx, n, bits, per_word, nw, words);
+    values_kernel<T><<<blocks(d, 256), 256, 0, stream>>>(keys, d, flags, vals);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_words, words, nw * 4, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_dict, vals, d * sizeof(T), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return 1;
+    *n_dict = (unsigned long)d;
+    *n_words = nw;
+    return 0;
+}
+
+template int dict_compress_prealloc<char>(const char*, size_t, void*, size_t, cudaStream_t, uint32_t*,
+                                          unsigned long*, char*, unsigned long*);
+template int dict_compress_prealloc<int>(const int*, size_t, void*, size_t, cudaStream_t, uint32_t*, unsigned long*,
+                                         int*, unsigned long*);
+template int dict_compress_prealloc<unsigned int>(const unsigned int*, size_t, void*, size_t, cudaStream_t,
+                                                  uint32_t*, unsigned long*, unsigned int*, unsigned long*);
+template int dict_compress_prealloc<double>(const double*, size_t, void*, size_t, cudaStream_t, uint32_t*,
+                                            unsigned long*, double*, unsigned long*);
+
 template int dict_compress_device<char>(const char*, size_t, void*, size_t, cudaStream_t, uint32_t*, unsigned long*,
                                         char*, unsigned long*, std::string*);
 template int dict_compress_device<int>(const int*, size_t, void*, size_t, cudaStream_t, uint32_t*, unsigned long*,

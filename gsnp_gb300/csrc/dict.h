@@ -28,6 +28,16 @@ int dict_compress_device(const T* d_in, size_t n, void* d_scratch, size_t scratc
                          uint32_t* h_words, unsigned long* n_words, T* h_dict, unsigned long* n_dict,
                          std::string* err);
 
+/* The same codec with host input and outputs over caller-provided device
+ * scratch of at least dict_static_bytes(n, sizeof(T)) bytes; it allocates
+ * nothing on the device or the host.  Returns 0, 1 (CUDA error) or 4
+ * (capacity). */
+size_t dict_static_bytes(size_t n, size_t elem);
+
+template <class T>
+int dict_compress_prealloc(const T* h_in, size_t n, void* d_scratch, size_t scratch_bytes, cudaStream_t stream,
+                           uint32_t* h_words, unsigned long* n_words, T* h_dict, unsigned long* n_dict);
+
 }  // namespace gsnp
 
 #endif

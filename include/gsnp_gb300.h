@@ -191,6 +191,31 @@ int gsnp_transfer_bytes(gsnp_context* ctx, uint64_t* h2d, uint64_t* d2h);
  *   [6], [7] reserved, 0 */
 int gsnp_get_stats(gsnp_context* ctx, uint64_t* stats, int n);
 
+/* Element types of gsnp_dict_compress_static */
+#define GSNP_DICT_CHAR 0
+#define GSNP_DICT_INT 1
+#define GSNP_DICT_UINT32 2
+#define GSNP_DICT_DOUBLE 3
+
+/* No counterpart in the reference.  The -C dictionary codec (the contract of
+ * cuda_dictCompression, cpp/dict_compression.h:26-37: dict = the distinct
+ * values ascending, words = their indices packed MSB-first) for callers that
+ * cannot allocate device memory on their path - a process whose free device
+ * memory is held by another allocator, or a streaming writer that must not
+ * call cudaMalloc/cudaFree because they synchronise the device.  Its scratch
+ * is a static device array reserved when the library loads (12.6 MB), so it
+ * takes at most 262,144 values (32 x 8192, the reference's dictionary
+ * capacity); larger inputs return GSNP_ERR_CAPACITY without touching the
+ * device.  values: n host values of the given GSNP_DICT_* type; *n_words and
+ * *n_dict hold the capacities of words and dict on entry and the counts on
+ * return.  Runs on the current device and the given cudaStream_t (NULL: the
+ * legacy default stream) and returns when the outputs are in host memory.
+ * The first call on a device looks up the scratch array's address; make it
+ * before any stream capture.  Every call clears the scratch it needs on the
+ * stream; calls that overlap on one GPU race and must be serialised. */
+int gsnp_dict_compress_static(int type, const void* values, uint64_t n, uint32_t* words, uint64_t* n_words,
+                              void* dict, uint64_t* n_dict, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
