@@ -40,6 +40,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIG = "c1"
+WORKLOADS = {
+    "c0": "c0: 1 Mbp reference, 50 bp reads at 10x (200 k alignments), -L 50 -t -u",
+    "c1": "c1: 50 Mbp reference, 100 bp reads at 30x (15 M alignments), dbSNP 1%, -L 100 -t -u -2 -s",
+    "c2": "c2: 50 Mbp, copy-number segments and 300-1000x hotspots, 35/50/75/100 bp reads, -L 100 -t -u",
+    "c3": "c3: c1 with Phred 2-60 qualities, -L 100 -Q '|' -t -u -2 -s",
+    "c4": "c4: 250 Mbp, 3 Mbp N block, 100 bp reads at 40x (100 M alignments), -L 100 -t -u",
+}
 METRIC = "sites/s at 30x (bases/s = sites/s x mean depth)"
 UNIT = "sites/s"
 
@@ -53,7 +60,9 @@ def parse_args():
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp32",
                     help="headline form: fp32 = FP32 compensated sums with FP64 fixup, fp64 = plain FP64")
     ap.add_argument("--no-compare", action="store_true", help="do not also time the other form")
-    ap.add_argument("--scale", type=float, default=1.0, help="genome scale (1.0 = the named 50 Mbp workload)")
+    ap.add_argument("--scale", type=float, default=1.0, help="genome scale (1.0 = the named workload's full size)")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=CONFIG,
+                    help="synthetic workload shape (the headline is c1, the 30x configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
     return ap.parse_args()
@@ -143,17 +152,17 @@ class OracleSample:
     input files, timed through the CPU oracle (a port of the reference's
     single-threaded calling code, run on one core)."""
 
-    def __init__(self, sample_len: int):
+    def __init__(self, sample_len: int, workload: str = CONFIG):
         from gsnp_gb300 import synth
         self.oracle = os.path.join(ROOT, "oracle", "_build", "gsnp_oracle")
         if not os.path.exists(self.oracle):
             subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8"], check=True)
-        self.w = synth.make_workload(CONFIG, genome_len=sample_len)
+        self.w = synth.make_workload(workload, genome_len=sample_len)
         self.dir = tempfile.TemporaryDirectory()
         self.paths = synth.write_inputs(self.w, self.dir.name)
         self.flags = [f for f in self.w.cli_flags(self.paths.get("dbsnp")) if f != "-C"]
-        self.sample = "%d-site c1-shaped sample (%d reads), calling pass (window loop + cns text), 1 thread" % (
-            self.w.genome_len, self.w.num_reads)
+        self.sample = "%d-site %s-shaped sample (%d reads), calling pass (window loop + cns text), 1 thread" % (
+            self.w.genome_len, workload, self.w.num_reads)
 
     def start(self, out_dir: str) -> subprocess.Popen:
         env = dict(os.environ, GSNP_ORACLE_TIMING="1")
@@ -184,8 +193,8 @@ class OracleSample:
         return procs * self.w.genome_len / max(secs)
 
 
-def cpu_baseline(sample_len: int):
-    s = OracleSample(sample_len)
+def cpu_baseline(sample_len: int, workload: str = CONFIG):
+    s = OracleSample(sample_len, workload)
     return s.run(), s.sample
 
 
@@ -202,7 +211,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     sample_len = 600_000 if args.scale >= 1.0 else max(40_000, int(600_000 * args.scale))
-    smp = OracleSample(sample_len)
+    smp = OracleSample(sample_len, args.workload)
     cores = host_cores()
     vals = []
     for i in range(args.warmup + args.steps):
@@ -215,8 +224,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * cores * sample_len / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "c1: 50 Mbp, 100 bp reads at 30x, dbSNP 1%, -L 100 -t -u -2 -s",
-                   "sample_sites": sample_len, "processes": cores},
+        "config": {"workload": WORKLOADS[args.workload], "sample_sites": sample_len, "processes": cores},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -243,13 +251,20 @@ def main():
     precision = api.PRECISION_FP64 if args.precision == "fp64" else api.PRECISION_FP32_FIXUP
     other = api.PRECISION_FP32_FIXUP if precision == api.PRECISION_FP64 else api.PRECISION_FP64
     t0 = time.time()
-    w = synth.make_workload(CONFIG, scale=args.scale, backend="torch", device="cuda:%d" % local)
+    w = synth.make_workload(args.workload, scale=args.scale, backend="torch", device="cuda:%d" % local)
     t_gen = time.time() - t0
     flags = w.cli_flags("dbsnp")   # the dbSNP rows are passed in memory
     codes = api.site_codes(w.ref, w.db_pos)
     caller = api.Caller(local)
     caller.load_reference(codes, api.snp_table(w))
-    arrs = [np.ascontiguousarray(x) for x in (w.pos, w.length, w.hit, w.strand)] + [w.seq, w.qual]
+    def pinned(x):
+        """x in page-locked host memory (the e2e copies read the inputs from pinned memory)"""
+        x = np.ascontiguousarray(x)
+        t = torch.empty(x.shape, dtype=getattr(torch, x.dtype.name), pin_memory=True)
+        t.numpy()[...] = x
+        return t.numpy()
+
+    arrs = [pinned(x) for x in (w.pos, w.length, w.hit, w.strand, w.seq, w.qual)]
     reads = api.Caller.reads_struct(*arrs)
     p = api.params_from_flags(flags, precision)
     pm = caller.calibrate(p, reads)
@@ -338,7 +353,8 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cv, sample = cpu_baseline(1_200_000 if args.scale >= 1.0 else max(40_000, int(1_200_000 * args.scale)))
+            cv, sample = cpu_baseline(1_200_000 if args.scale >= 1.0 else max(40_000, int(1_200_000 * args.scale)),
+                                      args.workload)
             cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
         except Exception as exc:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": "failed: %s" % exc}
@@ -350,8 +366,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if precision == api.PRECISION_FP64 else "f32+f64",
             "data": "synthetic (seeded generator of the c1 shape, generated on the GPU in %.1f s)" % t_gen,
-            "config": {"workload": "c1: 50 Mbp reference, 100 bp reads at 30x (15 M alignments), dbSNP 1%%, "
-                                   "-L 100 -t -u -2 -s; scale %.3g" % args.scale,
+            "config": {"workload": WORKLOADS[args.workload] + "; scale %.3g" % args.scale,
                        "sites": sites, "reads": w.num_reads, "bases": w.num_bases, "mean_depth": depth,
                        "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs (3 GB of alignments) exceed the 129 MB L2; no flush"},

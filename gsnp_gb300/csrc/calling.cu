@@ -136,18 +136,50 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
     return pk;
 }
 
-/* ascending insertion sort of one site's record column */
+/* Ascending sort of one site's record column.  Up to 32 records: a bitonic
+ * network in registers (the column padded with 0xFFFFFFFF, which no record
+ * word equals), the same instruction stream in every lane of the warp.
+ * Deeper columns: Shell sort with gaps 10, 4, 1, whose gapped passes leave
+ * the final insertion pass short shifts. */
 __device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
-    for (int i = 1; i < num; ++i) {
-        const uint32_t w = recs[i * kTile];
-        int j = i;
-        while (j > 0) {
-            const uint32_t prev = recs[(j - 1) * kTile];
-            if (prev <= w) break;
-            recs[j * kTile] = prev;
-            --j;
+    if (num <= 32) {
+        uint32_t v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = i < num ? recs[i * kTile] : 0xFFFFFFFFu;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const uint32_t a = v[i], b = v[l];
+                        const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+                        if ((i & k) == 0) { v[i] = lo; v[l] = hi; }
+                        else { v[i] = hi; v[l] = lo; }
+                    }
+                }
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (i < num) recs[i * kTile] = v[i];
+        return;
+    }
+    const int gaps[3] = {10, 4, 1};
+#pragma unroll
+    for (int gi = 0; gi < 3; ++gi) {
+        const int h = gaps[gi];
+        for (int i = h; i < num; ++i) {
+            const uint32_t w = recs[i * kTile];
+            int j = i;
+            while (j >= h) {
+                const uint32_t prev = recs[(j - h) * kTile];
+                if (prev <= w) break;
+                recs[j * kTile] = prev;
+                j -= h;
+            }
+            recs[j * kTile] = w;
         }
-        recs[j * kTile] = w;
     }
 }
 
@@ -250,6 +282,72 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
 
 __constant__ int c_slots[kNumBins] = {32, 48, 64, 96, 128, 256};
 
+/* Read range of every tile, [lower_bound(s0 - L + 1), lower_bound(s0 + kTile)),
+ * in one pass over the sorted starts: read r is the lower bound of every
+ * boundary b with pos[r - 1] < b <= pos[r] (thread n takes the boundaries
+ * past the last read). */
+__global__ void tile_bounds_kernel(const int32_t* __restrict__ pos, int64_t n, int64_t n_tiles, int L,
+                                   int64_t* __restrict__ rng) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > n) return;
+    const int64_t lo = r == 0 ? -((int64_t)1 << 40) : (int64_t)pos[r - 1];
+    const int64_t hi = r == n ? ((int64_t)1 << 40) : (int64_t)pos[r];
+    if (lo >= hi) return;
+    auto fdiv = [](int64_t x) { return x >= 0 ? x / kTile : -((-x + kTile - 1) / kTile); };
+    /* first boundaries t*kTile - L + 1 in (lo, hi] */
+    int64_t t0 = fdiv(lo + L - 1) + 1, t1 = fdiv(hi + L - 1);
+    if (t0 < 0) t0 = 0;
+    if (t1 > n_tiles - 1) t1 = n_tiles - 1;
+    for (int64_t t = t0; t <= t1; ++t) rng[t * 2] = r;
+    /* second boundaries (t + 1)*kTile in (lo, hi] */
+    t0 = fdiv(lo);
+    t1 = fdiv(hi) - 1;
+    if (t0 < 0) t0 = 0;
+    if (t1 > n_tiles - 1) t1 = n_tiles - 1;
+    for (int64_t t = t0; t <= t1; ++t) rng[t * 2 + 1] = r;
+}
+
+cudaError_t launch_tile_bounds(const CallArgs& a, cudaStream_t stream) {
+    tile_bounds_kernel<<<(unsigned)((a.n_reads + 1 + 255) / 256), 256, 0, stream>>>(a.pos, a.n_reads, a.n_tiles, a.L,
+                                                                                      a.tile_rng);
+    return cudaGetLastError();
+}
+
+/* The FP64 call of a site with no record and no count for each of the 16
+ * site codes (site_posterior over zero likelihoods), kept where it is
+ * homozygous and does not depend on a dbSNP row. */
+__global__ void empty_calls_kernel(CallArgs a, SiteCall* calls, uint8_t* valid) {
+    const int code = threadIdx.x;
+    if (code >= 16) return;
+    SitePileup p;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { p.cu[i] = 0; p.qs[i] = 0; p.ca[i] = 0; }
+    p.depth = 0;
+    p.repeat = 0;
+    p.dep_uni = 0;
+    p.num = 0;
+    double tl[16], lp[16];
+    for (int i = 0; i < 16; ++i) {
+        tl[i] = 0.0;
+        lp[i] = a.log_prior[((code & 7) << 4) + i];
+    }
+    bool used_next = false;
+    auto nq = [&](int) {
+        used_next = true;
+        return 0;
+    };
+    SiteCall c;
+    site_posterior(a, (uint8_t)code, p, tl, nullptr, lp, nullptr, 1, nq, &c);
+    const bool hom = (c.type1 >> 2) == (c.type1 & 3);
+    valid[code] = hom && !used_next && !((code & 8) && a.refine);
+    calls[code] = c;
+}
+
+cudaError_t launch_empty_calls(const CallArgs& a, SiteCall* calls, uint8_t* valid, cudaStream_t stream) {
+    empty_calls_kernel<<<1, 32, 0, stream>>>(a, calls, valid);
+    return cudaGetLastError();
+}
+
 /* Per tile: the deepest site's record need (reads starting in [site - L + 1,
  * site], capped at 255) picks the depth bin; the window's mode picks the FP64
  * kernel (bins 0 .. kNumBins-1) or the fast one (the next kNumBins).  Each warp's read range is
@@ -257,7 +355,6 @@ __constant__ int c_slots[kNumBins] = {32, 48, 64, 96, 128, 256};
 __global__ void __launch_bounds__(kTile) classify_tiles_kernel(CallArgs a, int pass, int* bin_count,
                                                                int32_t* bin_tiles) {
     __shared__ int32_t spos[kMaxStagedReads];
-    __shared__ int64_t sh[2];
     __shared__ int smax[kWarpsPerTile];
     const int64_t tile = blockIdx.x;
     const int64_t s0 = tile * kTile;
@@ -265,12 +362,7 @@ __global__ void __launch_bounds__(kTile) classify_tiles_kernel(CallArgs a, int p
     const uint8_t wflags = a.win_flags[win];
     const bool external = (wflags & kWinExternalLik) != 0;
     if (external != (pass == 1)) return;
-    if (threadIdx.x == 0) {
-        sh[0] = lower_bound_g(a.pos, a.n_reads, s0 - a.L + 1);
-        sh[1] = lower_bound_g(a.pos, a.n_reads, s0 + kTile);
-    }
-    __syncthreads();
-    const int64_t r_lo = sh[0], r_hi = sh[1];
+    const int64_t r_lo = a.tile_rng[tile * 2], r_hi = a.tile_rng[tile * 2 + 1];
     const bool staged = (r_hi - r_lo) <= kMaxStagedReads;
     if (staged)
         for (int64_t i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) spos[i] = __ldg(a.pos + r_lo + i);
@@ -477,7 +569,14 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
         const uint8_t ori = deal.ori[me];
         SiteCall call;
         if ((site & 4095) == 0 && a.stats) dflags = kCallSampled;
-        if (fast_posterior(a, deal.snp_row[me], ori, p, k.s, p.num, &call)) {
+        const bool empty = p.num == 0 && (p.ca[0] | p.ca[1] | p.ca[2] | p.ca[3]) == 0 && a.empty_valid[ori];
+        if (empty) {
+            /* no record and no count: the call depends on the site code only */
+            call = a.empty_calls[ori];
+            call.depth = p.depth;
+            call.repeat_time = p.repeat;
+            call.flags |= dflags;
+        } else if (fast_posterior(a, deal.snp_row[me], ori, p, k.s, p.num, &call)) {
             call.flags |= dflags;
         } else {
             call = SiteCall{};
@@ -524,7 +623,7 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
  * bound checks, then the FP64 sums where those fail.  Sampled sites also get
  * the FP64 sums for the accuracy figure, and when the fast kernel had decided
  * them its call is compared with this one. */
-__global__ void __launch_bounds__(128) deferred_sites_kernel(CallArgs a, int64_t n) {
+__global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DeferredSite d = a.dsites[i];
@@ -562,10 +661,10 @@ __global__ void __launch_bounds__(128) deferred_sites_kernel(CallArgs a, int64_t
     load_log_prior(a, d.snp_row, ori, lp);
     auto nq = [&](int b) { return neighbour_qsum(a, site, b); };
     SiteCall call;
-    if (!site_posterior(a, ori, p, tl, eps, lp, recs, 1, nq, &call)) {
+    if (!site_posterior<true>(a, ori, p, tl, eps, lp, recs, 1, nq, &call)) {
         /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
         likelihood_fp64(a, recs, seen, 1, p.num, tl);
-        site_posterior(a, ori, p, tl, nullptr, lp, recs, 1, nq, &call);
+        site_posterior<true>(a, ori, p, tl, nullptr, lp, recs, 1, nq, &call);
         call.flags |= kCallFixup;
         atomicAdd(a.stats + 1, 1ull);
     }
@@ -627,7 +726,9 @@ cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tile
 
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    deferred_sites_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(a, n);
+    /* one warp per CTA: the deferred sites are few and each is a long serial
+     * computation, so they are spread over as many SMs as possible */
+    deferred_sites_kernel<<<(unsigned)((n + 31) / 32), 32, 0, stream>>>(a, n);
     return cudaGetLastError();
 }
 

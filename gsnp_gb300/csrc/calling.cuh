@@ -85,7 +85,12 @@ struct CallArgs {
     const int32_t* win_lik_src;  /* per window: window whose likelihood is used (-1: zeros) */
     /* tiles */
     int64_t n_tiles;
+    int64_t* tile_rng;           /* [n_tiles][2]: reads starting in [s0 - L + 1, s0 + kTile) of each tile */
     int64_t* warp_rng;           /* [n_tiles][4][2]: reads that can cover each warp's 32 sites */
+    /* the call of a site without records or counts, by site code (16 entries;
+     * empty_valid[code] = 0 where it is not a fixed homozygous call) */
+    const SiteCall* empty_calls;
+    const uint8_t* empty_valid;
     /* sites deferred by the fast kernel */
     DeferredSite* dsites;        /* [dsite_cap] */
     uint32_t* dpool;             /* [dpool_cap] sorted records of the deferred sites */

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -36,19 +37,31 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
+cudaError_t launch_tile_bounds(const CallArgs& a, cudaStream_t stream);
+cudaError_t launch_empty_calls(const CallArgs& a, SiteCall* calls, uint8_t* valid, cudaStream_t stream);
 int bin_slots(int bin);
 
 /* ---- device helpers ---- */
 
-__global__ void gather_reads_kernel(int64_t n, const int64_t* __restrict__ idx, const uint8_t* __restrict__ seq,
-                                    const uint8_t* __restrict__ qual, int pitch, int L, uint16_t* __restrict__ bq,
-                                    int* __restrict__ error) {
-    /* one warp per read; bases go through the 2-bit round trip of the
-     * reference's pass-1 store (upper case; anything else is rejected) */
+__global__ void gather_reads_kernel(int64_t n, const int64_t* __restrict__ idx, const int32_t* __restrict__ rpos,
+                                    const int32_t* __restrict__ rlen, const int32_t* __restrict__ rhit,
+                                    const uint8_t* __restrict__ rstrand, const uint8_t* __restrict__ seq,
+                                    const uint8_t* __restrict__ qual, int pitch, int L, int32_t* __restrict__ pos,
+                                    int32_t* __restrict__ lenhit, int32_t* __restrict__ len,
+                                    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq) {
+    /* one warp per deposited read: its start, length, hit count and strand,
+     * and its base|quality row */
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= n) return;
     const int64_t src = idx[warp];
+    if (lane == 0) {
+        const int32_t l = rlen[src];
+        pos[warp] = rpos[src];
+        len[warp] = l;
+        lenhit[warp] = (int32_t)(((uint32_t)(l & 0xffff) << 16) | ((uint32_t)rhit[src] & 0xffffu));
+        strand[warp] = rstrand[src];
+    }
     const uint8_t* s = seq + src * pitch;
     const uint8_t* q = qual + src * pitch;
     uint16_t* d = bq + warp * L;
@@ -152,6 +165,16 @@ struct gsnp_context {
     float* d_snp_lp32 = nullptr;
     int32_t* d_tile_snp = nullptr;
     bool snp_lp_ready = false;
+    /* raw alignments of the last call (device copies, reused across calls) */
+    int32_t* d_raw_pos = nullptr;
+    int32_t* d_raw_len = nullptr;
+    int32_t* d_raw_hit = nullptr;
+    uint8_t* d_raw_strand = nullptr;
+    uint8_t* d_raw_seq = nullptr;
+    uint8_t* d_raw_qual = nullptr;
+    int64_t* d_idx = nullptr;
+    int64_t raw_cap = 0;
+    size_t raw_bytes = 0;
     /* resident reads (deposited, packed) */
     int64_t n_dep = 0;
     int64_t cap_dep = 0;
@@ -182,6 +205,9 @@ struct gsnp_context {
     unsigned long long* d_dcount = nullptr;  /* [2] requested sites, record words */
     int64_t dsite_cap = 0, dpool_cap = 0;
     int64_t* d_warp_rng = nullptr;  /* [n_tiles][4][2] */
+    int64_t* d_tile_rng = nullptr;  /* [n_tiles][2] */
+    SiteCall* d_empty_calls = nullptr;  /* [16] */
+    uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
     int h_bin_count[2 * kNumBins] = {};
     unsigned long long h_dcount[2] = {0, 0};
@@ -207,6 +233,25 @@ struct gsnp_context {
 };
 
 namespace {
+
+/* Host wall time of the phases of one call, printed to stderr when the
+ * environment variable GSNP_TIMING is set. */
+struct PhaseTimer {
+    const char* what;
+    bool on;
+    std::chrono::steady_clock::time_point t0, t;
+    explicit PhaseTimer(const char* w) : what(w), on(getenv("GSNP_TIMING") != nullptr) {
+        t0 = t = std::chrono::steady_clock::now();
+    }
+    void mark(const char* phase) {
+        if (!on) return;
+        const auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "%s: %-26s %8.2f ms (total %8.2f ms)\n", what, phase,
+                std::chrono::duration<double, std::milli>(now - t).count(),
+                std::chrono::duration<double, std::milli>(now - t0).count());
+        t = now;
+    }
+};
 
 int fail(gsnp_context* c, int code, const std::string& msg) {
     if (c) c->error = msg;
@@ -237,7 +282,9 @@ void free_all(gsnp_context* c) {
                     c->d_len, c->d_strand, c->d_bq, c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts,
                     c->d_lik_keep, c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles, c->d_dsites,
                     c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_dict, c->d_win_host_src, c->d_emit,
-                    c->d_text, c->d_chr, c->d_tile_snp};
+                    c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
+                    c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
+                    c->d_idx};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -283,6 +330,9 @@ CallArgs make_args(gsnp_context* c) {
     a.win_lik_src = c->d_win_lik_src;
     a.n_tiles = (c->chr_len + kTile - 1) / kTile;
     a.warp_rng = c->d_warp_rng;
+    a.tile_rng = c->d_tile_rng;
+    a.empty_calls = c->d_empty_calls;
+    a.empty_valid = c->d_empty_valid;
     a.dsites = c->d_dsites;
     a.dpool = c->d_dpool;
     a.dcount = c->d_dcount;
@@ -301,13 +351,19 @@ int run_calling(gsnp_context* c) {
     if (!c->snp_lp_ready) {
         CK(dev_alloc(&c->d_snp_lp, (size_t)std::max<int64_t>(c->n_snp, 1) * 16), "cudaMalloc dbSNP priors");
         CK(dev_alloc(&c->d_snp_lp32, (size_t)std::max<int64_t>(c->n_snp, 1) * 12), "cudaMalloc dbSNP priors");
+        if (!c->d_empty_calls) {
+            CK(dev_alloc(&c->d_empty_calls, 16), "cudaMalloc");
+            CK(dev_alloc(&c->d_empty_valid, 16), "cudaMalloc");
+        }
         const CallArgs a0 = make_args(c);
         CK(launch_snp_log_prior(a0, c->d_snp_lp, c->d_snp_lp32, c->stream), "dbSNP prior kernel");
+        CK(launch_empty_calls(a0, c->d_empty_calls, c->d_empty_valid, c->stream), "empty-site calls");
         c->snp_lp_ready = true;
     }
     if (n_tiles > c->tiles_cap) {
         CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * 2 * kNumBins), "cudaMalloc bins");
         CK(dev_alloc(&c->d_warp_rng, (size_t)n_tiles * kWarpsPerTile * 2), "cudaMalloc ranges");
+        CK(dev_alloc(&c->d_tile_rng, (size_t)n_tiles * 2), "cudaMalloc ranges");
         c->tiles_cap = n_tiles;
     }
     if (c->dsite_cap == 0) {
@@ -341,6 +397,7 @@ int run_calling(gsnp_context* c) {
     };
     for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
         int k = begin(kKindClassify, 0, n_tiles);
+        if (pass == 0) CK(launch_tile_bounds(a, c->stream), "tile bounds kernel");
         CK(launch_classify(a, pass, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
         end(k);
         CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(c->h_bin_count), cudaMemcpyDeviceToHost,
@@ -521,14 +578,47 @@ int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
         return fail(c, GSNP_ERR_ARG, "null read arrays");
     if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
     cudaSetDevice(c->device);
+    PhaseTimer timer("gsnp_call_chromosome");
     const int L = c->params.read_length;
-    for (int64_t i = 0; i < r->n; ++i)
-        if (r->len[i] < 0 || r->len[i] > L || r->len[i] > r->pitch)
+    const int64_t n = r->n;
+    /* 1. the raw alignments go to the device first; the copies run while the
+     *    host replays the window loop */
+    const size_t raw = (size_t)n * r->pitch;
+    if (n > c->raw_cap || raw > c->raw_bytes) {
+        const int64_t cap = std::max<int64_t>(n, 1);
+        CK(dev_alloc(&c->d_raw_pos, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_len, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_hit, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_strand, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_seq, std::max<size_t>(raw, 1)), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_qual, std::max<size_t>(raw, 1)), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_idx, (size_t)cap), "cudaMalloc raw");
+        c->raw_cap = cap;
+        c->raw_bytes = std::max<size_t>(raw, 1);
+    }
+    if (n > 0) {
+        CK(cudaMemcpyAsync(c->d_raw_pos, r->pos, n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_len, r->len, n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_hit, r->hit, n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_strand, r->strand, n, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload seq");
+        CK(cudaMemcpyAsync(c->d_raw_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload qual");
+    }
+    timer.mark("uploads issued");
+    /* 2. host: lengths, then the window replay */
+    for (int64_t i = 0; i < n; ++i)
+        if (r->len[i] < 0 || r->len[i] > L || r->len[i] > r->pitch) {
+            cudaStreamSynchronize(c->stream);
             return fail(c, GSNP_ERR_INPUT, "alignment " + std::to_string(i) + " is longer than -L");
+        }
     ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
     std::string err;
     const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, &c->plan, &err);
-    if (rc != 0) return fail(c, rc, err);
+    if (rc != 0) {
+        cudaStreamSynchronize(c->stream);
+        return fail(c, rc, err);
+    }
+    timer.mark("window replay");
     const WindowPlan& P = c->plan;
     const int64_t nd = (int64_t)P.deposited.size();
 
@@ -558,59 +648,38 @@ int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
         c->have_lik_keep = true;
     }
 
-    /* upload the alignments and gather the deposited ones */
+    /* 3. gather the deposited alignments on the device */
     if (nd > c->cap_dep) {
         CK(dev_alloc(&c->d_pos, (size_t)nd), "cudaMalloc reads");
         CK(dev_alloc(&c->d_lenhit, (size_t)nd), "cudaMalloc reads");
         CK(dev_alloc(&c->d_len, (size_t)nd), "cudaMalloc reads");
         CK(dev_alloc(&c->d_strand, (size_t)nd), "cudaMalloc reads");
-        CK(dev_alloc(&c->d_bq, (size_t)nd * L), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_bq, (size_t)nd * L + 8), "cudaMalloc reads");
         c->cap_dep = nd;
     }
     c->n_dep = nd;
-    c->h2d_bytes = (uint64_t)P.n_windows * 5 + (uint64_t)nd * (4 + 4 + 4 + 1 + 8) + 2ULL * (uint64_t)r->n * r->pitch;
+    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) + 2ULL * (uint64_t)n * r->pitch +
+                   (uint64_t)nd * 8;
     c->d2h_bytes = 0;
-    {
-        std::vector<int32_t> pos(nd), lenhit(nd), len(nd);
-        std::vector<uint8_t> strand(nd);
-        for (int64_t k = 0; k < nd; ++k) {
-            const int64_t i = P.deposited[k];
-            pos[k] = r->pos[i];
-            len[k] = r->len[i];
-            lenhit[k] = (int32_t)(((r->len[i] & 0xffff) << 16) | r->hit[i]);
-            strand[k] = r->strand[i];
-        }
-        CK(cudaMemcpyAsync(c->d_pos, pos.data(), nd * 4, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_lenhit, lenhit.data(), nd * 4, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_len, len.data(), nd * 4, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_strand, strand.data(), nd, cudaMemcpyHostToDevice, c->stream), "upload");
-        /* raw base/quality rows of every alignment, then gather on the device */
-        const size_t raw = (size_t)r->n * r->pitch;
-        uint8_t *d_seq = nullptr, *d_qual = nullptr;
-        int64_t* d_idx = nullptr;
-        CK(cudaMalloc((void**)&d_seq, std::max<size_t>(raw, 1)), "cudaMalloc raw");
-        CK(cudaMalloc((void**)&d_qual, std::max<size_t>(raw, 1)), "cudaMalloc raw");
-        CK(cudaMalloc((void**)&d_idx, std::max<int64_t>(nd, 1) * 8), "cudaMalloc raw");
-        CK(cudaMemcpyAsync(d_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload seq");
-        CK(cudaMemcpyAsync(d_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload qual");
-        CK(cudaMemcpyAsync(d_idx, P.deposited.data(), nd * 8, cudaMemcpyHostToDevice, c->stream), "upload idx");
-        CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
-        if (nd > 0) {
-            const int64_t threads = nd * 32;
-            gather_reads_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-                nd, d_idx, d_seq, d_qual, r->pitch, L, c->d_bq, c->d_error);
-            normalise_bases_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(nd, c->d_len, c->d_bq, L,
-                                                                                               c->d_error);
-        }
-        int err2 = 0;
-        CK(cudaMemcpyAsync(&err2, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
-        CK(cudaStreamSynchronize(c->stream), "gather");
-        cudaFree(d_seq);
-        cudaFree(d_qual);
-        cudaFree(d_idx);
-        if (err2) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
+    CK(cudaMemcpyAsync(c->d_idx, P.deposited.data(), nd * 8, cudaMemcpyHostToDevice, c->stream), "upload idx");
+    CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
+    if (nd > 0) {
+        const int64_t threads = nd * 32;
+        gather_reads_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+            nd, c->d_idx, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
+            r->pitch, L, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq);
+        normalise_bases_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(nd, c->d_len, c->d_bq, L,
+                                                                                           c->d_error);
+        CK(cudaGetLastError(), "gather kernels");
     }
-    return run_calling(c);
+    int err2 = 0;
+    CK(cudaMemcpyAsync(&err2, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
+    CK(cudaStreamSynchronize(c->stream), "gather");
+    timer.mark("uploads and gather done");
+    if (err2) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
+    const int rc2 = run_calling(c);
+    timer.mark("calling");
+    return rc2;
 }
 
 int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, double* pm) {

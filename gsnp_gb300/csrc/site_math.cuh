@@ -403,7 +403,7 @@ __device__ __forceinline__ void load_log_prior(const CallArgs& a, int64_t snp_ro
  * truncated, clamped consensus quality) is provably the one the FP64 values
  * give.  nq(b) is q_sum[b] of the next site, which the reference reads when
  * base1/base2 name an N reference base. */
-template <class NQ>
+template <bool FAST_LOG = false, class NQ>
 __device__ bool site_posterior(const CallArgs& a, uint8_t ori, const SitePileup& p, const double* tl,
                                const double* eps, const double* lp, const uint32_t* recs, int stride, NQ&& nq,
                                SiteCall* out) {
@@ -460,13 +460,26 @@ __device__ bool site_posterior(const CallArgs& a, uint8_t ori, const SitePileup&
         q = finalize_q(0, hom, het_ok, tb, type1);
     } else {
         const double d = GSNP_DMUL(10.0, GSNP_DSUB(tp[type1], tp[type2]));
-        const double raw = GSNP_DADD(d, GSNP_DMUL(10.0, gsnp_cr_log10(rs)));
+        /* FAST_LOG: log10 of the rank-sum value from the CUDA math library,
+         * whose error is far below 2^-40 relative; dl bounds the resulting
+         * error of raw.  The correctly rounded log10 is evaluated only when
+         * raw +- dl could change the truncated, clamped quality. */
+        const bool approx = FAST_LOG && rs != 1.0;
+        double lg = approx ? log10(rs) : gsnp_cr_log10(rs);
+        double raw = GSNP_DADD(d, GSNP_DMUL(10.0, lg));
+        const double dl = approx ? 10.0 * fabs(lg) * 0x1p-40 + 0x1p-48 * (fabs(raw) + 1.0) : 0.0;
         q = finalize_q((int)raw, hom, het_ok, tb, type1);
         if (eps && ep[type1] + ep[type2] > 0.0) {
-            const double delta = 10.0 * (ep[type1] + ep[type2]) * (1.0 + 0x1p-20) + 0x1p-48 * (fabs(raw) + 1.0);
+            const double delta =
+                10.0 * (ep[type1] + ep[type2]) * (1.0 + 0x1p-20) + 0x1p-48 * (fabs(raw) + 1.0) + dl;
             if (finalize_q((int)(raw - delta), hom, het_ok, tb, type1) !=
                 finalize_q((int)(raw + delta), hom, het_ok, tb, type1))
                 return false;
+        } else if (approx && finalize_q((int)(raw - dl), hom, het_ok, tb, type1) !=
+                                 finalize_q((int)(raw + dl), hom, het_ok, tb, type1)) {
+            lg = gsnp_cr_log10(rs);
+            raw = GSNP_DADD(d, GSNP_DMUL(10.0, lg));
+            q = finalize_q((int)raw, hom, het_ok, tb, type1);
         }
     }
     fill_call(out, p, tb, type1, q, normal_path, rs);
