@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "calling.cuh"
@@ -43,61 +44,146 @@ int bin_slots(int bin);
 
 /* ---- device helpers ---- */
 
-__global__ void gather_reads_kernel(int64_t n, const int64_t* __restrict__ idx, const int32_t* __restrict__ rpos,
+/* The deposited alignments are those that pass the position filters
+ * (0 <= pos, pos + len < chr_len), in file order, the first n_dep of them.
+ * Their index list is built in chunks of kDepChunk alignments: a count per
+ * chunk, an exclusive scan of the counts, and a pass that writes each passing
+ * alignment's index at its rank. */
+constexpr int kDepThreads = 256;
+constexpr int kDepChunk = kDepThreads * 16;
+
+__device__ __forceinline__ bool dep_passes(const int32_t* __restrict__ pos, const int32_t* __restrict__ len,
+                                           int64_t i, int64_t chr_len) {
+    const int64_t p = pos[i];
+    return p >= 0 && p + len[i] < chr_len;
+}
+
+__global__ void __launch_bounds__(kDepThreads) dep_count_kernel(int64_t n, const int32_t* __restrict__ pos,
+                                                                const int32_t* __restrict__ len, int64_t chr_len,
+                                                                int64_t* __restrict__ counts) {
+    __shared__ int warp_sum[kDepThreads / 32];
+    const int64_t base = (int64_t)blockIdx.x * kDepChunk;
+    int c = 0;
+    for (int j = 0; j < kDepChunk / kDepThreads; ++j) {
+        const int64_t i = base + j * kDepThreads + threadIdx.x;
+        if (i < n && dep_passes(pos, len, i, chr_len)) ++c;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < kDepThreads / 32; ++w) t += warp_sum[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+/* in-place exclusive scan of the chunk counts, one CTA */
+__global__ void __launch_bounds__(1024) dep_scan_kernel(int64_t* __restrict__ counts, int64_t n_chunks) {
+    __shared__ int64_t warp_sum[32];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t b = 0; b < n_chunks; b += 1024) {
+        const int64_t i = b + threadIdx.x;
+        const int64_t v = i < n_chunks ? counts[i] : 0;
+        int64_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int64_t s = warp_sum[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            warp_sum[lane] = s;   /* inclusive over warps */
+        }
+        __syncthreads();
+        const int64_t excl = carry + (warp > 0 ? warp_sum[warp - 1] : 0) + x - v;
+        if (i < n_chunks) counts[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sum[31];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kDepThreads) dep_index_kernel(int64_t n, const int32_t* __restrict__ pos,
+                                                                const int32_t* __restrict__ len, int64_t chr_len,
+                                                                const int64_t* __restrict__ offsets, int64_t n_dep,
+                                                                int64_t* __restrict__ idx) {
+    __shared__ int warp_cnt[kDepThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kDepChunk;
+    int64_t run = offsets[blockIdx.x];
+    for (int j = 0; j < kDepChunk / kDepThreads; ++j) {
+        const int64_t i = base + j * kDepThreads + threadIdx.x;
+        const bool v = i < n && dep_passes(pos, len, i, chr_len);
+        const unsigned ballot = __ballot_sync(0xffffffffu, v);
+        if (lane == 0) warp_cnt[warp] = __popc(ballot);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < kDepThreads / 32; ++w) {
+            before += w < warp ? warp_cnt[w] : 0;
+            total += warp_cnt[w];
+        }
+        const int64_t r = run + before + __popc(ballot & ((1u << lane) - 1u));
+        if (v && r < n_dep) idx[r] = i;
+        run += total;
+        __syncthreads();
+    }
+}
+
+__global__ void gather_reads_kernel(int64_t n, const int64_t* __restrict__ idx, int64_t n_raw,
+                                    const int32_t* __restrict__ rpos,
                                     const int32_t* __restrict__ rlen, const int32_t* __restrict__ rhit,
                                     const uint8_t* __restrict__ rstrand, const uint8_t* __restrict__ seq,
                                     const uint8_t* __restrict__ qual, int pitch, int L, int32_t* __restrict__ pos,
                                     int32_t* __restrict__ lenhit, int32_t* __restrict__ len,
-                                    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq) {
+                                    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq, int* __restrict__ error) {
     /* one warp per deposited read: its start, length, hit count and strand,
-     * and its base|quality row */
+     * and its base|quality row with the bases in upper case ('A' past the
+     * read's end; any base other than ACGT/acgt sets *error) */
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= n) return;
     const int64_t src = idx[warp];
+    if (src < 0 || src >= n_raw) {   /* the host and device filters disagree */
+        if (lane == 0) atomicExch(error, 3);
+        return;
+    }
+    const int32_t rl = rlen[src];
     if (lane == 0) {
-        const int32_t l = rlen[src];
         pos[warp] = rpos[src];
-        len[warp] = l;
-        lenhit[warp] = (int32_t)(((uint32_t)(l & 0xffff) << 16) | ((uint32_t)rhit[src] & 0xffffu));
+        len[warp] = rl;
+        lenhit[warp] = (int32_t)(((uint32_t)(rl & 0xffff) << 16) | ((uint32_t)rhit[src] & 0xffffu));
         strand[warp] = rstrand[src];
     }
     const uint8_t* s = seq + src * pitch;
     const uint8_t* q = qual + src * pitch;
     uint16_t* d = bq + warp * L;
+    bool bad = false;
     for (int c = lane; c < L; c += 32) {
         uint8_t b = 'A', qq = 0;
         if (c < pitch) {
-            b = s[c];
             qq = q[c];
+            if (c < rl) {
+                switch (s[c]) {
+                    case 'A': case 'a': b = 'A'; break;
+                    case 'C': case 'c': b = 'C'; break;
+                    case 'G': case 'g': b = 'G'; break;
+                    case 'T': case 't': b = 'T'; break;
+                    default: bad = true;
+                }
+            }
         }
         d[c] = (uint16_t)b | ((uint16_t)qq << 8);
     }
-}
-
-__global__ void normalise_bases_kernel(int64_t n, const int32_t* __restrict__ len, uint16_t* __restrict__ bq, int L,
-                                       int* __restrict__ error) {
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= n) return;
-    const int rl = len[warp];
-    uint16_t* d = bq + warp * L;
-    for (int c = lane; c < L; c += 32) {
-        const uint16_t v = d[c];
-        uint8_t b = (uint8_t)(v & 0xff);
-        if (c >= rl) {
-            b = 'A';
-        } else {
-            switch (b) {
-                case 'A': case 'a': b = 'A'; break;
-                case 'C': case 'c': b = 'C'; break;
-                case 'G': case 'g': b = 'G'; break;
-                case 'T': case 't': b = 'T'; break;
-                default: atomicExch(error, 2); b = 'A';
-            }
-        }
-        d[c] = (uint16_t)b | (v & 0xff00);
-    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(error, 2);
 }
 
 /* pass-1 calibration histogram (cpp/matrix.cc:58-118): unique reads, non-N
@@ -173,6 +259,8 @@ struct gsnp_context {
     uint8_t* d_raw_seq = nullptr;
     uint8_t* d_raw_qual = nullptr;
     int64_t* d_idx = nullptr;
+    int64_t* d_dep_off = nullptr;     /* per-chunk offsets of the deposited index list */
+    int64_t dep_chunk_cap = 0;
     int64_t raw_cap = 0;
     size_t raw_bytes = 0;
     /* resident reads (deposited, packed) */
@@ -276,6 +364,18 @@ cudaError_t dev_alloc(T** p, size_t count) {
     return cudaMalloc((void**)p, count * sizeof(T));
 }
 
+/* host threads for the per-alignment pass of the window replay:
+ * GSNP_HOST_THREADS, else every hardware thread (at most 64) */
+int host_threads() {
+    static const int n = [] {
+        const char* e = getenv("GSNP_HOST_THREADS");
+        int v = e ? atoi(e) : 0;
+        if (v <= 0) v = (int)std::thread::hardware_concurrency();
+        return std::max(1, std::min(v, 64));
+    }();
+    return n;
+}
+
 void free_all(gsnp_context* c) {
     void* ptrs[] = {c->d_lik64, c->d_lik32, c->d_qadj, c->d_p_prior, c->d_log_prior, c->d_log_prior32,
                     c->d_p_rank, c->d_codes, c->d_snp, c->d_snp_lp, c->d_snp_lp32, c->d_pos, c->d_lenhit,
@@ -284,7 +384,7 @@ void free_all(gsnp_context* c) {
                     c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_dict, c->d_win_host_src, c->d_emit,
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-                    c->d_idx};
+                    c->d_idx, c->d_dep_off};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -605,22 +705,17 @@ int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
         CK(cudaMemcpyAsync(c->d_raw_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload qual");
     }
     timer.mark("uploads issued");
-    /* 2. host: lengths, then the window replay */
-    for (int64_t i = 0; i < n; ++i)
-        if (r->len[i] < 0 || r->len[i] > L || r->len[i] > r->pitch) {
-            cudaStreamSynchronize(c->stream);
-            return fail(c, GSNP_ERR_INPUT, "alignment " + std::to_string(i) + " is longer than -L");
-        }
+    /* 2. host: the length check and the window replay */
     ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
     std::string err;
-    const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, &c->plan, &err);
+    const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, host_threads(), &c->plan, &err);
     if (rc != 0) {
         cudaStreamSynchronize(c->stream);
         return fail(c, rc, err);
     }
     timer.mark("window replay");
     const WindowPlan& P = c->plan;
-    const int64_t nd = (int64_t)P.deposited.size();
+    const int64_t nd = P.n_deposited;
 
     /* window tables */
     if (P.n_windows > c->n_win_alloc) {
@@ -658,24 +753,32 @@ int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
         c->cap_dep = nd;
     }
     c->n_dep = nd;
-    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) + 2ULL * (uint64_t)n * r->pitch +
-                   (uint64_t)nd * 8;
+    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) + 2ULL * (uint64_t)n * r->pitch;
     c->d2h_bytes = 0;
-    CK(cudaMemcpyAsync(c->d_idx, P.deposited.data(), nd * 8, cudaMemcpyHostToDevice, c->stream), "upload idx");
     CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
     if (nd > 0) {
+        /* index list of the deposited alignments, then the gather */
+        const int64_t n_chunks = (n + kDepChunk - 1) / kDepChunk;
+        if (n_chunks > c->dep_chunk_cap) {
+            CK(dev_alloc(&c->d_dep_off, (size_t)n_chunks), "cudaMalloc index");
+            c->dep_chunk_cap = n_chunks;
+        }
+        dep_count_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(n, c->d_raw_pos, c->d_raw_len,
+                                                                            c->chr_len, c->d_dep_off);
+        dep_scan_kernel<<<1, 1024, 0, c->stream>>>(c->d_dep_off, n_chunks);
+        dep_index_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(n, c->d_raw_pos, c->d_raw_len, c->chr_len,
+                                                                            c->d_dep_off, nd, c->d_idx);
         const int64_t threads = nd * 32;
         gather_reads_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-            nd, c->d_idx, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-            r->pitch, L, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq);
-        normalise_bases_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(nd, c->d_len, c->d_bq, L,
-                                                                                           c->d_error);
+            nd, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
+            r->pitch, L, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq, c->d_error);
         CK(cudaGetLastError(), "gather kernels");
     }
     int err2 = 0;
     CK(cudaMemcpyAsync(&err2, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
     CK(cudaStreamSynchronize(c->stream), "gather");
     timer.mark("uploads and gather done");
+    if (err2 == 3) return fail(c, GSNP_ERR_STATE, "deposited alignment list does not match the window replay");
     if (err2) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
     const int rc2 = run_calling(c);
     timer.mark("calling");

@@ -25,13 +25,22 @@
 
 namespace gsnp {
 
+/* a run of consecutive passing alignments that start in one window */
+struct WindowRun {
+    int64_t window;
+    int64_t first;    /* index of its first alignment */
+    int64_t count;    /* passing alignments in the run */
+};
+
 struct WindowPlan {
     int64_t n_windows = 0;
     std::vector<int64_t> call_len;   /* sites called in window w */
     std::vector<int32_t> host_src;   /* window whose pileup the host count arrays hold, -1: zeros */
     std::vector<int32_t> lik_src;    /* window whose likelihood is used, -1: never computed (zeros) */
     std::vector<uint8_t> flags;      /* kWin* flags for the kernels */
-    std::vector<int64_t> deposited;  /* indices of the deposited alignments, in order */
+    std::vector<WindowRun> runs;     /* the runs of passing alignments, in order */
+    int64_t n_valid = 0;             /* alignments that pass the position filters */
+    int64_t n_deposited = 0;         /* the first n_deposited of those are deposited */
     int64_t skipped = 0;             /* alignments skipped by the position filters */
     bool dropped_last = false;       /* the last alignment was not deposited */
 };
@@ -46,8 +55,15 @@ struct ReadView {
     int32_t pitch;
 };
 
-/* Returns 0, or 5 (GSNP_ERR_UNSORTED) with *err set to the reference's message. */
-int replay_windows(const ReadView& r, int64_t chr_len, int L, int qmin, WindowPlan* plan, std::string* err);
+/* An alignment passes the position filters when 0 <= pos and pos + len <
+ * chr_len; those are deposited in file order, all but the last when
+ * dropped_last.  Runs the per-alignment pass on up to `threads` threads.
+ * Returns 0; 6 (GSNP_ERR_INPUT) when an alignment is longer than L or its
+ * pitch, or when no alignment has a non-negative start; 5
+ * (GSNP_ERR_UNSORTED) with the reference's message when the passing
+ * alignments are not sorted by start. */
+int replay_windows(const ReadView& r, int64_t chr_len, int L, int qmin, int threads, WindowPlan* plan,
+                   std::string* err);
 
 }  // namespace gsnp
 
