@@ -12,9 +12,10 @@ beside it in the same run (the "compare" object).
   value : sites/s with the alignments resident in HBM (tile classification and
           the binned calling kernels, CUDA events on the launching stream);
           the alignments (3 GB) exceed L2, so no flush is needed between steps.
-  e2e   : sites/s through the C ABI from pinned host buffers: upload of the
-          alignments, window replay, gather, calling, and the download of
-          every site's 32-byte call, all inside the timed step.
+  e2e   : sites/s through the C ABI (gsnp_call_chromosome_into) from pinned
+          host buffers: upload of the alignments, window replay, gather,
+          calling, and the download of every site's 32-byte call, all inside
+          the timed step (the library overlaps them segment by segment).
 The calling kernels' roofline is the HBM bandwidth; the algorithmic bytes of a
 site are 2*D + 9*D/Lbar + 0.5 + 32 (bases and qualities of the covering reads,
 per-read start/length/strand, the 4-bit reference code, a 32-byte call).
@@ -54,7 +55,7 @@ UNIT = "sites/s"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gsnp", "reference"], default="gsnp")
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp32",
@@ -86,6 +87,7 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines = []
+        self.first = 0
 
     def __enter__(self):
         if self.device < 0:
@@ -98,6 +100,13 @@ class ClockSampler:
             self.thread.start()
         except OSError:
             self.proc = None
+            return self
+        # nvidia-smi takes a while to start: wait for its first sample, so that
+        # the timed region that follows is sampled from its beginning
+        t0 = time.time()
+        while not self.lines and self.proc.poll() is None and time.time() - t0 < 20:
+            time.sleep(0.02)
+        self.first = len(self.lines)
         return self
 
     def _read(self):
@@ -113,9 +122,10 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        """samples taken after the first one (which precedes the timed region)"""
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[self.first:] or self.lines[-1:]:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -265,6 +275,8 @@ def main():
         return t.numpy()
 
     arrs = [pinned(x) for x in (w.pos, w.length, w.hit, w.strand, w.seq, w.qual)]
+    # pinned destination of the e2e steps' site calls, allocated with the inputs
+    out_pinned = torch.empty(w.genome_len * 32, dtype=torch.uint8, pin_memory=True)
     reads = api.Caller.reads_struct(*arrs)
     p = api.params_from_flags(flags, precision)
     pm = caller.calibrate(p, reads)
@@ -286,7 +298,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    def time_form(prec, sample_clocks):
+    def time_form(prec):
         """Warm up, then time exactly args.steps device-resident calling passes."""
         caller.load_tables(api.params_from_flags(flags, prec), pm, prior, rank_tab)
         for _ in range(args.warmup):
@@ -296,41 +308,42 @@ def main():
         torch.cuda.synchronize()
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         kernel_ms = {}
-        with ClockSampler(local if sample_clocks else -1) as clocks:
-            start.record(stream)
-            for _ in range(args.steps):
-                caller.recall_resident()
-                for li in caller.last_launches():
-                    key = (li["kind"], li["slots"])
-                    kernel_ms.setdefault(key, []).append((li["ms"], li["sites"], li["tiles"]))
-            end.record(stream)
-            torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            caller.recall_resident()
+            for li in caller.last_launches():
+                key = (li["kind"], li["slots"])
+                kernel_ms.setdefault(key, []).append((li["ms"], li["sites"], li["tiles"]))
+        end.record(stream)
+        torch.cuda.synchronize()
         barrier()
         ms_step = max_over_ranks(start.elapsed_time(end)) / args.steps
         return {"ms_step": ms_step, "value": world * sites / (ms_step / 1000.0), "launches": n_launch,
-                "kernel_ms": kernel_ms, "clocks": clocks.summary() if sample_clocks else None,
-                "stats": caller.stats()}
+                "kernel_ms": kernel_ms, "stats": caller.stats()}
 
-    compare = time_form(other, False) if not args.no_compare else None
-    head = time_form(precision, True)
+    compare = time_form(other) if not args.no_compare else None
+    # clocks are sampled through the headline's timed steps and the e2e steps
+    sampler = ClockSampler(local)
+    sampler.__enter__()
+    head = time_form(precision)
     value, ms_step, kernel_ms = head["value"], head["ms_step"], head["kernel_ms"]
     stats = head["stats"]
 
     # ---- end to end through the C ABI from pinned host buffers ----
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 3)
-    out_pinned = torch.empty(sites * 32, dtype=torch.uint8, pin_memory=True)
     e2e_times = []
-    for _ in range(e2e_steps):
+    for i in range(1 + e2e_steps):           # the first pass warms the pinned result buffer, untimed
         barrier()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        caller.call(reads)
-        caller.lib.gsnp_fetch_sites(caller.ctx, 0, sites, out_pinned.data_ptr())
+        caller.call_into(reads, out_pinned.data_ptr())
         torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t1)
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t1)
     h2d, d2h = caller.transfer_bytes()
     e2e_s = max_over_ranks(max(statistics.mean(e2e_times), 1e-9))
     e2e_value = world * sites / e2e_s
+    sampler.__exit__(None, None, None)
 
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
@@ -372,7 +385,7 @@ def main():
                        "l2": "inputs (3 GB of alignments) exceed the 129 MB L2; no flush"},
             "bases_per_s": value * depth,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "steps": e2e_steps},
+                    "steps": e2e_steps, "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
             "gpu_launches": head["launches"] * args.steps,
             "kernels_ms": kernel_table(kernel_ms),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -380,7 +393,7 @@ def main():
                          "kernel": "%s<%d>" % (names[dom_key[0]], dom_key[1]), "sites_per_launch": dom_sites,
                          "bytes_per_site": bsite, "peak_source": peak_kind},
             "cpu_baseline": cpu,
-            "clocks": head["clocks"],
+            "clocks": sampler.summary(),
             "stats": stats,
         }
         if compare is not None:

@@ -80,6 +80,7 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_prior_table": (ctypes.c_int, [ctypes.POINTER(Params), _P]),
         "gsnp_rank_table": (ctypes.c_int, [_P]),
         "gsnp_call_chromosome": (ctypes.c_int, [_P, ctypes.POINTER(Reads)]),
+        "gsnp_call_chromosome_into": (ctypes.c_int, [_P, ctypes.POINTER(Reads), _P]),
         "gsnp_recall_resident": (ctypes.c_int, [_P]),
         "gsnp_fetch_sites": (ctypes.c_int, [_P, _I64, _I64, _P]),
         "gsnp_format_cns": (ctypes.c_int, [_P, ctypes.c_char_p, _P, ctypes.POINTER(_I64)]),
@@ -237,6 +238,12 @@ class Caller:
 
     def call(self, reads: Reads) -> None:
         self._check(self.lib.gsnp_call_chromosome(self.ctx, ctypes.byref(reads)), "gsnp_call_chromosome")
+
+    def call_into(self, reads: Reads, out_ptr: int) -> None:
+        """Call the chromosome and download every site's call to out_ptr (host
+        memory of length * 32 bytes, pinned for the downloads to overlap)."""
+        self._check(self.lib.gsnp_call_chromosome_into(self.ctx, ctypes.byref(reads), out_ptr),
+                    "gsnp_call_chromosome_into")
 
     def recall_resident(self) -> None:
         self._check(self.lib.gsnp_recall_resident(self.ctx), "gsnp_recall_resident")

@@ -47,6 +47,11 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+/* resident CTAs per SM the calling kernels are compiled for; this caps their
+ * registers (28 warps of the FP32 kernel, 16 of the FP64 kernel per SM) */
+constexpr int kFastCtasPerSm = 28 * 32 / kTile;
+constexpr int kFp64CtasPerSm = 16 * 32 / kTile;
+
 __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v) {
     int lo = 0, hi = n;
     while (lo < hi) {
@@ -67,7 +72,7 @@ template <int SLOTS>
 __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
                                                    bool active, uint32_t* recs) {
     /* records are appended in pileup order; sort_column puts them in
-     * ascending order once the tile's columns are dealt to the threads */
+     * ascending order after the pileup */
     const int lane = threadIdx.x & 31;
     const int L = a.L;
     const signed char qmin = (signed char)a.qmin;
@@ -185,56 +190,11 @@ __device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
 
 /* dbSNP row of each flagged site of a tile: the rows before the tile plus the
  * flagged sites before it in the tile (the rows are the flagged sites in
- * position order).  Every thread of the CTA calls it. */
-__device__ __forceinline__ int32_t tile_snp_row(const CallArgs& a, int64_t tile, bool flagged, int* s_cnt) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+ * position order).  Every lane of the tile's warp calls it. */
+__device__ __forceinline__ int32_t tile_snp_row(const CallArgs& a, int64_t tile, bool flagged) {
     const unsigned b = __ballot_sync(kFull, flagged);
-    if (lane == 0) s_cnt[warp] = __popc(b);
-    __syncthreads();
-    int before = 0;
-    for (int w = 0; w < warp; ++w) before += s_cnt[w];
-    return flagged ? a.tile_snp[tile] + before + __popc(b & ((1u << lane) - 1u)) : -1;
-}
-
-/* Shared state of a tile after its pileup, re-dealt to the threads by record
- * count.  The columns c, c+32, c+64, c+96 share shared-memory banks; the four
- * sites of each such class go to the four warps in order of record count, so
- * that each warp walks columns of similar depth while a warp's lanes still
- * touch 32 distinct banks.  The packed counts of the tile's sites pass
- * through the pcr-bitset area of the dynamic shared memory, which is free
- * until the record walk. */
-struct TileDeal {
-    int32_t snp_row[kTile];
-    int num[kTile];
-    int perm[kTile];
-    uint8_t ori[kTile];
-    int cnt[kWarpsPerTile];
-};
-
-/* Returns the tile column (site offset) this thread calls from here on and
- * its pileup counts; the pcr-bitset area may be written once it returns. */
-__device__ __forceinline__ int deal_by_depth(TileDeal& d, PackedPileup* pk_area, const PackedPileup& pk, bool active,
-                                             uint8_t ori, int32_t snp_row, SitePileup* p) {
-    const int t = threadIdx.x, lane = t & 31;
-    pk_area[t] = pk;
-    d.snp_row[t] = snp_row;
-    d.ori[t] = ori;
-    const int key = active ? (int)pk.num : -1;
-    d.num[t] = key;
-    __syncthreads();
-    int rank = 0;
-#pragma unroll
-    for (int k = 0; k < kWarpsPerTile; ++k) {
-        const int c = k * 32 + lane;
-        const int kc = d.num[c];
-        rank += (kc < key || (kc == key && c < t)) ? 1 : 0;
-    }
-    d.perm[rank * 32 + lane] = t;
-    __syncthreads();
-    const int me = d.perm[t];
-    *p = pk_area[me].unpack();
-    __syncthreads();
-    return me;
+    const int lane = threadIdx.x & 31;
+    return flagged ? a.tile_snp[tile] + __popc(b & ((1u << lane) - 1u)) : -1;
 }
 
 __device__ __forceinline__ void store_counts(const CallArgs& a, int64_t site, const SitePileup& p) {
@@ -284,14 +244,17 @@ __constant__ int c_slots[kNumBins] = {32, 48, 64, 96, 128, 256};
 
 /* Read range of every tile, [lower_bound(s0 - L + 1), lower_bound(s0 + kTile)),
  * in one pass over the sorted starts: read r is the lower bound of every
- * boundary b with pos[r - 1] < b <= pos[r] (thread n takes the boundaries
- * past the last read). */
-__global__ void tile_bounds_kernel(const int32_t* __restrict__ pos, int64_t n, int64_t n_tiles, int L,
-                                   int64_t* __restrict__ rng) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r > n) return;
-    const int64_t lo = r == 0 ? -((int64_t)1 << 40) : (int64_t)pos[r - 1];
-    const int64_t hi = r == n ? ((int64_t)1 << 40) : (int64_t)pos[r];
+ * boundary b with pos[r - 1] < b <= pos[r].  Threads r_begin .. r_end; the
+ * start of read r_end is next_pos (kNoRead past the last read), so that a
+ * segment of the reads can be done before the next segment is on the device:
+ * consecutive segments share their boundary thread, which writes the same
+ * values twice. */
+__global__ void tile_bounds_kernel(const int32_t* __restrict__ pos, int64_t r_begin, int64_t r_end, int64_t next_pos,
+                                   int64_t n_tiles, int L, int64_t* __restrict__ rng) {
+    const int64_t r = r_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > r_end) return;
+    const int64_t lo = r == 0 ? -kNoRead : (int64_t)pos[r - 1];
+    const int64_t hi = r == r_end ? next_pos : (int64_t)pos[r];
     if (lo >= hi) return;
     auto fdiv = [](int64_t x) { return x >= 0 ? x / kTile : -((-x + kTile - 1) / kTile); };
     /* first boundaries t*kTile - L + 1 in (lo, hi] */
@@ -307,9 +270,11 @@ __global__ void tile_bounds_kernel(const int32_t* __restrict__ pos, int64_t n, i
     for (int64_t t = t0; t <= t1; ++t) rng[t * 2 + 1] = r;
 }
 
-cudaError_t launch_tile_bounds(const CallArgs& a, cudaStream_t stream) {
-    tile_bounds_kernel<<<(unsigned)((a.n_reads + 1 + 255) / 256), 256, 0, stream>>>(a.pos, a.n_reads, a.n_tiles, a.L,
-                                                                                      a.tile_rng);
+cudaError_t launch_tile_bounds(const CallArgs& a, int64_t r_begin, int64_t r_end, int64_t next_pos,
+                               cudaStream_t stream) {
+    const int64_t n = r_end - r_begin + 1;
+    tile_bounds_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(a.pos, r_begin, r_end, next_pos, a.n_tiles,
+                                                                         a.L, a.tile_rng);
     return cudaGetLastError();
 }
 
@@ -350,51 +315,71 @@ cudaError_t launch_empty_calls(const CallArgs& a, SiteCall* calls, uint8_t* vali
 
 /* Per tile: the deepest site's record need (reads starting in [site - L + 1,
  * site], capped at 255) picks the depth bin; the window's mode picks the FP64
- * kernel (bins 0 .. kNumBins-1) or the fast one (the next kNumBins).  Each warp's read range is
- * stored for the calling kernels. */
-__global__ void __launch_bounds__(kTile) classify_tiles_kernel(CallArgs a, int pass, int* bin_count,
-                                                               int32_t* bin_tiles) {
-    __shared__ int32_t spos[kMaxStagedReads];
-    __shared__ int smax[kWarpsPerTile];
-    const int64_t tile = blockIdx.x;
+ * kernel (bins 0 .. kNumBins-1) or the fast one (the next kNumBins).  Each
+ * warp's read range is stored for the calling kernels.  A CTA classifies
+ * kClassifyTiles tiles and adds its bin counts to the global ones with one
+ * atomic per bin. */
+constexpr int kClassifyThreads = 256;
+constexpr int kClassifyTiles = kClassifyThreads / kTile;
+constexpr int kClassifyStage = 256;   /* read starts staged in shared memory per tile */
+static_assert(kClassifyThreads % kTile == 0, "a classify CTA holds whole tiles");
+
+__global__ void __launch_bounds__(kClassifyThreads) classify_tiles_kernel(CallArgs a, int pass, int64_t t_begin,
+                                                                          int64_t t_end, int* bin_count,
+                                                                          int32_t* bin_tiles) {
+    __shared__ int32_t spos[kClassifyTiles][kClassifyStage];
+    __shared__ int smax[kClassifyThreads / 32];
+    __shared__ int sbin_count[2 * kNumBins], sbin_base[2 * kNumBins];
+    const int lt = threadIdx.x / kTile, tt = threadIdx.x % kTile;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t tile = t_begin + (int64_t)blockIdx.x * kClassifyTiles + lt;
+    if (threadIdx.x < 2 * kNumBins) sbin_count[threadIdx.x] = 0;
     const int64_t s0 = tile * kTile;
-    const int win = (int)(s0 / kWin);
-    const uint8_t wflags = a.win_flags[win];
-    const bool external = (wflags & kWinExternalLik) != 0;
-    if (external != (pass == 1)) return;
-    const int64_t r_lo = a.tile_rng[tile * 2], r_hi = a.tile_rng[tile * 2 + 1];
-    const bool staged = (r_hi - r_lo) <= kMaxStagedReads;
-    if (staged)
-        for (int64_t i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) spos[i] = __ldg(a.pos + r_lo + i);
-    __syncthreads();
+    bool part = tile < t_end;
+    uint8_t wflags = 0;
+    if (part) {
+        wflags = a.win_flags[(int)(s0 / kWin)];
+        part = ((wflags & kWinExternalLik) != 0) == (pass == 1);
+    }
+    int64_t r_lo = 0, r_hi = 0;
+    if (part) {
+        r_lo = a.tile_rng[tile * 2];
+        r_hi = a.tile_rng[tile * 2 + 1];
+    }
     const int n = (int)(r_hi - r_lo);
+    const bool staged = r_hi - r_lo <= kClassifyStage;
+    if (part && staged)
+        for (int i = tt; i < n; i += kTile) spos[lt][i] = __ldg(a.pos + r_lo + i);
+    __syncthreads();
     auto lb = [&](int64_t v) -> int64_t {
-        return staged ? r_lo + lower_bound_s(spos, n, v) : r_lo + lower_bound_g(a.pos + r_lo, r_hi - r_lo, v);
+        return staged ? r_lo + lower_bound_s(spos[lt], n, v) : r_lo + lower_bound_g(a.pos + r_lo, r_hi - r_lo, v);
     };
-    const int64_t site = s0 + threadIdx.x;
+    const int64_t site = s0 + tt;
     int need = 0;
-    if (site < a.chr_len) {
+    if (part && site < a.chr_len) {
         const int64_t c = lb(site + 1) - lb(site - a.L + 1);
         need = (int)(c < kMaxRecords ? c : kMaxRecords);
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane < 2) {
-        const int64_t w0 = s0 + warp * 32;
-        a.warp_rng[(tile * kWarpsPerTile + warp) * 2 + lane] = lane == 0 ? lb(w0 - a.L + 1) : lb(w0 + 32);
-    }
+    if (part && lane < 2) a.warp_rng[tile * 2 + lane] = lane == 0 ? lb(s0 - a.L + 1) : lb(s0 + kTile);
     for (int off = 16; off > 0; off >>= 1) need = max(need, __shfl_xor_sync(kFull, need, off));
     if (lane == 0) smax[warp] = need;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int m = 0;
-        for (int i = 0; i < kWarpsPerTile; ++i) m = max(m, smax[i]);
+    int my_bin = -1, my_rank = 0;
+    if (part && tt == 0) {
+        const int m = smax[lt];
         const bool fast = a.precision == 1 && !(wflags & (kWinKeepLik | kWinExternalLik));
         int bin = 0;
         while (bin < kNumBins - 1 && m > c_slots[bin]) ++bin;
-        bin += fast ? kNumBins : 0;
-        const int idx = atomicAdd(&bin_count[bin], 1);
-        bin_tiles[(int64_t)bin * a.n_tiles + idx] = (int32_t)tile;
+        my_bin = bin + (fast ? kNumBins : 0);
+        my_rank = atomicAdd(&sbin_count[my_bin], 1);
     }
+    __syncthreads();
+    if (threadIdx.x < 2 * kNumBins) {
+        const int cnt = sbin_count[threadIdx.x];
+        sbin_base[threadIdx.x] = cnt ? atomicAdd(&bin_count[threadIdx.x], cnt) : 0;
+    }
+    __syncthreads();
+    if (my_bin >= 0) bin_tiles[(int64_t)my_bin * a.n_tiles + sbin_base[my_bin] + my_rank] = (int32_t)tile;
 }
 
 /* log10 genotype priors of every dbSNP row (kernel/posterior_kernel.cu:575-633,
@@ -441,30 +426,26 @@ cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, c
 /* ------------------------------------------------------------------------ */
 
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
+__global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);                   /* [SLOTS][kTile] */
     uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;    /* [nw][kTile] */
 
-    __shared__ TileDeal deal;
-    const int t = threadIdx.x, warp = t >> 5;
+    const int t = threadIdx.x;
     const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
     const int win = (int)(s0 / kWin);
     const uint8_t wflags = a.win_flags[win];
-    const int64_t r_lo = a.warp_rng[(tile * kWarpsPerTile + warp) * 2];
-    const int64_t r_hi = a.warp_rng[(tile * kWarpsPerTile + warp) * 2 + 1];
-    const bool active_t = s0 + t < a.chr_len;
-    const uint8_t ori_t = active_t ? __ldg(a.ori + s0 + t) : 0;
-    const int32_t row_t = tile_snp_row(a, tile, (ori_t & 8) != 0, deal.cnt);
-    const PackedPileup pk = warp_pileup<SLOTS>(a, r_lo, r_hi, s0 + t, active_t, recs_all + t);
-    SitePileup p;
-    const int me = deal_by_depth(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t, &p);
-    const int64_t site = s0 + me;
-    if (site >= a.chr_len) return;
-    const uint8_t ori = deal.ori[me];
-    uint32_t* recs = recs_all + me;
-    uint32_t* seen = seen_all + me;
+    const int64_t r_lo = a.warp_rng[tile * 2];
+    const int64_t r_hi = a.warp_rng[tile * 2 + 1];
+    const int64_t site = s0 + t;
+    const bool active = site < a.chr_len;
+    const uint8_t ori = active ? __ldg(a.ori + site) : 0;
+    const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
+    const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs_all + t).unpack();
+    if (!active) return;
+    uint32_t* recs = recs_all + t;
+    uint32_t* seen = seen_all + t;
     sort_column(recs, p.num);
 
     double tl[16];
@@ -488,7 +469,7 @@ __global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const 
     if (wflags & kWinKeepCounts) store_counts(a, site, p);
 
     double lp[16];
-    load_log_prior(a, deal.snp_row[me], ori, lp);
+    load_log_prior(a, snp_row, ori, lp);
     auto nq = [&](int b) { return neighbour_qsum(a, site, b); };
     SiteCall call;
     site_posterior(a, ori, p, tl, nullptr, lp, recs, kTile, nq, &call);
@@ -505,29 +486,25 @@ __global__ void __launch_bounds__(kTile, 4) call_tiles_kernel(CallArgs a, const 
  * keep counting past the capacities so that the host can size the pool and
  * run the pass again. */
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
+__global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);
     uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;
-    __shared__ TileDeal deal;
 
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int t = threadIdx.x, lane = t & 31;
     const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
     const int win = (int)(s0 / kWin);
     const uint8_t wflags = a.win_flags[win];
-    const int64_t r_lo = a.warp_rng[(tile * kWarpsPerTile + warp) * 2];
-    const int64_t r_hi = a.warp_rng[(tile * kWarpsPerTile + warp) * 2 + 1];
-    const bool active_t = s0 + t < a.chr_len;
-    const uint8_t ori_t = active_t ? __ldg(a.ori + s0 + t) : 0;
-    const int32_t row_t = tile_snp_row(a, tile, (ori_t & 8) != 0, deal.cnt);
-    const PackedPileup pk = warp_pileup<SLOTS>(a, r_lo, r_hi, s0 + t, active_t, recs_all + t);
-    SitePileup p;
-    const int me = deal_by_depth(deal, reinterpret_cast<PackedPileup*>(seen_all), pk, active_t, ori_t, row_t, &p);
-    const int64_t site = s0 + me;
+    const int64_t r_lo = a.warp_rng[tile * 2];
+    const int64_t r_hi = a.warp_rng[tile * 2 + 1];
+    const int64_t site = s0 + t;
     const bool active = site < a.chr_len;
-    uint32_t* recs = recs_all + me;
-    uint32_t* seen = seen_all + me;
+    const uint8_t ori = active ? __ldg(a.ori + site) : 0;
+    const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
+    const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs_all + t).unpack();
+    uint32_t* recs = recs_all + t;
+    uint32_t* seen = seen_all + t;
     if (active) sort_column(recs, p.num);
 
     uint8_t dflags = 0;
@@ -566,7 +543,6 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
             }
             k.add(x);
         }
-        const uint8_t ori = deal.ori[me];
         SiteCall call;
         if ((site & 4095) == 0 && a.stats) dflags = kCallSampled;
         const bool empty = p.num == 0 && (p.ca[0] | p.ca[1] | p.ca[2] | p.ca[3]) == 0 && a.empty_valid[ori];
@@ -576,7 +552,7 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
             call.depth = p.depth;
             call.repeat_time = p.repeat;
             call.flags |= dflags;
-        } else if (fast_posterior(a, deal.snp_row[me], ori, p, k.s, p.num, &call)) {
+        } else if (fast_posterior(a, snp_row, ori, p, k.s, p.num, &call)) {
             call.flags |= dflags;
         } else {
             call = SiteCall{};
@@ -609,7 +585,7 @@ __global__ void __launch_bounds__(kTile, 7) call_fast_kernel(CallArgs a, const i
     d.rec_off = (uint32_t)off;
     d.num = (uint16_t)p.num;
     d.dep_uni = (uint16_t)p.dep_uni;
-    d.snp_row = deal.snp_row[me];
+    d.snp_row = snp_row;
     d.flags = dflags;
 #pragma unroll
     for (int i = 0; i < 3; ++i) d.pad[i] = 0;
@@ -684,17 +660,18 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
 static const int kSlots[kNumBins] = {32, 48, 64, 96, 128, 256};
 
 size_t call_smem_bytes(int slots, int L) {
-    /* records [slots][kTile], then the pcr bitsets [nw][kTile], which first
-     * hold the tile's packed pileup counts */
+    /* records [slots][kTile], then the pcr bitsets [nw][kTile] */
     const size_t nw = (2 * L + 31) >> 5;
-    const size_t bits = nw * kTile * 4, packed = sizeof(PackedPileup) * kTile;
-    return (size_t)slots * kTile * 4 + (bits > packed ? bits : packed);
+    return (size_t)slots * kTile * 4 + nw * kTile * 4;
 }
 
-cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32_t* d_bin_tiles, cudaStream_t stream) {
+cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
+                            int32_t* d_bin_tiles, cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(d_bin_count, 0, sizeof(int) * 2 * kNumBins, stream);
     if (e != cudaSuccess) return e;
-    classify_tiles_kernel<<<(unsigned)a.n_tiles, kTile, 0, stream>>>(a, pass, d_bin_count, d_bin_tiles);
+    const unsigned blocks = (unsigned)((t_end - t_begin + kClassifyTiles - 1) / kClassifyTiles);
+    if (blocks == 0) return cudaSuccess;
+    classify_tiles_kernel<<<blocks, kClassifyThreads, 0, stream>>>(a, pass, t_begin, t_end, d_bin_count, d_bin_tiles);
     return cudaGetLastError();
 }
 

@@ -12,9 +12,12 @@ namespace gsnp {
 
 constexpr int kNumStats = 8;
 
-constexpr int kTile = 128;        /* sites per tile (divides the window) */
-constexpr int kWarpsPerTile = kTile / 32;
-constexpr int kMaxStagedReads = 2048;
+/* sites per tile (divides the window): one warp, one thread per site.  A
+ * CTA's shared memory and registers are released as soon as its warp is
+ * done, where with several warps per tile the shallow-site warps would hold
+ * them idle until the deepest warp finished. */
+constexpr int kTile = 32;
+constexpr int64_t kNoRead = (int64_t)1 << 40;   /* a start beyond every read */
 constexpr int kNumBins = 6;       /* record slots 32 / 48 / 64 / 96 / 128 / 256 */
 
 /* calling kernels */
@@ -86,7 +89,7 @@ struct CallArgs {
     /* tiles */
     int64_t n_tiles;
     int64_t* tile_rng;           /* [n_tiles][2]: reads starting in [s0 - L + 1, s0 + kTile) of each tile */
-    int64_t* warp_rng;           /* [n_tiles][4][2]: reads that can cover each warp's 32 sites */
+    int64_t* warp_rng;           /* [n_tiles][2]: reads that can cover each tile's sites */
     /* the call of a site without records or counts, by site code (16 entries;
      * empty_valid[code] = 0 where it is not a fixed homozygous call) */
     const SiteCall* empty_calls;

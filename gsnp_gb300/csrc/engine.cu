@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <thread>
 #include <vector>
@@ -34,11 +35,13 @@
 
 namespace gsnp {
 
-cudaError_t launch_classify(const CallArgs& a, int pass, int* d_bin_count, int32_t* d_bin_tiles, cudaStream_t stream);
+cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
+                            int32_t* d_bin_tiles, cudaStream_t stream);
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
-cudaError_t launch_tile_bounds(const CallArgs& a, cudaStream_t stream);
+cudaError_t launch_tile_bounds(const CallArgs& a, int64_t r_begin, int64_t r_end, int64_t next_pos,
+                               cudaStream_t stream);
 cudaError_t launch_empty_calls(const CallArgs& a, SiteCall* calls, uint8_t* valid, cudaStream_t stream);
 int bin_slots(int bin);
 
@@ -138,52 +141,70 @@ __global__ void __launch_bounds__(kDepThreads) dep_index_kernel(int64_t n, const
     }
 }
 
-__global__ void gather_reads_kernel(int64_t n, const int64_t* __restrict__ idx, int64_t n_raw,
-                                    const int32_t* __restrict__ rpos,
-                                    const int32_t* __restrict__ rlen, const int32_t* __restrict__ rhit,
-                                    const uint8_t* __restrict__ rstrand, const uint8_t* __restrict__ seq,
-                                    const uint8_t* __restrict__ qual, int pitch, int L, int32_t* __restrict__ pos,
-                                    int32_t* __restrict__ lenhit, int32_t* __restrict__ len,
-                                    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq, int* __restrict__ error) {
-    /* one warp per deposited read: its start, length, hit count and strand,
-     * and its base|quality row with the bases in upper case ('A' past the
-     * read's end; any base other than ACGT/acgt sets *error) */
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= n) return;
-    const int64_t src = idx[warp];
-    if (src < 0 || src >= n_raw) {   /* the host and device filters disagree */
-        if (lane == 0) atomicExch(error, 3);
-        return;
+__device__ __forceinline__ uint8_t upper_base(uint8_t b, bool* bad) {
+    switch (b) {
+        case 'A': case 'a': return 'A';
+        case 'C': case 'c': return 'C';
+        case 'G': case 'g': return 'G';
+        case 'T': case 't': return 'T';
+        default: *bad = true; return 'A';
     }
-    const int32_t rl = rlen[src];
-    if (lane == 0) {
-        pos[warp] = rpos[src];
-        len[warp] = rl;
-        lenhit[warp] = (int32_t)(((uint32_t)(rl & 0xffff) << 16) | ((uint32_t)rhit[src] & 0xffffu));
-        strand[warp] = rstrand[src];
-    }
-    const uint8_t* s = seq + src * pitch;
-    const uint8_t* q = qual + src * pitch;
-    uint16_t* d = bq + warp * L;
-    bool bad = false;
-    for (int c = lane; c < L; c += 32) {
-        uint8_t b = 'A', qq = 0;
-        if (c < pitch) {
-            qq = q[c];
-            if (c < rl) {
-                switch (s[c]) {
-                    case 'A': case 'a': b = 'A'; break;
-                    case 'C': case 'c': b = 'C'; break;
-                    case 'G': case 'g': b = 'G'; break;
-                    case 'T': case 't': b = 'T'; break;
-                    default: bad = true;
+}
+
+/* The deposited reads in the packed layout of the calling kernels: start,
+ * len<<16|hit, len, strand, and the base|quality row with the bases in upper
+ * case ('A' past the read's end; a base other than ACGT/acgt sets *error to
+ * 2).  Rows [row_begin, row_end); a block holds rows_per_block rows, each
+ * thread VEC consecutive columns of one row (VEC = 4 when L and the pitch are
+ * multiples of 4 and L <= pitch: 32-bit loads, 64-bit stores). */
+template <int VEC>
+__global__ void __launch_bounds__(256) gather_reads_kernel(
+    int64_t row_begin, int64_t row_end, const int64_t* __restrict__ idx, int64_t n_raw, const int32_t* __restrict__ rpos,
+    const int32_t* __restrict__ rlen, const int32_t* __restrict__ rhit, const uint8_t* __restrict__ rstrand,
+    const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual, int pitch, int L, int rows_per_block,
+    int32_t* __restrict__ pos, int32_t* __restrict__ lenhit, int32_t* __restrict__ len,
+    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq, int* __restrict__ error) {
+    const int per_row = (L + VEC - 1) / VEC;
+    const int local = threadIdx.x / per_row, cv = threadIdx.x - local * per_row;
+    const int64_t row = row_begin + (int64_t)blockIdx.x * rows_per_block + local;
+    bool bad = false, bad_idx = false;
+    if (local < rows_per_block && row < row_end) {
+        const int64_t src = idx[row];
+        if (src < 0 || src >= n_raw) {   /* the host and device filters disagree */
+            bad_idx = true;
+        } else {
+            const int32_t rl = rlen[src];
+            if (cv == 0) {
+                pos[row] = rpos[src];
+                len[row] = rl;
+                lenhit[row] = (int32_t)(((uint32_t)(rl & 0xffff) << 16) | ((uint32_t)rhit[src] & 0xffffu));
+                strand[row] = rstrand[src];
+            }
+            const int c0 = cv * VEC;
+            if (VEC == 4) {
+                const uint32_t s4 = *reinterpret_cast<const uint32_t*>(seq + src * pitch + c0);
+                const uint32_t q4 = *reinterpret_cast<const uint32_t*>(qual + src * pitch + c0);
+                uint32_t lo = 0, hi = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint8_t b = c0 + k < rl ? upper_base((uint8_t)(s4 >> (8 * k)), &bad) : (uint8_t)'A';
+                    const uint32_t v = (uint32_t)b | (((q4 >> (8 * k)) & 0xffu) << 8);
+                    if (k < 2) lo |= v << (16 * k);
+                    else hi |= v << (16 * (k - 2));
                 }
+                *reinterpret_cast<uint2*>(bq + row * L + c0) = make_uint2(lo, hi);
+            } else {
+                uint8_t b = 'A', q = 0;
+                if (c0 < pitch) {
+                    q = qual[src * pitch + c0];
+                    if (c0 < rl) b = upper_base(seq[src * pitch + c0], &bad);
+                }
+                bq[row * L + c0] = (uint16_t)b | ((uint16_t)q << 8);
             }
         }
-        d[c] = (uint16_t)b | ((uint16_t)qq << 8);
     }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(error, 2);
+    const unsigned any_bad = __ballot_sync(0xffffffffu, bad), any_idx = __ballot_sync(0xffffffffu, bad_idx);
+    if ((threadIdx.x & 31) == 0 && (any_bad | any_idx)) atomicMax(error, any_idx ? 3 : 2);
 }
 
 /* pass-1 calibration histogram (cpp/matrix.cc:58-118): unique reads, non-N
@@ -292,7 +313,7 @@ struct gsnp_context {
     uint32_t* d_dpool = nullptr;             /* their sorted records */
     unsigned long long* d_dcount = nullptr;  /* [2] requested sites, record words */
     int64_t dsite_cap = 0, dpool_cap = 0;
-    int64_t* d_warp_rng = nullptr;  /* [n_tiles][4][2] */
+    int64_t* d_warp_rng = nullptr;  /* [n_tiles][2] */
     int64_t* d_tile_rng = nullptr;  /* [n_tiles][2] */
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
@@ -302,11 +323,17 @@ struct gsnp_context {
     bool called = false;
     uint64_t stats[kNumStats] = {};
     /* CUDA events around each launch of the last calling pass */
-    static const int kMaxLaunches = 32;
+    static const int kMaxLaunches = 128;
     cudaEvent_t ev[2 * kMaxLaunches] = {};
     gsnp_launch_info launches[kMaxLaunches];
     int n_launches = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
+    /* the call's copy streams: uploads in chunks, downloads per segment */
+    static const int kUploadChunks = 16;
+    cudaStream_t up_stream = nullptr, down_stream = nullptr;
+    cudaEvent_t ev_small = nullptr, ev_seg = nullptr, ev_chunk[kUploadChunks] = {};
+    int* d_gerror = nullptr;       /* gather: 2 a base other than ACGT/acgt, 3 index list mismatch */
+    int64_t n_gathered = 0;        /* deposited reads in the packed layout so far */
     /* dictionary codec scratch (-C output) */
     void* d_dict = nullptr;
     size_t dict_bytes = 0;
@@ -384,7 +411,7 @@ void free_all(gsnp_context* c) {
                     c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_dict, c->d_win_host_src, c->d_emit,
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-                    c->d_idx, c->d_dep_off};
+                    c->d_idx, c->d_dep_off, c->d_gerror};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -446,7 +473,22 @@ CallArgs make_args(gsnp_context* c) {
     return a;
 }
 
-int run_calling(gsnp_context* c) {
+/* A stretch of whole windows called together: its tiles, the deposited reads
+ * that start in it, the alignments that hold them and the start of the next
+ * deposited read. */
+struct Segment {
+    int64_t t0, t1;      /* tiles */
+    int64_t dlo, dhi;    /* deposited reads */
+    int64_t raw_hi;      /* alignments [0, raw_hi) hold deposited reads [0, dhi) */
+    int64_t next_pos;    /* start of deposited read dhi, kNoRead when there is none */
+};
+
+/* The calling pass, segment by segment.  before(s) runs first for each
+ * segment (the call gathers the reads there; it must leave the reads of
+ * segment s + 1 on the device too, which the tile ranges and the next-site
+ * lookups of segment s reach), after(s) once its calls are queued. */
+int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
+                const std::function<int(size_t)>& after) {
     const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
     if (!c->snp_lp_ready) {
         CK(dev_alloc(&c->d_snp_lp, (size_t)std::max<int64_t>(c->n_snp, 1) * 16), "cudaMalloc dbSNP priors");
@@ -462,7 +504,7 @@ int run_calling(gsnp_context* c) {
     }
     if (n_tiles > c->tiles_cap) {
         CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * 2 * kNumBins), "cudaMalloc bins");
-        CK(dev_alloc(&c->d_warp_rng, (size_t)n_tiles * kWarpsPerTile * 2), "cudaMalloc ranges");
+        CK(dev_alloc(&c->d_warp_rng, (size_t)n_tiles * 2), "cudaMalloc ranges");
         CK(dev_alloc(&c->d_tile_rng, (size_t)n_tiles * 2), "cudaMalloc ranges");
         c->tiles_cap = n_tiles;
     }
@@ -495,56 +537,76 @@ int run_calling(gsnp_context* c) {
     auto end = [&](int k) {
         if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], c->stream);
     };
-    for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
-        int k = begin(kKindClassify, 0, n_tiles);
-        if (pass == 0) CK(launch_tile_bounds(a, c->stream), "tile bounds kernel");
-        CK(launch_classify(a, pass, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
-        end(k);
-        CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(c->h_bin_count), cudaMemcpyDeviceToHost,
-                           c->stream),
-           "bin counts");
-        CK(cudaStreamSynchronize(c->stream), "classify");
-        bool any_fast = false;
-        for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
-        for (int b = 0; b < kNumBins; ++b) {
-            if (c->h_bin_count[b] == 0) continue;
-            k = begin(kKindFP64, bin_slots(b), c->h_bin_count[b]);
-            CK(launch_bin(a, kKindFP64, b, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b], c->stream),
-               "calling kernel");
-            end(k);
+    for (size_t si = 0; si < segs.size(); ++si) {
+        const Segment& g = segs[si];
+        if (before) {
+            const int rc = before(si);
+            if (rc != GSNP_OK) return rc;
         }
-        if (!any_fast) continue;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-            const CallArgs af = make_args(c);
-            const int first = c->n_launches;
-            CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+        CallArgs a = make_args(c);
+        a.n_reads = c->n_gathered;
+        int k = begin(kKindClassify, 0, g.t1 - g.t0);
+        CK(launch_tile_bounds(a, g.dlo, g.dhi, g.next_pos, c->stream), "tile bounds kernel");
+        for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
+            if (pass == 1) k = begin(kKindClassify, 0, g.t1 - g.t0);
+            CK(launch_classify(a, pass, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
+            end(k);
+            CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(c->h_bin_count), cudaMemcpyDeviceToHost,
+                               c->stream),
+               "bin counts");
+            CK(cudaStreamSynchronize(c->stream), "classify");
+            bool any_fast = false;
+            for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
             for (int b = 0; b < kNumBins; ++b) {
-                const int nb = c->h_bin_count[kNumBins + b];
-                if (nb == 0) continue;
-                k = begin(kKindFast, bin_slots(b), nb);
-                CK(launch_bin(af, kKindFast, b, c->d_bin_tiles + (int64_t)(kNumBins + b) * n_tiles, nb, c->stream),
-                   "fast calling kernel");
+                if (c->h_bin_count[b] == 0) continue;
+                k = begin(kKindFP64, bin_slots(b), c->h_bin_count[b]);
+                CK(launch_bin(a, kKindFP64, b, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b], c->stream),
+                   "calling kernel");
                 end(k);
             }
-            CK(cudaMemcpyAsync(c->h_dcount, c->d_dcount, sizeof(c->h_dcount), cudaMemcpyDeviceToHost, c->stream),
-               "deferred counts");
-            CK(cudaStreamSynchronize(c->stream), "fast calling");
-            const int64_t ns = (int64_t)c->h_dcount[0], nw = (int64_t)c->h_dcount[1];
-            if (ns <= c->dsite_cap && nw <= c->dpool_cap) {
-                k = begin(kKindDeferred, 0, (ns + kTile - 1) / kTile);
-                if (k >= 0) c->launches[k].sites = ns;
-                CK(launch_deferred(af, ns, c->stream), "deferred calling kernel");
-                end(k);
-                break;
+            if (!any_fast) continue;
+            for (int attempt = 0; attempt < 2; ++attempt) {
+                CallArgs af = make_args(c);
+                af.n_reads = c->n_gathered;
+                const int first = c->n_launches;
+                CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+                for (int b = 0; b < kNumBins; ++b) {
+                    const int nb = c->h_bin_count[kNumBins + b];
+                    if (nb == 0) continue;
+                    k = begin(kKindFast, bin_slots(b), nb);
+                    CK(launch_bin(af, kKindFast, b, c->d_bin_tiles + (int64_t)(kNumBins + b) * n_tiles, nb,
+                                  c->stream),
+                       "fast calling kernel");
+                    end(k);
+                }
+                CK(cudaMemcpyAsync(c->h_dcount, c->d_dcount, sizeof(c->h_dcount), cudaMemcpyDeviceToHost,
+                                   c->stream),
+                   "deferred counts");
+                CK(cudaStreamSynchronize(c->stream), "fast calling");
+                const int64_t ns = (int64_t)c->h_dcount[0], nw = (int64_t)c->h_dcount[1];
+                if (ns <= c->dsite_cap && nw <= c->dpool_cap) {
+                    if (ns > 0) {
+                        k = begin(kKindDeferred, 0, (ns + kTile - 1) / kTile);
+                        if (k >= 0) c->launches[k].sites = ns;
+                        CK(launch_deferred(af, ns, c->stream), "deferred calling kernel");
+                        end(k);
+                    }
+                    break;
+                }
+                if (attempt == 1) return fail(c, GSNP_ERR_STATE, "deferred-site pool overflow");
+                /* grow the pool to what the segment asked for and run its fast
+                 * kernels again (their sampled-site statistics were not yet
+                 * counted: that happens in the deferred pass) */
+                c->dsite_cap = std::max(c->dsite_cap, ns + ns / 8 + 1024);
+                c->dpool_cap = std::max(c->dpool_cap, nw + nw / 8 + 65536);
+                CK(dev_alloc(&c->d_dsites, (size_t)c->dsite_cap), "cudaMalloc deferred");
+                CK(dev_alloc(&c->d_dpool, (size_t)c->dpool_cap), "cudaMalloc deferred");
+                c->n_launches = first;
             }
-            if (attempt == 1) return fail(c, GSNP_ERR_STATE, "deferred-site pool overflow");
-            /* grow the pool to what the pass asked for and run it again */
-            c->dsite_cap = std::max(c->dsite_cap, ns + ns / 8 + 1024);
-            c->dpool_cap = std::max(c->dpool_cap, nw + nw / 8 + 65536);
-            CK(dev_alloc(&c->d_dsites, (size_t)c->dsite_cap), "cudaMalloc deferred");
-            CK(dev_alloc(&c->d_dpool, (size_t)c->dpool_cap), "cudaMalloc deferred");
-            CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * kNumStats, c->stream), "memset");
-            c->n_launches = first;
+        }
+        if (after) {
+            const int rc = after(si);
+            if (rc != GSNP_OK) return rc;
         }
     }
     int err = 0;
@@ -556,6 +618,241 @@ int run_calling(gsnp_context* c) {
     if (err) return fail(c, GSNP_ERR_STATE, "record slots of a tile overflowed its depth bin");
     c->stats[0] = (uint64_t)c->chr_len;
     c->called = true;
+    return GSNP_OK;
+}
+
+
+/* the whole chromosome as one segment (the deposited reads are resident) */
+Segment whole_segment(const gsnp_context* c) {
+    return Segment{0, (c->chr_len + kTile - 1) / kTile, 0, c->n_dep, 0, kNoRead};
+}
+
+/* Window-aligned segments with about the same number of windows each.  The
+ * deposited reads of a window are the passing alignments of its run (less the
+ * dropped last one), so the run list gives every segment's read ranges. */
+std::vector<Segment> plan_segments(const gsnp_context* c, const ReadView& r, int n_seg) {
+    const WindowPlan& P = c->plan;
+    const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    const int64_t per = (P.n_windows + n_seg - 1) / n_seg;
+    std::vector<Segment> segs;
+    size_t k = 0;            /* first run at or past the segment's first window */
+    int64_t dep = 0;         /* passing alignments of the runs before run k */
+    int64_t raw = 0;
+    for (int64_t w0 = 0; w0 < P.n_windows; w0 += per) {
+        const int64_t w1 = std::min(P.n_windows, w0 + per);
+        Segment g;
+        g.t0 = std::min(n_tiles, w0 * (int64_t)(kWin / kTile));
+        g.t1 = w1 == P.n_windows ? n_tiles : std::min(n_tiles, w1 * (int64_t)(kWin / kTile));
+        g.dlo = std::min(dep, P.n_deposited);
+        while (k < P.runs.size() && P.runs[k].window < w1) {
+            dep += P.runs[k].count;
+            ++k;
+        }
+        raw = k < P.runs.size() ? P.runs[k].first : r.n;
+        g.dhi = std::min(dep, P.n_deposited);
+        g.raw_hi = raw;
+        g.next_pos = g.dhi < P.n_deposited ? (int64_t)r.pos[P.runs[k].first] : kNoRead;
+        if (g.t1 > g.t0 || w1 == P.n_windows) segs.push_back(g);
+    }
+    return segs;
+}
+
+/* number of segments of a call: one per two million deposited reads, 1 .. 16
+ * (GSNP_SEGMENTS overrides) */
+int segment_count(int64_t n_dep, int64_t n_windows) {
+    int n = (int)std::min<int64_t>(16, std::max<int64_t>(1, n_dep / 2000000));
+    if (const char* e = getenv("GSNP_SEGMENTS")) n = std::max(1, atoi(e));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(n, n_windows));
+}
+
+/* gsnp_call_chromosome, and with out != NULL the download of every call.
+ *   copy stream up:   start/length/hit/strand, then bases and qualities in
+ *                     kUploadChunks pieces, an event after each;
+ *   host:             the window replay, meanwhile;
+ *   compute stream:   the deposited index list once the small arrays are
+ *                     there, then per segment the gather of the next
+ *                     segment's reads (after the upload pieces that hold
+ *                     them) and the calling of this one;
+ *   copy stream down: each segment's calls once they are final. */
+int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
+    if (!c || !r || r->n < 0 || r->pitch < 0 ||
+        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
+        return fail(c, GSNP_ERR_ARG, "null read arrays");
+    if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
+    cudaSetDevice(c->device);
+    PhaseTimer timer("gsnp_call_chromosome");
+    const int L = c->params.read_length;
+    const int64_t n = r->n;
+    if (!c->up_stream) {
+        CK(cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaStreamCreateWithFlags(&c->down_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_small, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_seg, cudaEventDisableTiming), "cudaEventCreate");
+        for (int i = 0; i < gsnp_context::kUploadChunks; ++i)
+            CK(cudaEventCreateWithFlags(&c->ev_chunk[i], cudaEventDisableTiming), "cudaEventCreate");
+        CK(dev_alloc(&c->d_gerror, 1), "cudaMalloc");
+    }
+    /* 1. uploads, on their own stream */
+    const size_t raw = (size_t)n * r->pitch;
+    if (n > c->raw_cap || raw > c->raw_bytes) {
+        const int64_t cap = std::max<int64_t>(n, 1);
+        CK(dev_alloc(&c->d_raw_pos, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_len, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_hit, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_strand, (size_t)cap), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_seq, std::max<size_t>(raw, 1)), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_raw_qual, std::max<size_t>(raw, 1)), "cudaMalloc raw");
+        CK(dev_alloc(&c->d_idx, (size_t)cap), "cudaMalloc raw");
+        c->raw_cap = cap;
+        c->raw_bytes = std::max<size_t>(raw, 1);
+    }
+    const int64_t chunk_rows = std::max<int64_t>(1, (n + gsnp_context::kUploadChunks - 1) / gsnp_context::kUploadChunks);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(c->d_raw_pos, r->pos, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_len, r->len, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_hit, r->hit, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
+        CK(cudaMemcpyAsync(c->d_raw_strand, r->strand, n, cudaMemcpyHostToDevice, c->up_stream), "upload");
+    }
+    CK(cudaEventRecord(c->ev_small, c->up_stream), "event");
+    for (int k = 0; k < gsnp_context::kUploadChunks; ++k) {
+        const int64_t b = std::min(n, k * chunk_rows), e = std::min(n, (k + 1) * chunk_rows);
+        if (e > b) {
+            const size_t off = (size_t)b * r->pitch, bytes = (size_t)(e - b) * r->pitch;
+            CK(cudaMemcpyAsync(c->d_raw_seq + off, r->seq + off, bytes, cudaMemcpyHostToDevice, c->up_stream),
+               "upload seq");
+            CK(cudaMemcpyAsync(c->d_raw_qual + off, r->qual + off, bytes, cudaMemcpyHostToDevice, c->up_stream),
+               "upload qual");
+        }
+        CK(cudaEventRecord(c->ev_chunk[k], c->up_stream), "event");
+    }
+    timer.mark("uploads issued");
+    auto drain = [&]() {
+        cudaStreamSynchronize(c->up_stream);
+        cudaStreamSynchronize(c->stream);
+        cudaStreamSynchronize(c->down_stream);
+    };
+    /* 2. host: the length check and the window replay */
+    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
+    std::string err;
+    const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, host_threads(), &c->plan, &err);
+    if (rc != 0) {
+        drain();
+        return fail(c, rc, err);
+    }
+    timer.mark("window replay");
+    const WindowPlan& P = c->plan;
+    const int64_t nd = P.n_deposited;
+
+    /* window tables */
+    if (P.n_windows > c->n_win_alloc) {
+        CK(dev_alloc(&c->d_win_flags, (size_t)P.n_windows), "cudaMalloc");
+        CK(dev_alloc(&c->d_win_lik_src, (size_t)P.n_windows), "cudaMalloc");
+        CK(dev_alloc(&c->d_win_host_src, (size_t)P.n_windows), "cudaMalloc");
+        c->n_win_alloc = P.n_windows;
+    }
+    CK(cudaMemcpyAsync(c->d_win_flags, P.flags.data(), P.n_windows, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(c->d_win_lik_src, P.lik_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
+       "upload");
+    CK(cudaMemcpyAsync(c->d_win_host_src, P.host_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
+       "upload");
+    bool need_counts = false, need_lik = false;
+    for (int64_t w = 0; w < P.n_windows; ++w) {
+        need_counts |= (P.flags[w] & kWinKeepCounts) != 0;
+        need_lik |= (P.flags[w] & kWinKeepLik) != 0;
+    }
+    if (need_counts && !c->have_counts) {
+        CK(dev_alloc(&c->d_counts, (size_t)c->chr_len), "cudaMalloc counts");
+        c->have_counts = true;
+    }
+    if (need_lik && !c->have_lik_keep) {
+        CK(dev_alloc(&c->d_lik_keep, (size_t)c->chr_len * 10), "cudaMalloc likelihood");
+        c->have_lik_keep = true;
+    }
+    if (nd > c->cap_dep) {
+        CK(dev_alloc(&c->d_pos, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_lenhit, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_len, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_strand, (size_t)nd), "cudaMalloc reads");
+        CK(dev_alloc(&c->d_bq, (size_t)nd * L + 8), "cudaMalloc reads");
+        c->cap_dep = nd;
+    }
+    c->n_dep = nd;
+    c->n_gathered = 0;
+    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) + 2ULL * (uint64_t)n * r->pitch;
+    c->d2h_bytes = out ? (uint64_t)c->chr_len * sizeof(SiteCall) : 0;
+
+    /* 3. the deposited index list, once the small arrays are on the device */
+    CK(cudaMemsetAsync(c->d_gerror, 0, sizeof(int), c->stream), "memset");
+    CK(cudaStreamWaitEvent(c->stream, c->ev_small, 0), "wait");
+    if (nd > 0) {
+        const int64_t n_chunks = (n + kDepChunk - 1) / kDepChunk;
+        if (n_chunks > c->dep_chunk_cap) {
+            CK(dev_alloc(&c->d_dep_off, (size_t)n_chunks), "cudaMalloc index");
+            c->dep_chunk_cap = n_chunks;
+        }
+        dep_count_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(n, c->d_raw_pos, c->d_raw_len,
+                                                                            c->chr_len, c->d_dep_off);
+        dep_scan_kernel<<<1, 1024, 0, c->stream>>>(c->d_dep_off, n_chunks);
+        dep_index_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(n, c->d_raw_pos, c->d_raw_len, c->chr_len,
+                                                                            c->d_dep_off, nd, c->d_idx);
+        CK(cudaGetLastError(), "index kernels");
+    }
+
+    /* 4. segments: gather one segment ahead, call, download */
+    const std::vector<Segment> segs = plan_segments(c, v, segment_count(nd, P.n_windows));
+    const bool vec4 = L % 4 == 0 && r->pitch % 4 == 0 && L <= r->pitch;
+    const int per_row = vec4 ? L / 4 : L;
+    const int rows_per_block = std::max(1, 256 / per_row);
+    int64_t gathered_seg = -1;
+    auto gather_through = [&](int64_t target) -> int {
+        while (gathered_seg < target) {
+            const Segment& g = segs[(size_t)++gathered_seg];
+            if (g.dhi > g.dlo) {
+                const int64_t chunk = std::min<int64_t>((g.raw_hi - 1) / chunk_rows, gsnp_context::kUploadChunks - 1);
+                CK(cudaStreamWaitEvent(c->stream, c->ev_chunk[chunk], 0), "wait");
+                const int64_t rows = g.dhi - g.dlo;
+                const unsigned blocks = (unsigned)((rows + rows_per_block - 1) / rows_per_block);
+                if (vec4)
+                    gather_reads_kernel<4><<<blocks, 256, 0, c->stream>>>(
+                        g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
+                        c->d_raw_seq, c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
+                        c->d_strand, c->d_bq, c->d_gerror);
+                else
+                    gather_reads_kernel<1><<<blocks, 256, 0, c->stream>>>(
+                        g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
+                        c->d_raw_seq, c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
+                        c->d_strand, c->d_bq, c->d_gerror);
+                CK(cudaGetLastError(), "gather kernel");
+            }
+            c->n_gathered = g.dhi;
+        }
+        return GSNP_OK;
+    };
+    auto before = [&](size_t si) { return gather_through(std::min<int64_t>((int64_t)si + 1, (int64_t)segs.size() - 1)); };
+    auto after = [&](size_t si) -> int {
+        if (!out) return GSNP_OK;
+        const int64_t s0 = segs[si].t0 * kTile, s1 = std::min(segs[si].t1 * kTile, c->chr_len);
+        if (s1 <= s0) return GSNP_OK;
+        CK(cudaEventRecord(c->ev_seg, c->stream), "event");
+        CK(cudaStreamWaitEvent(c->down_stream, c->ev_seg, 0), "wait");
+        CK(cudaMemcpyAsync(out + s0, c->d_out + s0, (size_t)(s1 - s0) * sizeof(SiteCall), cudaMemcpyDeviceToHost,
+                           c->down_stream),
+           "download");
+        return GSNP_OK;
+    };
+    int rc2 = run_calling(c, segs, before, after);
+    cudaError_t e_up = cudaStreamSynchronize(c->up_stream), e_down = cudaStreamSynchronize(c->down_stream);
+    timer.mark("calling (pipelined)");
+    if (rc2 != GSNP_OK) {
+        drain();
+        return rc2;
+    }
+    CK(e_up, "upload");
+    CK(e_down, "download");
+    int gerr = 0;
+    CK(cudaMemcpy(&gerr, c->d_gerror, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+    if (gerr == 3) return fail(c, GSNP_ERR_STATE, "deposited alignment list does not match the window replay");
+    if (gerr) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
     return GSNP_OK;
 }
 
@@ -592,6 +889,18 @@ void gsnp_context_destroy(gsnp_context* c) {
     if (c->h_text) cudaFreeHost(c->h_text);
     for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < gsnp_context::kUploadChunks; ++i)
+        if (c->ev_chunk[i]) cudaEventDestroy(c->ev_chunk[i]);
+    if (c->ev_small) cudaEventDestroy(c->ev_small);
+    if (c->ev_seg) cudaEventDestroy(c->ev_seg);
+    if (c->up_stream) {
+        cudaStreamSynchronize(c->up_stream);
+        cudaStreamDestroy(c->up_stream);
+    }
+    if (c->down_stream) {
+        cudaStreamSynchronize(c->down_stream);
+        cudaStreamDestroy(c->down_stream);
+    }
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -673,116 +982,11 @@ int gsnp_load_reference(gsnp_context* c, const uint8_t* codes, int64_t length, c
     return GSNP_OK;
 }
 
-int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) {
-    if (!c || !r || r->n < 0 || (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
-        return fail(c, GSNP_ERR_ARG, "null read arrays");
-    if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
-    cudaSetDevice(c->device);
-    PhaseTimer timer("gsnp_call_chromosome");
-    const int L = c->params.read_length;
-    const int64_t n = r->n;
-    /* 1. the raw alignments go to the device first; the copies run while the
-     *    host replays the window loop */
-    const size_t raw = (size_t)n * r->pitch;
-    if (n > c->raw_cap || raw > c->raw_bytes) {
-        const int64_t cap = std::max<int64_t>(n, 1);
-        CK(dev_alloc(&c->d_raw_pos, (size_t)cap), "cudaMalloc raw");
-        CK(dev_alloc(&c->d_raw_len, (size_t)cap), "cudaMalloc raw");
-        CK(dev_alloc(&c->d_raw_hit, (size_t)cap), "cudaMalloc raw");
-        CK(dev_alloc(&c->d_raw_strand, (size_t)cap), "cudaMalloc raw");
-        CK(dev_alloc(&c->d_raw_seq, std::max<size_t>(raw, 1)), "cudaMalloc raw");
-        CK(dev_alloc(&c->d_raw_qual, std::max<size_t>(raw, 1)), "cudaMalloc raw");
-        CK(dev_alloc(&c->d_idx, (size_t)cap), "cudaMalloc raw");
-        c->raw_cap = cap;
-        c->raw_bytes = std::max<size_t>(raw, 1);
-    }
-    if (n > 0) {
-        CK(cudaMemcpyAsync(c->d_raw_pos, r->pos, n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_raw_len, r->len, n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_raw_hit, r->hit, n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_raw_strand, r->strand, n, cudaMemcpyHostToDevice, c->stream), "upload");
-        CK(cudaMemcpyAsync(c->d_raw_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload seq");
-        CK(cudaMemcpyAsync(c->d_raw_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload qual");
-    }
-    timer.mark("uploads issued");
-    /* 2. host: the length check and the window replay */
-    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
-    std::string err;
-    const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, host_threads(), &c->plan, &err);
-    if (rc != 0) {
-        cudaStreamSynchronize(c->stream);
-        return fail(c, rc, err);
-    }
-    timer.mark("window replay");
-    const WindowPlan& P = c->plan;
-    const int64_t nd = P.n_deposited;
+int gsnp_call_chromosome(gsnp_context* c, const gsnp_reads* r) { return call_chromosome(c, r, nullptr); }
 
-    /* window tables */
-    if (P.n_windows > c->n_win_alloc) {
-        CK(dev_alloc(&c->d_win_flags, (size_t)P.n_windows), "cudaMalloc");
-        CK(dev_alloc(&c->d_win_lik_src, (size_t)P.n_windows), "cudaMalloc");
-        CK(dev_alloc(&c->d_win_host_src, (size_t)P.n_windows), "cudaMalloc");
-        c->n_win_alloc = P.n_windows;
-    }
-    CK(cudaMemcpyAsync(c->d_win_flags, P.flags.data(), P.n_windows, cudaMemcpyHostToDevice, c->stream), "upload");
-    CK(cudaMemcpyAsync(c->d_win_lik_src, P.lik_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
-       "upload");
-    CK(cudaMemcpyAsync(c->d_win_host_src, P.host_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
-       "upload");
-    bool need_counts = false, need_lik = false;
-    for (int64_t w = 0; w < P.n_windows; ++w) {
-        need_counts |= (P.flags[w] & kWinKeepCounts) != 0;
-        need_lik |= (P.flags[w] & kWinKeepLik) != 0;
-    }
-    if (need_counts && !c->have_counts) {
-        CK(dev_alloc(&c->d_counts, (size_t)c->chr_len), "cudaMalloc counts");
-        c->have_counts = true;
-    }
-    if (need_lik && !c->have_lik_keep) {
-        CK(dev_alloc(&c->d_lik_keep, (size_t)c->chr_len * 10), "cudaMalloc likelihood");
-        c->have_lik_keep = true;
-    }
-
-    /* 3. gather the deposited alignments on the device */
-    if (nd > c->cap_dep) {
-        CK(dev_alloc(&c->d_pos, (size_t)nd), "cudaMalloc reads");
-        CK(dev_alloc(&c->d_lenhit, (size_t)nd), "cudaMalloc reads");
-        CK(dev_alloc(&c->d_len, (size_t)nd), "cudaMalloc reads");
-        CK(dev_alloc(&c->d_strand, (size_t)nd), "cudaMalloc reads");
-        CK(dev_alloc(&c->d_bq, (size_t)nd * L + 8), "cudaMalloc reads");
-        c->cap_dep = nd;
-    }
-    c->n_dep = nd;
-    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) + 2ULL * (uint64_t)n * r->pitch;
-    c->d2h_bytes = 0;
-    CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
-    if (nd > 0) {
-        /* index list of the deposited alignments, then the gather */
-        const int64_t n_chunks = (n + kDepChunk - 1) / kDepChunk;
-        if (n_chunks > c->dep_chunk_cap) {
-            CK(dev_alloc(&c->d_dep_off, (size_t)n_chunks), "cudaMalloc index");
-            c->dep_chunk_cap = n_chunks;
-        }
-        dep_count_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(n, c->d_raw_pos, c->d_raw_len,
-                                                                            c->chr_len, c->d_dep_off);
-        dep_scan_kernel<<<1, 1024, 0, c->stream>>>(c->d_dep_off, n_chunks);
-        dep_index_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(n, c->d_raw_pos, c->d_raw_len, c->chr_len,
-                                                                            c->d_dep_off, nd, c->d_idx);
-        const int64_t threads = nd * 32;
-        gather_reads_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-            nd, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-            r->pitch, L, c->d_pos, c->d_lenhit, c->d_len, c->d_strand, c->d_bq, c->d_error);
-        CK(cudaGetLastError(), "gather kernels");
-    }
-    int err2 = 0;
-    CK(cudaMemcpyAsync(&err2, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
-    CK(cudaStreamSynchronize(c->stream), "gather");
-    timer.mark("uploads and gather done");
-    if (err2 == 3) return fail(c, GSNP_ERR_STATE, "deposited alignment list does not match the window replay");
-    if (err2) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
-    const int rc2 = run_calling(c);
-    timer.mark("calling");
-    return rc2;
+int gsnp_call_chromosome_into(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
+    if (!out) return fail(c, GSNP_ERR_ARG, "null output");
+    return call_chromosome(c, r, out);
 }
 
 int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, double* pm) {
@@ -846,7 +1050,7 @@ int gsnp_rank_table(double* out) {
 int gsnp_recall_resident(gsnp_context* c) {
     if (!c || !c->have_tables || c->plan.n_windows == 0) return fail(c, GSNP_ERR_STATE, "nothing resident");
     cudaSetDevice(c->device);
-    return run_calling(c);
+    return run_calling(c, {whole_segment(c)}, nullptr, nullptr);
 }
 
 int gsnp_fetch_sites(gsnp_context* c, int64_t first, int64_t count, gsnp_site_call* out) {

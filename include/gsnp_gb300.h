@@ -135,6 +135,14 @@ int gsnp_rank_table(double* p_rank);
  * GSNP_ERR_UNSORTED, and the reference's window semantics are reproduced. */
 int gsnp_call_chromosome(gsnp_context* ctx, const gsnp_reads* reads);
 
+/* gsnp_call_chromosome followed by the download of every site's call into
+ * out (one gsnp_site_call per site of the chromosome).  The chromosome is
+ * called in window-aligned segments, so that the upload of the alignments,
+ * the calling and the download of the calls overlap; out should be pinned
+ * host memory for the downloads to overlap.  The results equal those of
+ * gsnp_call_chromosome + gsnp_fetch_sites, which remain available. */
+int gsnp_call_chromosome_into(gsnp_context* ctx, const gsnp_reads* reads, gsnp_site_call* out);
+
 /* Re-run the calling kernels on the alignments already resident on the device
  * (no host transfer); used to time the kernels alone. */
 int gsnp_recall_resident(gsnp_context* ctx);
