@@ -330,7 +330,7 @@ def main():
     stats = head["stats"]
 
     # ---- end to end through the C ABI from pinned host buffers ----
-    e2e_steps = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 3)
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 5)
     e2e_times = []
     for i in range(1 + e2e_steps):           # the first pass warms the pinned result buffer, untimed
         barrier()
@@ -341,7 +341,9 @@ def main():
         if i > 0:
             e2e_times.append(time.perf_counter() - t1)
     h2d, d2h = caller.transfer_bytes()
-    e2e_s = max_over_ranks(max(statistics.mean(e2e_times), 1e-9))
+    # median step: the host link is shared with the other GPUs of the machine,
+    # and a step that meets their traffic is reported in step_ms, not averaged in
+    e2e_s = max_over_ranks(max(statistics.median(e2e_times), 1e-9))
     e2e_value = world * sites / e2e_s
     sampler.__exit__(None, None, None)
 
@@ -385,7 +387,8 @@ def main():
                        "l2": "inputs (3 GB of alignments) exceed the 129 MB L2; no flush"},
             "bases_per_s": value * depth,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "steps": e2e_steps, "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
+                    "steps": e2e_steps, "stat": "median step",
+                    "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
             "gpu_launches": head["launches"] * args.steps,
             "kernels_ms": kernel_table(kernel_ms),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

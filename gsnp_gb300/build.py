@@ -7,7 +7,9 @@ linked with a static CUDA runtime into
                                      (include/gsnp_backend.h) for host code
                                      written against them;
   gsnp_gb300/_lib/gsnp               the command-line caller (cli.cpp) over
-                                     the C ABI.
+                                     the C ABI;
+  gsnp_gb300/_lib/gsnp_decompress    the -C decompressor command
+                                     (decompress_main.cpp) over the C ABI.
 Floating point is pinned: device code with --fmad=false (no fused
 multiply-add the source does not spell out), host code with
 -ffp-contract=off.
@@ -32,6 +34,9 @@ BACKEND_ONLY = {"compat.cu"}
 BACKEND_UNITS = {"compat.cu", "dict.cu", "tables.cpp"}
 CLI_UNIT = "cli.cpp"
 CLI = os.path.join(LIBDIR, "gsnp")
+DECOMPRESS_UNIT = "decompress_main.cpp"
+DECOMPRESS = os.path.join(LIBDIR, "gsnp_decompress")
+COMMANDS = {CLI_UNIT: CLI, DECOMPRESS_UNIT: DECOMPRESS}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -99,7 +104,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 failed.append(cmd[-3])
     if failed:
         raise RuntimeError("compilation failed: " + ", ".join(failed))
-    lib_objs = [o for o in objs if os.path.basename(o)[:-2] != CLI_UNIT]
+    lib_objs = [o for o in objs if os.path.basename(o)[:-2] not in COMMANDS]
     for lib, units in ((LIB, [o for o in lib_objs if os.path.basename(o)[:-2] not in BACKEND_ONLY]),
                        (BACKEND_LIB, [o for o in lib_objs if os.path.basename(o)[:-2] in BACKEND_UNITS])):
         if force or jobs or not os.path.exists(lib):
@@ -107,12 +112,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-    cli_obj = os.path.join(BUILD, CLI_UNIT + ".o")
-    if force or _newer(CLI, [cli_obj, LIB]):
-        cmd = ["g++", "-o", CLI, cli_obj, "-L" + LIBDIR, "-lgsnp_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    for unit, exe in COMMANDS.items():
+        obj = os.path.join(BUILD, unit + ".o")
+        if force or _newer(exe, [obj, LIB]):
+            cmd = ["g++", "-o", exe, obj, "-L" + LIBDIR, "-lgsnp_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     return LIB
 
 

@@ -47,6 +47,12 @@ int bin_slots(int bin);
 
 /* ---- device helpers ---- */
 
+/* bytes between device memory and mapped host memory (small control data) */
+__global__ void copy_bytes_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 /* The deposited alignments are those that pass the position filters
  * (0 <= pos, pos + len < chr_len), in file order, the first n_dep of them.
  * Their index list is built in chunks of kDepChunk alignments: a count per
@@ -333,6 +339,13 @@ struct gsnp_context {
     cudaStream_t up_stream = nullptr, down_stream = nullptr;
     cudaEvent_t ev_small = nullptr, ev_seg = nullptr, ev_chunk[kUploadChunks] = {};
     int* d_gerror = nullptr;       /* gather: 2 a base other than ACGT/acgt, 3 index list mismatch */
+    /* Pinned host memory mapped into the device: the small values the host
+     * reads back between launches (bin counts, deferred counts, error flags,
+     * statistics) and the window tables it sends.  A kernel moves them, so
+     * they do not queue behind the call's bulk copies on the copy engines. */
+    uint8_t* h_map = nullptr;
+    uint8_t* d_map = nullptr;
+    size_t map_bytes = 0;
     int64_t n_gathered = 0;        /* deposited reads in the packed layout so far */
     /* dictionary codec scratch (-C output) */
     void* d_dict = nullptr;
@@ -401,6 +414,39 @@ int host_threads() {
         return std::max(1, std::min(v, 64));
     }();
     return n;
+}
+
+/* layout of the mapped control area */
+constexpr size_t kMapBins = 0;       /* int[2 * kNumBins] */
+constexpr size_t kMapDcount = 64;    /* unsigned long long[2] */
+constexpr size_t kMapError = 96;     /* int */
+constexpr size_t kMapGerror = 100;   /* int */
+constexpr size_t kMapStats = 128;    /* unsigned long long[kNumStats] */
+constexpr size_t kMapWindows = 256;  /* the call's window tables */
+
+int ensure_map(gsnp_context* c, size_t bytes) {
+    if (bytes <= c->map_bytes) return GSNP_OK;
+    if (c->h_map) {
+        cudaFreeHost(c->h_map);
+        c->h_map = c->d_map = nullptr;
+        c->map_bytes = 0;
+    }
+    CK(cudaHostAlloc((void**)&c->h_map, bytes, cudaHostAllocMapped), "cudaHostAlloc");
+    CK(cudaHostGetDevicePointer((void**)&c->d_map, c->h_map, 0), "cudaHostGetDevicePointer");
+    c->map_bytes = bytes;
+    return GSNP_OK;
+}
+
+/* device bytes to the mapped area at off, and back, on the context's stream */
+cudaError_t to_map(gsnp_context* c, const void* d_src, size_t off, size_t n) {
+    copy_bytes_kernel<<<1, 128, 0, c->stream>>>((const uint8_t*)d_src, c->d_map + off, n);
+    return cudaGetLastError();
+}
+
+cudaError_t from_map(gsnp_context* c, size_t off, void* d_dst, size_t n) {
+    const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>(64, (n + 255) / 256));
+    copy_bytes_kernel<<<blocks, 256, 0, c->stream>>>(c->d_map + off, (uint8_t*)d_dst, n);
+    return cudaGetLastError();
 }
 
 void free_all(gsnp_context* c) {
@@ -490,6 +536,10 @@ struct Segment {
 int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
                 const std::function<int(size_t)>& after) {
     const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    {
+        const int rc = ensure_map(c, kMapWindows);
+        if (rc != GSNP_OK) return rc;
+    }
     if (!c->snp_lp_ready) {
         CK(dev_alloc(&c->d_snp_lp, (size_t)std::max<int64_t>(c->n_snp, 1) * 16), "cudaMalloc dbSNP priors");
         CK(dev_alloc(&c->d_snp_lp32, (size_t)std::max<int64_t>(c->n_snp, 1) * 12), "cudaMalloc dbSNP priors");
@@ -551,10 +601,9 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             if (pass == 1) k = begin(kKindClassify, 0, g.t1 - g.t0);
             CK(launch_classify(a, pass, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
             end(k);
-            CK(cudaMemcpyAsync(c->h_bin_count, c->d_bin_count, sizeof(c->h_bin_count), cudaMemcpyDeviceToHost,
-                               c->stream),
-               "bin counts");
+            CK(to_map(c, c->d_bin_count, kMapBins, sizeof(c->h_bin_count)), "bin counts");
             CK(cudaStreamSynchronize(c->stream), "classify");
+            memcpy(c->h_bin_count, c->h_map + kMapBins, sizeof(c->h_bin_count));
             bool any_fast = false;
             for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
             for (int b = 0; b < kNumBins; ++b) {
@@ -579,10 +628,9 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
                        "fast calling kernel");
                     end(k);
                 }
-                CK(cudaMemcpyAsync(c->h_dcount, c->d_dcount, sizeof(c->h_dcount), cudaMemcpyDeviceToHost,
-                                   c->stream),
-                   "deferred counts");
+                CK(to_map(c, c->d_dcount, kMapDcount, sizeof(c->h_dcount)), "deferred counts");
                 CK(cudaStreamSynchronize(c->stream), "fast calling");
+                memcpy(c->h_dcount, c->h_map + kMapDcount, sizeof(c->h_dcount));
                 const int64_t ns = (int64_t)c->h_dcount[0], nw = (int64_t)c->h_dcount[1];
                 if (ns <= c->dsite_cap && nw <= c->dpool_cap) {
                     if (ns > 0) {
@@ -610,9 +658,11 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         }
     }
     int err = 0;
-    CK(cudaMemcpyAsync(&err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
-    CK(cudaMemcpyAsync(c->stats, c->d_stats, sizeof(c->stats), cudaMemcpyDeviceToHost, c->stream), "stats");
+    CK(to_map(c, c->d_error, kMapError, sizeof(int)), "error flag");
+    CK(to_map(c, c->d_stats, kMapStats, sizeof(c->stats)), "stats");
     CK(cudaStreamSynchronize(c->stream), "calling");
+    memcpy(&err, c->h_map + kMapError, sizeof(int));
+    memcpy(c->stats, c->h_map + kMapStats, sizeof(c->stats));
     for (int k = 0; k < c->n_launches; ++k) cudaEventElapsedTime(&c->launches[k].ms, c->ev[2 * k], c->ev[2 * k + 1]);
     if (err == 1) return fail(c, GSNP_ERR_CAPACITY, "a site is covered by more than 65535 alignments");
     if (err) return fail(c, GSNP_ERR_STATE, "record slots of a tile overflowed its depth bin");
@@ -750,11 +800,23 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(dev_alloc(&c->d_win_host_src, (size_t)P.n_windows), "cudaMalloc");
         c->n_win_alloc = P.n_windows;
     }
-    CK(cudaMemcpyAsync(c->d_win_flags, P.flags.data(), P.n_windows, cudaMemcpyHostToDevice, c->stream), "upload");
-    CK(cudaMemcpyAsync(c->d_win_lik_src, P.lik_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
-       "upload");
-    CK(cudaMemcpyAsync(c->d_win_host_src, P.host_src.data(), P.n_windows * 4, cudaMemcpyHostToDevice, c->stream),
-       "upload");
+    {
+        /* through the mapped area: a copy on the copy engine would wait for
+         * the alignment uploads queued before it */
+        const size_t nw = (size_t)P.n_windows, off_f = kMapWindows, off_l = off_f + ((nw + 15) & ~(size_t)15),
+                     off_h = off_l + nw * 4;
+        const int rcm = ensure_map(c, off_h + nw * 4);
+        if (rcm != GSNP_OK) {
+            drain();
+            return rcm;
+        }
+        memcpy(c->h_map + off_f, P.flags.data(), nw);
+        memcpy(c->h_map + off_l, P.lik_src.data(), nw * 4);
+        memcpy(c->h_map + off_h, P.host_src.data(), nw * 4);
+        CK(from_map(c, off_f, c->d_win_flags, nw), "window tables");
+        CK(from_map(c, off_l, c->d_win_lik_src, nw * 4), "window tables");
+        CK(from_map(c, off_h, c->d_win_host_src, nw * 4), "window tables");
+    }
     bool need_counts = false, need_lik = false;
     for (int64_t w = 0; w < P.n_windows; ++w) {
         need_counts |= (P.flags[w] & kWinKeepCounts) != 0;
@@ -850,7 +912,9 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     CK(e_up, "upload");
     CK(e_down, "download");
     int gerr = 0;
-    CK(cudaMemcpy(&gerr, c->d_gerror, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+    CK(to_map(c, c->d_gerror, kMapGerror, sizeof(int)), "error flag");
+    CK(cudaStreamSynchronize(c->stream), "error flag");
+    memcpy(&gerr, c->h_map + kMapGerror, sizeof(int));
     if (gerr == 3) return fail(c, GSNP_ERR_STATE, "deposited alignment list does not match the window replay");
     if (gerr) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
     return GSNP_OK;
@@ -892,6 +956,7 @@ void gsnp_context_destroy(gsnp_context* c) {
     for (int i = 0; i < gsnp_context::kUploadChunks; ++i)
         if (c->ev_chunk[i]) cudaEventDestroy(c->ev_chunk[i]);
     if (c->ev_small) cudaEventDestroy(c->ev_small);
+    if (c->h_map) cudaFreeHost(c->h_map);
     if (c->ev_seg) cudaEventDestroy(c->ev_seg);
     if (c->up_stream) {
         cudaStreamSynchronize(c->up_stream);

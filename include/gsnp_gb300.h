@@ -37,7 +37,8 @@ extern "C" {
 #define GSNP_ERR_STATE 3       /* call out of order (e.g. no tables loaded) */
 #define GSNP_ERR_CAPACITY 4    /* an input exceeds a stated limit */
 #define GSNP_ERR_UNSORTED 5    /* alignments not sorted by position (the reference exits 255) */
-#define GSNP_ERR_INPUT 6       /* invalid alignment (read longer than -L, bad base) */
+#define GSNP_ERR_INPUT 6       /* invalid input (read longer than -L, bad base, unreadable file) */
+#define GSNP_ERR_MISMATCH 7    /* gsnp_check_columns found a differing row */
 
 #define GSNP_PRECISION_FP64 0        /* likelihood summed in FP64, in the reference's order */
 #define GSNP_PRECISION_FP32_FIXUP 1  /* FP32 compensated sums, FP64 recomputation near ties */
@@ -166,6 +167,20 @@ int gsnp_write_cns(gsnp_context* ctx, const char* chr_name, const char* path);
  * device.  With chr_name == NULL the files a text-mode run leaves are written
  * instead (.1_2 holding "0", the others empty). */
 int gsnp_write_columns(gsnp_context* ctx, const char* chr_name, const char* base_path);
+
+/* The cns rows of the -C files <base>.1_2 ... <base>.15_17, written to
+ * out_path exactly as the reference's decompressor prints them
+ * (cpp/decompression.cpp:130-232: its N-site literal, %#.6g doubles), decoded
+ * on `threads` host threads (<= 0: all).  Needs no context or GPU.  Returns
+ * GSNP_OK or GSNP_ERR_INPUT with the reason in err. */
+int gsnp_decompress_columns(const char* base, const char* out_path, int threads, char* err, int err_len);
+
+/* The reference decompressor's check (cpp/decompression.cpp:236-401): every
+ * row of the cns text at cns_path against the -C files at base, characters
+ * and integers exactly, the two double columns within 1e-5.  GSNP_OK when
+ * every row matches, GSNP_ERR_MISMATCH with the first difference in report,
+ * GSNP_ERR_INPUT when a file cannot be read. */
+int gsnp_check_columns(const char* cns_path, const char* base, char* report, int report_len);
 
 /* One kernel launch of the last calling pass, timed with CUDA events on the
  * context's stream. */

@@ -8,7 +8,9 @@ the reference's own host code (cpp/main.cc, call_genotype.cc, matrix.cc,
 prior.cc, rank_sum.cc, chromosome.cc, normal_dis.cc, compiled in place from
 the reference tree by `make -C oracle ref`) over the restated backend. The
 digests of the inputs and of every output file (cns text, the -C files, the
--M matrix) are recorded.  The reference tree is needed to run this script;
+-M matrix) are recorded.  For the -C cases the reference's own decompressor
+(cpp/decompression.cpp, built in place by `make -C oracle ref-decompress`)
+turns the files back into text, and that text's digest is recorded too.  The reference tree is needed to run this script;
 the tests that read golden.json are not.
 
     python tests/golden/make_golden.py [--ref /path/to/reference]
@@ -77,16 +79,23 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     args = ap.parse_args()
-    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + args.ref])
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "ref-decompress", "REF=" + args.ref])
     if r.returncode:
         sys.exit("cannot build the reference host code")
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "gsnp_ref")
+    ref_decompress = os.path.join(ROOT, "oracle", "_ref", "gsnp_ref_decompress")
     golden = {}
     for cid, name, scale, compress in CASES:
-        with tempfile.TemporaryDirectory() as d:
+        with tempfile.TemporaryDirectory(dir=HERE) as d:
             w, paths, in_digests = inputs(name, scale, d)
             flags = case_flags(w, paths, compress)
             outs = run_and_digest(ref_bin, paths, flags, os.path.join(d, "out"))
+            if compress:
+                text = os.path.join(d, "decompressed")
+                subprocess.run([ref_decompress, os.path.join(d, "out", "cns"), text], check=True,
+                               capture_output=True)
+                with open(text, "rb") as fh:
+                    outs["decompressed"] = sha(fh.read())
         golden[cid] = {"config": name, "scale": scale, "compress": compress,
                        "flags": [f if not os.path.isabs(f) else os.path.basename(f) for f in flags],
                        "inputs": in_digests, "outputs": outs}

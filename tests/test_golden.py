@@ -7,6 +7,9 @@ matrix) must have the recorded digest:
   - CPU: the restated oracle, so the oracle stays pinned to the reference on
     machines without the reference tree;
   - GPU: the `gsnp` command.
+For the -C cases the files are also decompressed with `gsnp_decompress`,
+whose text must have the digest of the reference decompressor's text
+(cpp/decompression.cpp) on the reference's files.
 """
 import hashlib
 import json
@@ -42,13 +45,19 @@ def run_case(binary, cid, tmp_path):
                         str(out / "mat")] + flags, cwd=str(out), capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     got = {f: sha_file(str(out / f)) for f in sorted(os.listdir(str(out))) if f.startswith("cns") or f == "mat"}
-    assert sorted(got) == sorted(g["outputs"])
-    bad = [f for f in got if got[f] != g["outputs"][f]]
+    files = {k: v for k, v in g["outputs"].items() if k != "decompressed"}
+    assert sorted(got) == sorted(files)
+    bad = [f for f in got if got[f] != files[f]]
     assert not bad, f"{cid}: {bad} differ from the reference's output"
+    if "decompressed" in g["outputs"]:
+        text = str(tmp_path / "decompressed")
+        r = subprocess.run([build.DECOMPRESS, str(out / "cns"), text], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        assert sha_file(text) == g["outputs"]["decompressed"], f"{cid}: decompressed text differs from the reference's"
 
 
 @pytest.mark.parametrize("cid", CPU_CASES)
-def test_oracle_matches_golden(cid, tmp_path, oracle_bin):
+def test_oracle_matches_golden(cid, tmp_path, oracle_bin, native_lib):
     run_case(oracle_bin, cid, tmp_path)
 
 
