@@ -48,8 +48,9 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 
 /* resident CTAs per SM the calling kernels are compiled for; this caps their
- * registers (28 warps of the FP32 kernel, 16 of the FP64 kernel per SM) */
-constexpr int kFastCtasPerSm = 28 * 32 / kTile;
+ * registers: 64 for the FP32 kernel (32 warps per SM, a few spilled words
+ * cost less than the latency the extra warps hide), 128 for the FP64 one */
+constexpr int kFastCtasPerSm = 32 * 32 / kTile;
 constexpr int kFp64CtasPerSm = 16 * 32 / kTile;
 
 __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v) {
@@ -96,36 +97,50 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
         }
         const int cnt = (int)((r_hi - rb) < 32 ? (r_hi - rb) : 32);
         const uint16_t* rows = a.bq + rb * L;
-        for (int k = 0; k < cnt; ++k) {
-            const int32_t start = __shfl_sync(kFull, mpos, k);
-            const uint32_t lh = __shfl_sync(kFull, mlh, k);
-            const int minus = __shfl_sync(kFull, mminus, k);
-            const int coord = (int)(site - start);
-            const int rlen = (int)(lh >> 16);
-            if (!active || coord < 0 || coord >= rlen) continue;
-            const uint32_t hit = lh & 0xffffu;
-            const uint32_t bq = __ldg(rows + k * L + coord);
-            const signed char base = (signed char)(bq & 0xff);
-            const signed char qual = (signed char)(bq >> 8);
-            depth += 1;
-            repeat += hit;
-            if (base == 'N' || qual < qmin || dep_uni >= 0xFF) continue;
-            const int sh = ((base >> 1) & 3) * 16;
-            if (hit == 1) {
-                dep_uni += 1;
-                const int q = qual - qmin;
-                const uint32_t coord_val = minus ? (uint32_t)(rlen - 1 - coord) : (uint32_t)coord;
-                const uint32_t w = make_record(base, q, coord_val, (uint32_t)minus);
-                if (num < SLOTS) {
-                    recs[num * kTile] = w;
-                    num += 1;
-                } else {
-                    overflow = true;
-                }
-                cu4 += 1u << (sh >> 1);
-                qs4 += (uint64_t)(uint32_t)q << sh;
+        /* four reads at a time: their row loads are issued together, then
+         * the covering ones are taken in order */
+        for (int k0 = 0; k0 < cnt; k0 += 4) {
+            uint32_t bqv[4], lhv[4];
+            int coordv[4], minusv[4];
+            bool covv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = k0 + u;
+                const int32_t start = __shfl_sync(kFull, mpos, k & 31);
+                lhv[u] = __shfl_sync(kFull, mlh, k & 31);
+                minusv[u] = __shfl_sync(kFull, mminus, k & 31);
+                coordv[u] = (int)(site - start);
+                covv[u] = active && k < cnt && coordv[u] >= 0 && coordv[u] < (int)(lhv[u] >> 16);
+                bqv[u] = covv[u] ? (uint32_t)__ldg(rows + k * L + coordv[u]) : 0u;
             }
-            ca4 += 1ull << sh;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (!covv[u]) continue;
+                const int coord = coordv[u], minus = minusv[u];
+                const int rlen = (int)(lhv[u] >> 16);
+                const uint32_t hit = lhv[u] & 0xffffu;
+                const signed char base = (signed char)(bqv[u] & 0xff);
+                const signed char qual = (signed char)(bqv[u] >> 8);
+                depth += 1;
+                repeat += hit;
+                if (base == 'N' || qual < qmin || dep_uni >= 0xFF) continue;
+                const int sh = ((base >> 1) & 3) * 16;
+                if (hit == 1) {
+                    dep_uni += 1;
+                    const int q = qual - qmin;
+                    const uint32_t coord_val = minus ? (uint32_t)(rlen - 1 - coord) : (uint32_t)coord;
+                    const uint32_t w = make_record(base, q, coord_val, (uint32_t)minus);
+                    if (num < SLOTS) {
+                        recs[num * kTile] = w;
+                        num += 1;
+                    } else {
+                        overflow = true;
+                    }
+                    cu4 += 1u << (sh >> 1);
+                    qs4 += (uint64_t)(uint32_t)q << sh;
+                }
+                ca4 += 1ull << sh;
+            }
         }
     }
     if (overflow) atomicExch(a.error, 2);
