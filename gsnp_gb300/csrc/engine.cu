@@ -336,7 +336,9 @@ struct gsnp_context {
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
     /* the call's copy streams: uploads in chunks, downloads per segment */
     static const int kUploadChunks = 16;
-    cudaStream_t up_stream = nullptr, down_stream = nullptr;
+    cudaStream_t up_stream = nullptr, down_stream = nullptr, gather_stream = nullptr;
+    std::vector<cudaEvent_t> ev_gather;   /* per segment: its reads are gathered */
+    cudaEvent_t ev_index = nullptr;       /* the deposited index list is built */
     cudaEvent_t ev_small = nullptr, ev_seg = nullptr, ev_chunk[kUploadChunks] = {};
     int* d_gerror = nullptr;       /* gather: 2 a base other than ACGT/acgt, 3 index list mismatch */
     /* Pinned host memory mapped into the device: the small values the host
@@ -423,6 +425,7 @@ constexpr size_t kMapError = 96;     /* int */
 constexpr size_t kMapGerror = 100;   /* int */
 constexpr size_t kMapStats = 128;    /* unsigned long long[kNumStats] */
 constexpr size_t kMapWindows = 256;  /* the call's window tables */
+static_assert(sizeof(int) * 2 * kNumBins <= kMapDcount, "bin counts overlap the deferred counts");
 
 int ensure_map(gsnp_context* c, size_t bytes) {
     if (bytes <= c->map_bytes) return GSNP_OK;
@@ -736,6 +739,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     if (!c->up_stream) {
         CK(cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaStreamCreateWithFlags(&c->down_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaStreamCreateWithFlags(&c->gather_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_index, cudaEventDisableTiming), "cudaEventCreate");
         CK(cudaEventCreateWithFlags(&c->ev_small, cudaEventDisableTiming), "cudaEventCreate");
         CK(cudaEventCreateWithFlags(&c->ev_seg, cudaEventDisableTiming), "cudaEventCreate");
         for (int i = 0; i < gsnp_context::kUploadChunks; ++i)
@@ -778,6 +783,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     timer.mark("uploads issued");
     auto drain = [&]() {
         cudaStreamSynchronize(c->up_stream);
+        if (c->gather_stream) cudaStreamSynchronize(c->gather_stream);
         cudaStreamSynchronize(c->stream);
         cudaStreamSynchronize(c->down_stream);
     };
@@ -860,8 +866,16 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(cudaGetLastError(), "index kernels");
     }
 
-    /* 4. segments: gather one segment ahead, call, download */
+    /* 4. segments: gathers on their own stream two segments ahead (segment s
+     *    is called once segment s + 1 is gathered), calls, downloads */
+    CK(cudaEventRecord(c->ev_index, c->stream), "event");
+    CK(cudaStreamWaitEvent(c->gather_stream, c->ev_index, 0), "wait");
     const std::vector<Segment> segs = plan_segments(c, v, segment_count(nd, P.n_windows));
+    while (c->ev_gather.size() < segs.size()) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        c->ev_gather.push_back(e);
+    }
     const bool vec4 = L % 4 == 0 && r->pitch % 4 == 0 && L <= r->pitch;
     const int per_row = vec4 ? L / 4 : L;
     const int rows_per_block = std::max(1, 256 / per_row);
@@ -871,26 +885,34 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
             const Segment& g = segs[(size_t)++gathered_seg];
             if (g.dhi > g.dlo) {
                 const int64_t chunk = std::min<int64_t>((g.raw_hi - 1) / chunk_rows, gsnp_context::kUploadChunks - 1);
-                CK(cudaStreamWaitEvent(c->stream, c->ev_chunk[chunk], 0), "wait");
+                CK(cudaStreamWaitEvent(c->gather_stream, c->ev_chunk[chunk], 0), "wait");
                 const int64_t rows = g.dhi - g.dlo;
                 const unsigned blocks = (unsigned)((rows + rows_per_block - 1) / rows_per_block);
                 if (vec4)
-                    gather_reads_kernel<4><<<blocks, 256, 0, c->stream>>>(
+                    gather_reads_kernel<4><<<blocks, 256, 0, c->gather_stream>>>(
                         g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
                         c->d_raw_seq, c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
                         c->d_strand, c->d_bq, c->d_gerror);
                 else
-                    gather_reads_kernel<1><<<blocks, 256, 0, c->stream>>>(
+                    gather_reads_kernel<1><<<blocks, 256, 0, c->gather_stream>>>(
                         g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
                         c->d_raw_seq, c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
                         c->d_strand, c->d_bq, c->d_gerror);
                 CK(cudaGetLastError(), "gather kernel");
             }
-            c->n_gathered = g.dhi;
+            CK(cudaEventRecord(c->ev_gather[(size_t)gathered_seg], c->gather_stream), "event");
         }
         return GSNP_OK;
     };
-    auto before = [&](size_t si) { return gather_through(std::min<int64_t>((int64_t)si + 1, (int64_t)segs.size() - 1)); };
+    auto before = [&](size_t si) -> int {
+        const int64_t last = (int64_t)segs.size() - 1;
+        const int64_t need = std::min<int64_t>((int64_t)si + 1, last);
+        const int rc = gather_through(std::min<int64_t>((int64_t)si + 2, last));
+        if (rc != GSNP_OK) return rc;
+        CK(cudaStreamWaitEvent(c->stream, c->ev_gather[(size_t)need], 0), "wait");
+        c->n_gathered = segs[(size_t)need].dhi;   /* the rows the kernels of si may read */
+        return GSNP_OK;
+    };
     auto after = [&](size_t si) -> int {
         if (!out) return GSNP_OK;
         const int64_t s0 = segs[si].t0 * kTile, s1 = std::min(segs[si].t1 * kTile, c->chr_len);
@@ -904,6 +926,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     };
     int rc2 = run_calling(c, segs, before, after);
     cudaError_t e_up = cudaStreamSynchronize(c->up_stream), e_down = cudaStreamSynchronize(c->down_stream);
+    const cudaError_t e_gather = cudaStreamSynchronize(c->gather_stream);
     timer.mark("calling (pipelined)");
     if (rc2 != GSNP_OK) {
         drain();
@@ -911,6 +934,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     }
     CK(e_up, "upload");
     CK(e_down, "download");
+    CK(e_gather, "gather");
     int gerr = 0;
     CK(to_map(c, c->d_gerror, kMapGerror, sizeof(int)), "error flag");
     CK(cudaStreamSynchronize(c->stream), "error flag");
@@ -958,6 +982,12 @@ void gsnp_context_destroy(gsnp_context* c) {
     if (c->ev_small) cudaEventDestroy(c->ev_small);
     if (c->h_map) cudaFreeHost(c->h_map);
     if (c->ev_seg) cudaEventDestroy(c->ev_seg);
+    if (c->ev_index) cudaEventDestroy(c->ev_index);
+    for (cudaEvent_t e : c->ev_gather) cudaEventDestroy(e);
+    if (c->gather_stream) {
+        cudaStreamSynchronize(c->gather_stream);
+        cudaStreamDestroy(c->gather_stream);
+    }
     if (c->up_stream) {
         cudaStreamSynchronize(c->up_stream);
         cudaStreamDestroy(c->up_stream);
