@@ -255,7 +255,7 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
 /* tile classification                                                       */
 /* ------------------------------------------------------------------------ */
 
-__constant__ int c_slots[kNumBins] = {32, 48, 64, 96, 128, 256};
+__constant__ int c_slots[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
 
 /* Read range of every tile, [lower_bound(s0 - L + 1), lower_bound(s0 + kTile)),
  * in one pass over the sorted starts: read r is the lower bound of every
@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
 /* launchers                                                                 */
 /* ------------------------------------------------------------------------ */
 
-static const int kSlots[kNumBins] = {32, 48, 64, 96, 128, 256};
+static const int kSlots[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
 
 size_t call_smem_bytes(int slots, int L) {
     /* records [slots][kTile], then the pcr bitsets [nw][kTile] */
@@ -708,10 +708,11 @@ static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles,
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream) {
     switch (bin) {
         case 0: return launch_one<32>(a, kind, tiles, count, stream);
-        case 1: return launch_one<48>(a, kind, tiles, count, stream);
-        case 2: return launch_one<64>(a, kind, tiles, count, stream);
-        case 3: return launch_one<96>(a, kind, tiles, count, stream);
-        case 4: return launch_one<128>(a, kind, tiles, count, stream);
+        case 1: return launch_one<40>(a, kind, tiles, count, stream);
+        case 2: return launch_one<48>(a, kind, tiles, count, stream);
+        case 3: return launch_one<64>(a, kind, tiles, count, stream);
+        case 4: return launch_one<96>(a, kind, tiles, count, stream);
+        case 5: return launch_one<128>(a, kind, tiles, count, stream);
         default: return launch_one<256>(a, kind, tiles, count, stream);
     }
 }

@@ -18,7 +18,9 @@ constexpr int kNumStats = 8;
  * them idle until the deepest warp finished. */
 constexpr int kTile = 32;
 constexpr int64_t kNoRead = (int64_t)1 << 40;   /* a start beyond every read */
-constexpr int kNumBins = 6;       /* record slots 32 / 48 / 64 / 96 / 128 / 256 */
+/* record-slot bins: 32 / 40 / 48 / 64 / 96 / 128 / 256.  At 32 sites per
+ * tile a 40-slot CTA (6 KB of records and pcr bits) still fits 32 per SM. */
+constexpr int kNumBins = 7;
 
 /* calling kernels */
 enum CallKind : int {
