@@ -47,6 +47,9 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+/* bins whose sites keep 4-bit pcr occurrence counts (walk_records) */
+__host__ __device__ constexpr bool kDeepBin(int slots) { return slots >= 96; }
+
 /* resident CTAs per SM the calling kernels are compiled for; this caps their
  * registers: 64 for the FP32 kernel (32 warps per SM, a few spilled words
  * cost less than the latency the extra warps hide), 128 for the FP64 one */
@@ -159,8 +162,8 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
 /* Ascending sort of one site's record column.  Up to 32 records: a bitonic
  * network in registers (the column padded with 0xFFFFFFFF, which no record
  * word equals), the same instruction stream in every lane of the warp.
- * Deeper columns: Shell sort with gaps 10, 4, 1, whose gapped passes leave
- * the final insertion pass short shifts. */
+ * Deeper columns: Shell sort with Ciura's gaps (132, 57, 23, 10, 4, 1),
+ * whose gapped passes leave the final insertion pass short shifts. */
 __device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
     if (num <= 32) {
         uint32_t v[32];
@@ -185,10 +188,11 @@ __device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
             if (i < num) recs[i * kTile] = v[i];
         return;
     }
-    const int gaps[3] = {10, 4, 1};
+    /* Ciura's gaps below the column length, each a constant of the unrolled loop */
 #pragma unroll
-    for (int gi = 0; gi < 3; ++gi) {
-        const int h = gaps[gi];
+    for (int gi = 0; gi < 6; ++gi) {
+        const int h = gi == 0 ? 132 : gi == 1 ? 57 : gi == 2 ? 23 : gi == 3 ? 10 : gi == 4 ? 4 : 1;
+        if (h >= num) continue;
         for (int i = h; i < num; ++i) {
             const uint32_t w = recs[i * kTile];
             int j = i;
@@ -474,7 +478,7 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
             for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = srcp[i];
         }
     } else {
-        likelihood_fp64(a, recs, seen, kTile, p.num, tl);
+        likelihood_fp64<kDeepBin(SLOTS)>(a, recs, seen, kTile, p.num, tl);
         if (wflags & kWinKeepLik) {
             double* dst = a.lik_keep + site * 10;
 #pragma unroll
@@ -526,7 +530,7 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
     if (active) {
         if (wflags & kWinKeepCounts) store_counts(a, site, p);
         /* adjusted quality of each record, written over its occurrence byte */
-        walk_records<true>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
+        walk_records<true, kDeepBin(SLOTS)>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
             recs[i * kTile] = (recs[i * kTile] & ~0xffu) | (uint32_t)qa;
         });
         /* FP32 sums, four records per compensated step (the grouping of
@@ -620,7 +624,7 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
     const DeferredSite d = a.dsites[i];
     const int64_t site = d.site;
     const uint32_t* recs = a.dpool + d.rec_off;
-    uint32_t seen[16];
+    uint32_t seen[64];   /* 4-bit pcr counts of 2L <= 510 keys (walk_records) */
     SitePileup p;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
@@ -635,12 +639,12 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
     double tl[16], eps[16];
 #pragma unroll
     for (int g = 0; g < 16; ++g) { tl[g] = 0.0; eps[g] = 0.0; }
-    likelihood_fp32(a, recs, seen, 1, p.num, tl, eps);
+    likelihood_fp32<true>(a, recs, seen, 1, p.num, tl, eps);
     if (d.flags & kCallSampled) {
         double t64[16];
 #pragma unroll
         for (int g = 0; g < 16; ++g) t64[g] = 0.0;
-        likelihood_fp64(a, recs, seen, 1, p.num, t64);
+        likelihood_fp64<true>(a, recs, seen, 1, p.num, t64);
         double m = 0.0;
 #pragma unroll
         for (int g = 0; g < 16; ++g) m = fmax(m, fabs(t64[g] - tl[g]));
@@ -654,7 +658,7 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
     SiteCall call;
     if (!site_posterior<true>(a, ori, p, tl, eps, lp, recs, 1, nq, &call)) {
         /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
-        likelihood_fp64(a, recs, seen, 1, p.num, tl);
+        likelihood_fp64<true>(a, recs, seen, 1, p.num, tl);
         site_posterior<true>(a, ori, p, tl, nullptr, lp, recs, 1, nq, &call);
         call.flags |= kCallFixup;
         atomicAdd(a.stats + 1, 1ull);
@@ -675,8 +679,8 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
 static const int kSlots[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
 
 size_t call_smem_bytes(int slots, int L) {
-    /* records [slots][kTile], then the pcr bitsets [nw][kTile] */
-    const size_t nw = (2 * L + 31) >> 5;
+    /* records [slots][kTile], then the pcr state [nw][kTile] */
+    const size_t nw = (size_t)pcr_words(L, kDeepBin(slots));
     return (size_t)slots * kTile * 4 + nw * kTile * 4;
 }
 

@@ -76,12 +76,27 @@ static_assert(sizeof(PackedPileup) == 32, "PackedPileup is 32 bytes");
  * earlier occurrences of the record's (strand, cycle) and gdc the distinct
  * ones; f(i, q_adj, cycle, base) is called once per occurrence.  UNIT_OCC
  * says every record's occurrence field is 1 (the tile kernels' own pileup),
- * so that f may overwrite the low byte of record i. */
-template <bool UNIT_OCC, class F>
+ * so that f may overwrite the low byte of record i.
+ *
+ * The per-site state at `seen` is one of:
+ *   a bit per (strand, cycle) key, pcr_words(L, false) words: a repeated key
+ *   counts its earlier occurrences by a scan back over the group, which is
+ *   cheap where repeats are rare;
+ *   with COUNTS, a 4-bit occurrence count per key, pcr_words(L, true) words,
+ *   for deep sites where reads starting together repeat keys often.  The
+ *   count saturates at 15; that is exact when tmax <= 16, since every tmp
+ *   of 16 or more then gives q_adj = 1.  With a larger tmax the walk falls
+ *   back to the bits and the scan. */
+__host__ __device__ __forceinline__ int pcr_words(int L, bool counts) {
+    return counts ? (2 * L + 7) >> 3 : (2 * L + 31) >> 5;
+}
+
+template <bool UNIT_OCC, bool COUNTS = false, class F>
 __device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
                                              int num, F&& f) {
     const int L = a.L;
-    const int nw = (2 * L + 31) >> 5;
+    const bool counts = COUNTS && a.tmax <= 16;
+    const int nw = pcr_words(L, counts);
     int gdc = -1, last_o = -1, gstart = 0;
     for (int i = 0; i < num; ++i) {
         const uint32_t w = recs[i * stride];
@@ -94,20 +109,29 @@ __device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* 
             gdc = -1;
             last_o = o;
         }
-        uint32_t* sw = seen + (key >> 5) * stride;
-        const uint32_t bit = 1u << (key & 31);
-        const uint32_t word = *sw;
+        const int occ = UNIT_OCC ? 1 : rec_occ(w);
         int tmp = 0;
-        if (word & bit) {
-            for (int j = gstart; j < i; ++j) {
-                const uint32_t wj = recs[j * stride];
-                if (((wj ^ w) & 0x1ff00u) == 0) tmp += UNIT_OCC ? 1 : rec_occ(wj);
-            }
+        if (counts) {
+            uint32_t* cw = seen + (key >> 3) * stride;
+            const int sh = (key & 7) * 4;
+            const uint32_t word = *cw;
+            tmp = (int)((word >> sh) & 15u);
+            const uint32_t next = (uint32_t)min(tmp + occ, 15);
+            *cw = (word & ~(15u << sh)) | (next << sh);
         } else {
-            *sw = word | bit;
+            uint32_t* sw = seen + (key >> 5) * stride;
+            const uint32_t bit = 1u << (key & 31);
+            const uint32_t word = *sw;
+            if (word & bit) {
+                for (int j = gstart; j < i; ++j) {
+                    const uint32_t wj = recs[j * stride];
+                    if (((wj ^ w) & 0x1ff00u) == 0) tmp += UNIT_OCC ? 1 : rec_occ(wj);
+                }
+            } else {
+                *sw = word | bit;
+            }
         }
         const int q = rec_q(w);
-        const int occ = UNIT_OCC ? 1 : rec_occ(w);
         for (int k = 0; k < occ; ++k) {
             if (tmp == 0) gdc += 1;
             tmp++;
@@ -120,12 +144,13 @@ __device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* 
 }
 
 /* FP64 sums in the reference's order: the plain form and the fixup */
+template <bool COUNTS = false>
 __device__ __forceinline__ void likelihood_fp64(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
                                                 int num, double* tl) {
     double s[10];
 #pragma unroll
     for (int i = 0; i < 10; ++i) s[i] = 0.0;
-    walk_records<false>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
+    walk_records<false, COUNTS>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
         const double2* row = reinterpret_cast<const double2*>(a.lik64 + ((size_t)(qa * a.L + coord) * 4 + o) * 10);
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
@@ -170,13 +195,14 @@ __device__ __forceinline__ void lik32_row(const CallArgs& a, int qa, int coord, 
     x[8] = x2.x; x[9] = x2.y;
 }
 
+template <bool COUNTS = false>
 __device__ __forceinline__ void likelihood_fp32(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
                                                 int num, double* tl, double* eps) {
     Kahan10 k;
     k.init();
     float g0[10], g1[10];
     int pos = 0;   /* position of the next term in its group of four */
-    walk_records<false>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
+    walk_records<false, COUNTS>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
         float x[10];
         lik32_row(a, qa, coord, o, x);
         switch (pos) {

@@ -108,3 +108,26 @@ def test_calibration_matrix_matches_oracle(tmp_path, oracle_bin, native_lib):
             np.testing.assert_array_equal(pm[base:base + 16], vals)
             rows += 1
     assert rows == 41 * L
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pcr", ["0.9", "0.25"])
+def test_deep_sites_pcr_dependency(pcr, tmp_path, oracle_bin, native_lib):
+    """Deep hotspots (c2) under a pcr dependency whose adjusted-quality table
+    is longer than the deep bins' 4-bit occurrence counts reach (-p 0.9: tmax
+    47, the walk falls back to the bit set and the scan) or shorter (-p 0.25:
+    tmax 5, the counts), both forms against the oracle."""
+    w = synth.make_workload("c2", scale=0.01)
+    paths = synth.write_inputs(w, str(tmp_path))
+    flags = flags_for(w, paths) + ["-p", pcr]
+    ref = oracle_outputs(oracle_bin, w, flags, str(tmp_path))
+    assert ref["rc"] == 0, ref["stderr"]
+    for prec in (api.PRECISION_FP64, api.PRECISION_FP32_FIXUP):
+        c, reads, pm = api.run_workload(w, flags, precision=prec)
+        try:
+            got = c.format_cns(w.chr_name)
+        finally:
+            c.close()
+        if got != ref["cns"]:
+            i, x, y = first_diff(got, ref["cns"])
+            pytest.fail(f"-p {pcr}, precision {prec}: first differing row {i}:\n gpu   : {x!r}\n oracle: {y!r}")
