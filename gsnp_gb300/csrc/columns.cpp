@@ -13,17 +13,24 @@
  *   <out>.11_12_13        second-base quality/count columns: common entries
  *                         dictionary coded, the rest as sparse id/value lists
  *   <out>.15_17           sparse rank-sum values and dbSNP site ids
- * The dictionary codec runs on the GPU (dict.cu); run-length encoding, 2-bit
- * packing and the sparse lists are single passes on the host.
+ * Windows are encoded independently, in memory, on every host thread, and
+ * their blocks written in window order.  Run-length encoding, 2-bit packing,
+ * the sparse lists and the dictionary codec (the contract of dict.cu, here
+ * on the host so that the threads need no device) are single passes per
+ * window.
  */
 #include "columns.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
+#include "dict.h"
 #include "rows.h"
 
 namespace gsnp {
@@ -35,17 +42,64 @@ namespace {
 
 constexpr unsigned long kDictCap = 32UL * 8192UL;   /* the reference's dictionary capacity */
 
+/* one window's blocks of the five binary files */
 struct Files {
-    FILE* f346 = nullptr;
-    FILE* frle = nullptr;
-    FILE* f10 = nullptr;
-    FILE* f111213 = nullptr;
-    FILE* f1517 = nullptr;
+    std::string f346, frle, f10, f111213, f1517;
     bool ok = true;
-    void put(FILE* f, const void* p, size_t bytes) {
-        if (bytes && fwrite(p, 1, bytes, f) != bytes) ok = false;
+    void put(std::string& f, const void* p, size_t bytes) {
+        if (bytes) f.append(static_cast<const char*>(p), bytes);
+    }
+    void clear() {
+        for (std::string* x : {&f346, &frle, &f10, &f111213, &f1517}) x->clear();
+        ok = true;
     }
 };
+
+/* dict.cu's codec on the host: dict = the distinct values ascending (-0.0
+ * and +0.0 one entry, -0.0 when any -0.0 occurs), words = each value's index
+ * packed MSB-first, floor(32 / bits) per word, the last word right-aligned */
+template <class T>
+bool host_dict(const T* in, size_t n, uint32_t* words, unsigned long* n_words, T* dict, unsigned long* n_dict,
+               std::string* err) {
+    if (*n_dict < n) {
+        *err = "*numElementDict < numElementInData";
+        return false;
+    }
+    if (n == 0) {
+        *n_dict = 0;
+        *n_words = 0;
+        return true;
+    }
+    std::vector<T> d(in, in + n);
+    std::sort(d.begin(), d.end());
+    d.erase(std::unique(d.begin(), d.end()), d.end());
+    for (T& v : d)
+        if (v == (T)0) {
+            bool neg = false;
+            for (size_t i = 0; i < n && !neg; ++i) neg = in[i] == (T)0 && std::signbit((double)in[i]);
+            v = neg ? (T)(-0.0) : (T)0;
+        }
+    const int bits = dict_bits((unsigned long)d.size());
+    const size_t per = (size_t)floor(32 / (double)bits);
+    const size_t nw = (size_t)ceil(n / (double)per);
+    if (*n_words < nw) {
+        *err = "numWordOutData < numWordCompressed";
+        return false;
+    }
+    for (size_t w = 0; w < nw; ++w) {
+        const size_t first = w * per, cnt = (w == nw - 1) ? n - first : per;
+        uint32_t out = 0;
+        for (size_t i = 0; i < cnt; ++i) {
+            const uint32_t idx = (uint32_t)(std::lower_bound(d.begin(), d.end(), in[first + i]) - d.begin());
+            out = (out << bits) | idx;
+        }
+        words[w] = out;
+    }
+    std::copy(d.begin(), d.end(), dict);
+    *n_dict = (unsigned long)d.size();
+    *n_words = (unsigned long)nw;
+    return true;
+}
 
 int base_bits(char c) {
     switch (c) {
@@ -288,33 +342,84 @@ FILE* open_file(const std::string& path, const char* mode, std::string* err) {
 
 }  // namespace
 
+bool HostDictCodec::compress(const int* in, size_t n, uint32_t* words, unsigned long* n_words, int* dict,
+                             unsigned long* n_dict, std::string* err) const {
+    return host_dict(in, n, words, n_words, dict, n_dict, err);
+}
+bool HostDictCodec::compress(const uint32_t* in, size_t n, uint32_t* words, unsigned long* n_words, uint32_t* dict,
+                             unsigned long* n_dict, std::string* err) const {
+    return host_dict(in, n, words, n_words, dict, n_dict, err);
+}
+bool HostDictCodec::compress(const double* in, size_t n, uint32_t* words, unsigned long* n_words, double* dict,
+                             unsigned long* n_dict, std::string* err) const {
+    return host_dict(in, n, words, n_words, dict, n_dict, err);
+}
+
 int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* calls, const SiteCounts* counts,
-                  const char* chr_name, const std::string& base, const DictCodec& dict, std::string* err) {
-    Files f;
-    f.f346 = open_file(base + ".3_4_6", "wb", err);
-    f.frle = open_file(base + ".5_7_8_9_14_16", "wb", err);
-    f.f10 = open_file(base + ".10", "wb", err);
-    f.f111213 = open_file(base + ".11_12_13", "wb", err);
-    f.f1517 = open_file(base + ".15_17", "wb", err);
+                  const char* chr_name, const std::string& base, const DictCodec& dict, int threads, std::string* err) {
+    const char* ext[5] = {".3_4_6", ".5_7_8_9_14_16", ".10", ".11_12_13", ".15_17"};
+    FILE* fb[5];
+    for (int i = 0; i < 5; ++i) fb[i] = open_file(base + ext[i], "wb", err);
     FILE* f12 = open_file(base + ".1_2", "w", err);
     int rc = 0;
-    if (!f.f346 || !f.frle || !f.f10 || !f.f111213 || !f.f1517 || !f12) rc = 1;
+    for (FILE* x : fb)
+        if (!x) rc = 1;
+    if (!f12) rc = 1;
     if (rc == 0 && calls) {
         fprintf(f12, "%lu\n", (unsigned long)plan.n_windows);
-        Writer wr(dict, f);
-        std::vector<CnsRow> rows;
-        for (int64_t w = 0; w < plan.n_windows && rc == 0; ++w) {
-            const int64_t len = plan.call_len[w];
-            fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1), (unsigned long)len);
-            rows.resize((size_t)len);
-            for (int64_t j = 0; j < len; ++j) rows[(size_t)j] = resolve_row(plan, w, j, codes, calls, counts);
-            if (!wr.window(rows, err)) rc = err->empty() ? (*err = "write failed", 1) : 1;
+        for (int64_t w = 0; w < plan.n_windows; ++w)
+            fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1),
+                    (unsigned long)plan.call_len[w]);
+        /* windows in batches: encoded in parallel, written in order */
+        const int nt = std::max(1, threads);
+        const size_t batch = (size_t)nt * 2;
+        std::vector<Files> out(batch);
+        std::vector<std::string> errs(batch);
+        for (int64_t w0 = 0; w0 < plan.n_windows && rc == 0; w0 += (int64_t)batch) {
+            const size_t k = (size_t)std::min<int64_t>((int64_t)batch, plan.n_windows - w0);
+            std::atomic<size_t> next(0);
+            std::atomic<bool> ok(true);
+            auto work = [&]() {
+                std::vector<CnsRow> rows;
+                for (size_t i; (i = next.fetch_add(1)) < k;) {
+                    const int64_t w = w0 + (int64_t)i;
+                    const int64_t len = plan.call_len[w];
+                    rows.resize((size_t)len);
+                    for (int64_t j = 0; j < len; ++j) rows[(size_t)j] = resolve_row(plan, w, j, codes, calls, counts);
+                    out[i].clear();
+                    Writer wr(dict, out[i]);
+                    if (!wr.window(rows, &errs[i])) ok = false;
+                }
+            };
+            std::vector<std::thread> pool;
+            for (int t = 1; t < std::min<int>(nt, (int)k); ++t) pool.emplace_back(work);
+            work();
+            for (auto& th : pool) th.join();
+            if (!ok) {
+                for (const std::string& e : errs)
+                    if (!e.empty()) {
+                        *err = e;
+                        break;
+                    }
+                if (err->empty()) *err = "write failed";
+                rc = 1;
+                break;
+            }
+            for (size_t i = 0; i < k && rc == 0; ++i) {
+                const std::string* parts[5] = {&out[i].f346, &out[i].frle, &out[i].f10, &out[i].f111213,
+                                               &out[i].f1517};
+                for (int f = 0; f < 5; ++f)
+                    if (!parts[f]->empty() && fwrite(parts[f]->data(), 1, parts[f]->size(), fb[f]) != parts[f]->size()) {
+                        *err = "write failed";
+                        rc = 1;
+                    }
+            }
         }
     } else if (rc == 0) {
         /* text mode: the column files exist and are empty, the table says 0 windows */
         fprintf(f12, "0\n");
     }
-    for (FILE* x : {f.f346, f.frle, f.f10, f.f111213, f.f1517, f12})
+    for (FILE* x : {fb[0], fb[1], fb[2], fb[3], fb[4], f12})
         if (x && fclose(x) != 0 && rc == 0) {
             *err = "write failed";
             rc = 1;

@@ -27,7 +27,6 @@
 
 #include "calling.cuh"
 #include "columns.h"
-#include "dict.h"
 #include "emit.h"
 #include "gsnp_gb300.h"
 #include "plan.h"
@@ -349,9 +348,6 @@ struct gsnp_context {
     uint8_t* d_map = nullptr;
     size_t map_bytes = 0;
     int64_t n_gathered = 0;        /* deposited reads in the packed layout so far */
-    /* dictionary codec scratch (-C output) */
-    void* d_dict = nullptr;
-    size_t dict_bytes = 0;
     /* cns text emission */
     void* d_emit = nullptr;
     size_t emit_bytes = 0;
@@ -457,7 +453,7 @@ void free_all(gsnp_context* c) {
                     c->d_p_rank, c->d_codes, c->d_snp, c->d_snp_lp, c->d_snp_lp32, c->d_pos, c->d_lenhit,
                     c->d_len, c->d_strand, c->d_bq, c->d_win_flags, c->d_win_lik_src, c->d_out, c->d_counts,
                     c->d_lik_keep, c->d_error, c->d_stats, c->d_bin_count, c->d_bin_tiles, c->d_dsites,
-                    c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_dict, c->d_win_host_src, c->d_emit,
+                    c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_win_host_src, c->d_emit,
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
                     c->d_idx, c->d_dep_off, c->d_gerror};
@@ -1187,53 +1183,6 @@ int gsnp_get_stats(gsnp_context* c, uint64_t* s, int n) {
 namespace gsnp {
 namespace {
 
-/* the dictionary codec of the -C output on the context's device */
-class GpuDict : public DictCodec {
-public:
-    explicit GpuDict(gsnp_context* c) : c_(c) {}
-    bool compress(const int* in, size_t n, uint32_t* w, unsigned long* nw, int* d, unsigned long* nd,
-                  std::string* err) const override {
-        return run(in, n, w, nw, d, nd, err);
-    }
-    bool compress(const uint32_t* in, size_t n, uint32_t* w, unsigned long* nw, uint32_t* d, unsigned long* nd,
-                  std::string* err) const override {
-        return run(in, n, w, nw, d, nd, err);
-    }
-    bool compress(const double* in, size_t n, uint32_t* w, unsigned long* nw, double* d, unsigned long* nd,
-                  std::string* err) const override {
-        return run(in, n, w, nw, d, nd, err);
-    }
-
-private:
-    gsnp_context* c_;
-    template <class T>
-    bool run(const T* in, size_t n, uint32_t* w, unsigned long* nw, T* d, unsigned long* nd, std::string* err) const {
-        const size_t in_bytes = ((n * sizeof(T) + 255) / 256) * 256;
-        const size_t need = in_bytes + dict_scratch_bytes(n);
-        if (need > c_->dict_bytes) {
-            if (c_->d_dict) cudaFree(c_->d_dict);
-            c_->d_dict = nullptr;
-            c_->dict_bytes = 0;
-            const cudaError_t e = cudaMalloc(&c_->d_dict, need);
-            if (e != cudaSuccess) {
-                *err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
-                return false;
-            }
-            c_->dict_bytes = need;
-        }
-        if (n) {
-            const cudaError_t e = cudaMemcpyAsync(c_->d_dict, in, n * sizeof(T), cudaMemcpyHostToDevice, c_->stream);
-            if (e != cudaSuccess) {
-                *err = std::string("upload: ") + cudaGetErrorString(e);
-                return false;
-            }
-        }
-        return dict_compress_device<T>(reinterpret_cast<const T*>(c_->d_dict), n,
-                                       reinterpret_cast<char*>(c_->d_dict) + in_bytes, c_->dict_bytes - in_bytes,
-                                       c_->stream, w, nw, d, nd, err) == 0;
-    }
-};
-
 int fetch_results(gsnp_context* c, std::vector<SiteCall>* calls, std::vector<SiteCounts>* counts) {
     calls->resize((size_t)c->chr_len);
     CK(cudaMemcpy(calls->data(), c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost), "fetch");
@@ -1361,11 +1310,11 @@ extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const c
     std::vector<SiteCall> calls;
     std::vector<SiteCounts> counts;
     std::string err;
-    GpuDict dict(c);
+    HostDictCodec dict;
     if (!chr_name) {
         /* text-mode companion files */
         WindowPlan none;
-        if (write_columns(none, nullptr, nullptr, nullptr, "", base_path, dict, &err) != 0)
+        if (write_columns(none, nullptr, nullptr, nullptr, "", base_path, dict, 1, &err) != 0)
             return fail(c, GSNP_ERR_INPUT, err);
         return GSNP_OK;
     }
@@ -1373,7 +1322,7 @@ extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const c
     const int rc = fetch_results(c, &calls, &counts);
     if (rc != GSNP_OK) return rc;
     if (write_columns(c->plan, c->h_codes.data(), calls.data(), c->have_counts ? counts.data() : nullptr, chr_name,
-                      base_path, dict, &err) != 0)
+                      base_path, dict, host_threads(), &err) != 0)
         return fail(c, GSNP_ERR_INPUT, err);
     return GSNP_OK;
 }
