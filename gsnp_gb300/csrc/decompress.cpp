@@ -22,6 +22,7 @@
 #include "decompress.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cstdlib>
 #include <cmath>
@@ -52,13 +53,38 @@ struct WindowCols {
     }
 };
 
+/* a read position in one file's bytes; a short read is an error */
+struct Cursor {
+    const char* p = nullptr;
+    const char* end = nullptr;
+    std::string* err = nullptr;
+    template <class T>
+    bool get(T* out, size_t count, const char* what) {
+        const size_t bytes = count * sizeof(T);
+        if (count && (size_t)(end - p) < bytes) {
+            if (err->empty()) *err = std::string("truncated ") + what;
+            return false;
+        }
+        if (bytes) memcpy(out, p, bytes);
+        p += bytes;
+        return true;
+    }
+    bool skip(size_t bytes, const char* what) {
+        if ((size_t)(end - p) < bytes) {
+            if (err->empty()) *err = std::string("truncated ") + what;
+            return false;
+        }
+        p += bytes;
+        return true;
+    }
+};
+
+/* The -C files in memory and every window's block offsets in them, found by
+ * one pass over the block headers; windows then decode independently, on
+ * any thread. */
 class Reader {
 public:
     explicit Reader(std::string* err) : err_(err) {}
-    ~Reader() {
-        for (FILE* f : {f346_, frle_, f10_, f111213_, f1517_})
-            if (f) fclose(f);
-    }
 
     bool open(const std::string& base) {
         FILE* f12 = fopen((base + ".1_2").c_str(), "r");
@@ -73,28 +99,35 @@ public:
         }
         fclose(f12);
         if (!ok) return fail("malformed " + base + ".1_2");
-        struct {
-            FILE** f;
-            const char* ext;
-        } files[] = {{&f346_, ".3_4_6"}, {&frle_, ".5_7_8_9_14_16"}, {&f10_, ".10"},
-                     {&f111213_, ".11_12_13"}, {&f1517_, ".15_17"}};
-        for (auto& x : files) {
-            *x.f = fopen((base + x.ext).c_str(), "rb");
-            if (!*x.f) return fail(std::string("cannot open ") + base + x.ext);
+        static const char* ext[5] = {".3_4_6", ".5_7_8_9_14_16", ".10", ".11_12_13", ".15_17"};
+        for (int i = 0; i < 5; ++i) {
+            FILE* f = fopen((base + ext[i]).c_str(), "rb");
+            if (!f) return fail(std::string("cannot open ") + base + ext[i]);
+            char buf[1 << 16];
+            size_t got;
+            while ((got = fread(buf, 1, sizeof(buf), f)) > 0) data_[i].insert(data_[i].end(), buf, buf + got);
+            fclose(f);
         }
-        return true;
+        return index();
     }
 
     size_t n_windows() const { return windows_.size(); }
 
-    /* the next window's blocks, decoded */
-    bool read(size_t w, WindowCols* out) {
+    /* window w's blocks, decoded; safe to call for different windows at once */
+    bool read(size_t w, WindowCols* out, std::string* err) const {
         const Win& win = windows_[w];
         out->chr = win.chr;
         out->start = win.start;
         out->n = win.len;
         out->resize((size_t)win.len);
-        return read_346(out) && read_rle(out) && read_10(out) && read_111213(out) && read_1517(out);
+        Cursor c[5];
+        for (int i = 0; i < 5; ++i) {
+            c[i].p = data_[i].data() + offs_[w][i];
+            c[i].end = data_[i].data() + data_[i].size();
+            c[i].err = err;
+        }
+        return read_346(c[0], out) && read_rle(c[1], out) && read_10(c[2], out) && read_111213(c[3], out) &&
+               read_1517(c[4], out);
     }
 
 private:
@@ -103,17 +136,61 @@ private:
         uint64_t start, len;
     };
     std::vector<Win> windows_;
-    FILE *f346_ = nullptr, *frle_ = nullptr, *f10_ = nullptr, *f111213_ = nullptr, *f1517_ = nullptr;
+    std::vector<char> data_[5];
+    std::vector<std::array<size_t, 5>> offs_;
     std::string* err_;
 
     bool fail(const std::string& m) {
         if (err_->empty()) *err_ = m;
         return false;
     }
+    static bool bad(std::string* err, const std::string& m) {
+        if (err->empty()) *err = m;
+        return false;
+    }
 
-    template <class T>
-    bool get(FILE* f, T* p, size_t count, const char* what) {
-        if (count && fread(p, sizeof(T), count, f) != count) return fail(std::string("truncated ") + what);
+    /* each window's block offsets: headers read, payloads skipped */
+    bool index() {
+        Cursor c[5];
+        for (int i = 0; i < 5; ++i) {
+            c[i].p = data_[i].data();
+            c[i].end = data_[i].data() + data_[i].size();
+            c[i].err = err_;
+        }
+        for (size_t w = 0; w < windows_.size(); ++w) {
+            std::array<size_t, 5> o;
+            for (int i = 0; i < 5; ++i) o[i] = (size_t)(c[i].p - data_[i].data());
+            offs_.push_back(o);
+            unsigned long p7[7];
+            if (!c[0].get(p7, 7, ".3_4_6") || (p7[0] != 1 && !c[0].skip(p7[1], ".3_4_6"))) return false;
+            int flag = 0;
+            if (!c[1].get(&flag, 1, ".5_7_8_9_14_16")) return false;
+            for (int k = 0; flag != 1 && k < 6; ++k) {
+                unsigned long p6[6];
+                if (!c[1].get(p6, 6, ".5_7_8_9_14_16") || !c[1].skip(p6[5], ".5_7_8_9_14_16")) return false;
+            }
+            if (!c[2].get(&flag, 1, ".10")) return false;
+            if (flag != 1) {
+                unsigned long p3[3];
+                if (!c[2].get(p3, 3, ".10") || !c[2].skip(4 * (p3[1] + p3[0]), ".10")) return false;
+            }
+            if (!c[3].get(&flag, 1, ".11_12_13")) return false;
+            if (flag != 1) {
+                unsigned long p4[4];
+                if (!c[3].get(p4, 4, ".11_12_13") || !c[3].skip(4 * (2 * p4[2] + 2 * p4[3] + p4[1]), ".11_12_13"))
+                    return false;
+                for (int k = 0; k < 3; ++k) {
+                    unsigned long dp[2];
+                    if (!c[3].get(dp, 2, ".11_12_13") || !c[3].skip(4 * (dp[0] + dp[1]), ".11_12_13")) return false;
+                }
+            }
+            if (!c[4].get(&flag, 1, ".15_17")) return false;
+            if (flag != 1) {
+                int n = 0;
+                if (!c[4].get(&n, 1, ".15_17") || n < 0 || !c[4].skip(12 * (size_t)n, ".15_17")) return false;
+                if (!c[4].get(&n, 1, ".15_17") || n < 0 || !c[4].skip(4 * (size_t)n, ".15_17")) return false;
+            }
+        }
         return true;
     }
 
@@ -137,7 +214,8 @@ private:
 
     /* MSB-first packed dictionary indices, the last word right-aligned */
     template <class T>
-    bool undict(const std::vector<uint32_t>& words, const std::vector<T>& dict, size_t n, T* out) {
+    static bool undict(const std::vector<uint32_t>& words, const std::vector<T>& dict, size_t n, T* out,
+                       std::string* err) {
         if (words.empty() || n == 0) return true;
         const int bits = index_bits(dict.size());
         const size_t per = (size_t)(32 / bits);
@@ -148,18 +226,18 @@ private:
             const size_t k = (w == words.size() - 1) ? n - first : std::min(per, n - first);
             for (size_t i = 0; i < k; ++i) {
                 const uint32_t idx = (words[w] >> (bits * (k - 1 - i))) & mask;
-                if (idx >= dict.size()) return fail("dictionary index out of range");
+                if (idx >= dict.size()) return bad(err, "dictionary index out of range");
                 out[first + i] = dict[idx];
             }
         }
         return true;
     }
 
-    bool read_346(WindowCols* o) {
+    static bool read_346(Cursor& f, WindowCols* o) {
         unsigned long p[7];
-        if (!get(f346_, p, 7, ".3_4_6")) return false;
+        if (!f.get(p, 7, ".3_4_6")) return false;
         const size_t n = p[2];
-        if (n > o->n) return fail(".3_4_6 block longer than its window");
+        if (n > o->n) return bad(f.err, ".3_4_6 block longer than its window");
         if (p[0] == 1) {
             std::fill(o->c3.begin(), o->c3.begin() + n, 'N');
             std::fill(o->c4.begin(), o->c4.begin() + n, 'N');
@@ -169,140 +247,140 @@ private:
         std::vector<int> id4(p[5]), id6(p[6]), idn(p[4]);
         std::vector<char> v4(p[5]), v6(p[6]);
         std::vector<uint32_t> code(p[3]);
-        if (!(get(f346_, id4.data(), id4.size(), ".3_4_6") && get(f346_, v4.data(), v4.size(), ".3_4_6") &&
-              get(f346_, id6.data(), id6.size(), ".3_4_6") && get(f346_, v6.data(), v6.size(), ".3_4_6") &&
-              get(f346_, idn.data(), idn.size(), ".3_4_6") && get(f346_, code.data(), code.size(), ".3_4_6")))
+        if (!(f.get(id4.data(), id4.size(), ".3_4_6") && f.get(v4.data(), v4.size(), ".3_4_6") &&
+              f.get(id6.data(), id6.size(), ".3_4_6") && f.get(v6.data(), v6.size(), ".3_4_6") &&
+              f.get(idn.data(), idn.size(), ".3_4_6") && f.get(code.data(), code.size(), ".3_4_6")))
             return false;
         unpack2(code, n, o->c3.data());
         for (int i : idn) {
-            if (i < 0 || (size_t)i >= n) return fail("N id out of range");
+            if (i < 0 || (size_t)i >= n) return bad(f.err, "N id out of range");
             o->c3[(size_t)i] = 'N';
         }
         std::copy(o->c3.begin(), o->c3.begin() + n, o->c4.begin());
         std::copy(o->c3.begin(), o->c3.begin() + n, o->c6.begin());
         for (size_t i = 0; i < id4.size(); ++i) {
-            if (id4[i] < 0 || (size_t)id4[i] >= n) return fail("column 4 id out of range");
+            if (id4[i] < 0 || (size_t)id4[i] >= n) return bad(f.err, "column 4 id out of range");
             o->c4[(size_t)id4[i]] = v4[i];
         }
         for (size_t i = 0; i < id6.size(); ++i) {
-            if (id6[i] < 0 || (size_t)id6[i] >= n) return fail("column 6 id out of range");
+            if (id6[i] < 0 || (size_t)id6[i] >= n) return bad(f.err, "column 6 id out of range");
             o->c6[(size_t)id6[i]] = v6[i];
         }
         return true;
     }
 
     template <class T>
-    bool rle_column(T* out, size_t n) {
+    static bool rle_column(Cursor& f, T* out, size_t n) {
         unsigned long p[6];
-        if (!get(frle_, p, 6, ".5_7_8_9_14_16")) return false;
+        if (!f.get(p, 6, ".5_7_8_9_14_16")) return false;
         const size_t runs = p[0];
         std::vector<uint32_t> cv(p[1]), cl(p[2]), dl(p[4]);
         std::vector<T> dv(p[3]);
-        if (!(get(frle_, cv.data(), cv.size(), ".5_7_8_9_14_16") && get(frle_, cl.data(), cl.size(), ".5_7_8_9_14_16") &&
-              get(frle_, dv.data(), dv.size(), ".5_7_8_9_14_16") && get(frle_, dl.data(), dl.size(), ".5_7_8_9_14_16")))
+        if (!(f.get(cv.data(), cv.size(), ".5_7_8_9_14_16") && f.get(cl.data(), cl.size(), ".5_7_8_9_14_16") &&
+              f.get(dv.data(), dv.size(), ".5_7_8_9_14_16") && f.get(dl.data(), dl.size(), ".5_7_8_9_14_16")))
             return false;
         std::vector<T> val(runs);
         std::vector<uint32_t> len(runs);
-        if (!undict(cv, dv, runs, val.data()) || !undict(cl, dl, runs, len.data())) return false;
+        if (!undict(cv, dv, runs, val.data(), f.err) || !undict(cl, dl, runs, len.data(), f.err)) return false;
         size_t at = 0;
         for (size_t r = 0; r < runs; ++r) {
-            if (at + len[r] > n) return fail("run lengths exceed the window");
+            if (at + len[r] > n) return bad(f.err, "run lengths exceed the window");
             std::fill(out + at, out + at + len[r], val[r]);
             at += len[r];
         }
         return true;
     }
 
-    bool read_rle(WindowCols* o) {
+    static bool read_rle(Cursor& f, WindowCols* o) {
         int flag = 0;
-        if (!get(frle_, &flag, 1, ".5_7_8_9_14_16")) return false;
+        if (!f.get(&flag, 1, ".5_7_8_9_14_16")) return false;
         if (flag == 1) return true;   /* zeros and 255.0, as resize left them */
         const size_t n = o->n;
-        return rle_column(o->c5.data(), n) && rle_column(o->c7.data(), n) && rle_column(o->c8.data(), n) &&
-               rle_column(o->c9.data(), n) && rle_column(o->c14.data(), n) && rle_column(o->c16.data(), n);
+        return rle_column(f, o->c5.data(), n) && rle_column(f, o->c7.data(), n) && rle_column(f, o->c8.data(), n) &&
+               rle_column(f, o->c9.data(), n) && rle_column(f, o->c14.data(), n) && rle_column(f, o->c16.data(), n);
     }
 
-    bool read_10(WindowCols* o) {
+    static bool read_10(Cursor& f, WindowCols* o) {
         int flag = 0;
-        if (!get(f10_, &flag, 1, ".10")) return false;
+        if (!f.get(&flag, 1, ".10")) return false;
         if (flag == 1) {
             std::fill(o->c10.begin(), o->c10.end(), 'N');
             return true;
         }
         unsigned long p[3];
-        if (!get(f10_, p, 3, ".10")) return false;
-        if (p[2] != o->n) return fail(".10 block length differs from its window");
+        if (!f.get(p, 3, ".10")) return false;
+        if (p[2] != o->n) return bad(f.err, ".10 block length differs from its window");
         std::vector<uint32_t> code(p[1]), nid(p[0]);
-        if (!get(f10_, code.data(), code.size(), ".10") || !get(f10_, nid.data(), nid.size(), ".10")) return false;
+        if (!f.get(code.data(), code.size(), ".10") || !f.get(nid.data(), nid.size(), ".10")) return false;
         unpack2(code, o->n, o->c10.data());
         for (uint32_t i : nid) {
-            if (i >= o->n) return fail("column 10 N id out of range");
+            if (i >= o->n) return bad(f.err, "column 10 N id out of range");
             o->c10[i] = 'N';
         }
         return true;
     }
 
-    bool read_111213(WindowCols* o) {
+    static bool read_111213(Cursor& f, WindowCols* o) {
         int flag = 0;
-        if (!get(f111213_, &flag, 1, ".11_12_13")) return false;
+        if (!f.get(&flag, 1, ".11_12_13")) return false;
         if (flag == 1) return true;
         unsigned long p[4];
-        if (!get(f111213_, p, 4, ".11_12_13")) return false;
-        if (p[0] != o->n) return fail(".11_12_13 block length differs from its window");
+        if (!f.get(p, 4, ".11_12_13")) return false;
+        if (p[0] != o->n) return bad(f.err, ".11_12_13 block length differs from its window");
         std::vector<int> e12id(p[2]), e12(p[2]), e13id(p[3]), e13(p[3]), cid(p[1]);
-        if (!(get(f111213_, e12id.data(), e12id.size(), ".11_12_13") && get(f111213_, e12.data(), e12.size(), ".11_12_13") &&
-              get(f111213_, e13id.data(), e13id.size(), ".11_12_13") && get(f111213_, e13.data(), e13.size(), ".11_12_13") &&
-              get(f111213_, cid.data(), cid.size(), ".11_12_13")))
+        if (!(f.get(e12id.data(), e12id.size(), ".11_12_13") && f.get(e12.data(), e12.size(), ".11_12_13") &&
+              f.get(e13id.data(), e13id.size(), ".11_12_13") && f.get(e13.data(), e13.size(), ".11_12_13") &&
+              f.get(cid.data(), cid.size(), ".11_12_13")))
             return false;
         std::vector<int> vals[3];
         for (auto& v : vals) {
             unsigned long dp[2];
-            if (!get(f111213_, dp, 2, ".11_12_13")) return false;
+            if (!f.get(dp, 2, ".11_12_13")) return false;
             std::vector<uint32_t> words(dp[0]);
             std::vector<int> dict(dp[1]);
-            if (!get(f111213_, words.data(), words.size(), ".11_12_13") ||
-                !get(f111213_, dict.data(), dict.size(), ".11_12_13"))
+            if (!f.get(words.data(), words.size(), ".11_12_13") ||
+                !f.get(dict.data(), dict.size(), ".11_12_13"))
                 return false;
             v.assign(cid.size(), 0);
-            if (!undict(words, dict, cid.size(), v.data())) return false;
+            if (!undict(words, dict, cid.size(), v.data(), f.err)) return false;
         }
         const size_t n = o->n;
         for (size_t i = 0; i < cid.size(); ++i) {
-            if (cid[i] < 0 || (size_t)cid[i] >= n) return fail("column 11 id out of range");
+            if (cid[i] < 0 || (size_t)cid[i] >= n) return bad(f.err, "column 11 id out of range");
             o->c11[(size_t)cid[i]] = vals[0][i];
             o->c12[(size_t)cid[i]] = vals[1][i];
             o->c13[(size_t)cid[i]] = vals[2][i];
         }
         for (size_t i = 0; i < e12id.size(); ++i) {
-            if (e12id[i] < 0 || (size_t)e12id[i] >= n) return fail("column 12 id out of range");
+            if (e12id[i] < 0 || (size_t)e12id[i] >= n) return bad(f.err, "column 12 id out of range");
             o->c12[(size_t)e12id[i]] = e12[i];
         }
         for (size_t i = 0; i < e13id.size(); ++i) {
-            if (e13id[i] < 0 || (size_t)e13id[i] >= n) return fail("column 13 id out of range");
+            if (e13id[i] < 0 || (size_t)e13id[i] >= n) return bad(f.err, "column 13 id out of range");
             o->c13[(size_t)e13id[i]] = e13[i];
         }
         return true;
     }
 
-    bool read_1517(WindowCols* o) {
+    static bool read_1517(Cursor& f, WindowCols* o) {
         int flag = 0;
-        if (!get(f1517_, &flag, 1, ".15_17")) return false;
+        if (!f.get(&flag, 1, ".15_17")) return false;
         if (flag == 1) return true;
         int cnt = 0;
-        if (!get(f1517_, &cnt, 1, ".15_17") || cnt < 0) return fail("truncated .15_17");
+        if (!f.get(&cnt, 1, ".15_17") || cnt < 0) return bad(f.err, "truncated .15_17");
         std::vector<int> id((size_t)cnt);
         std::vector<double> val((size_t)cnt);
-        if (!get(f1517_, id.data(), id.size(), ".15_17") || !get(f1517_, val.data(), val.size(), ".15_17"))
+        if (!f.get(id.data(), id.size(), ".15_17") || !f.get(val.data(), val.size(), ".15_17"))
             return false;
         for (size_t i = 0; i < id.size(); ++i) {
-            if (id[i] < 0 || (uint64_t)id[i] >= o->n) return fail("column 15 id out of range");
+            if (id[i] < 0 || (uint64_t)id[i] >= o->n) return bad(f.err, "column 15 id out of range");
             o->c15[(size_t)id[i]] = val[i];
         }
-        if (!get(f1517_, &cnt, 1, ".15_17") || cnt < 0) return fail("truncated .15_17");
+        if (!f.get(&cnt, 1, ".15_17") || cnt < 0) return bad(f.err, "truncated .15_17");
         id.assign((size_t)cnt, 0);
-        if (!get(f1517_, id.data(), id.size(), ".15_17")) return false;
+        if (!f.get(id.data(), id.size(), ".15_17")) return false;
         for (int i : id) {
-            if (i < 0 || (uint64_t)i >= o->n) return fail("column 17 id out of range");
+            if (i < 0 || (uint64_t)i >= o->n) return bad(f.err, "column 17 id out of range");
             o->c17[(size_t)i] = 1;
         }
         return true;
@@ -404,19 +482,31 @@ int decompress_columns(const std::string& base, const std::string& out_path, int
     const size_t batch = text.size();
     const size_t nw = rd.n_windows();
     std::vector<WindowCols> cols(batch);
+    std::vector<std::string> errs(batch);
     for (size_t w0 = 0; w0 < nw && ok; w0 += batch) {
         const size_t k = std::min(batch, nw - w0);
-        for (size_t i = 0; i < k && ok; ++i) ok = rd.read(w0 + i, &cols[i]);
-        if (!ok) break;
         std::atomic<size_t> next(0);
+        std::atomic<bool> good(true);
         auto work = [&]() {
-            for (size_t i; (i = next.fetch_add(1)) < k;) format_window(cols[i], &text[i]);
+            for (size_t i; (i = next.fetch_add(1)) < k;) {
+                if (!rd.read(w0 + i, &cols[i], &errs[i])) {
+                    good = false;
+                    continue;
+                }
+                format_window(cols[i], &text[i]);
+            }
         };
         const int nt = (int)std::min<size_t>(k, (size_t)threads);
         std::vector<std::thread> pool;
         for (int t = 1; t < nt; ++t) pool.emplace_back(work);
         work();
         for (auto& th : pool) th.join();
+        if (!good) {
+            for (const std::string& e : errs)
+                if (!e.empty() && err->empty()) *err = e;
+            ok = false;
+            break;
+        }
         for (size_t i = 0; i < k && ok; ++i)
             ok = fwrite(text[i].data(), 1, text[i].size(), out) == text[i].size();
     }
@@ -478,7 +568,7 @@ int check_columns(const std::string& cns_path, const std::string& base, std::str
     size_t row = 0;
     WindowCols w;
     for (size_t wi = 0; wi < rd.n_windows(); ++wi) {
-        if (!rd.read(wi, &w)) return 1;
+        if (!rd.read(wi, &w, err)) return 1;
         for (uint64_t i = 0; i < w.n; ++i, ++row) {
             if (row >= nrows) {
                 *report = "the cns text has fewer rows than the compressed files";
