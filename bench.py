@@ -347,6 +347,17 @@ def main():
     e2e_value = world * sites / e2e_s
     sampler.__exit__(None, None, None)
 
+    # ---- the cns text of the last call (what the reference's pass writes), informational ----
+    text_ms = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        rc = caller.lib.gsnp_write_cns(caller.ctx, w.chr_name.encode(), os.devnull.encode())
+        text_ms.append((time.perf_counter() - t1) * 1e3)
+        if rc != 0:
+            text_ms = []
+            break
+
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
     bsite = site_bytes(w)
@@ -380,7 +391,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if precision == api.PRECISION_FP64 else "f32+f64",
-            "data": "synthetic (seeded generator of the c1 shape, generated on the GPU in %.1f s)" % t_gen,
+            "data": "synthetic (seeded generator of the %s shape, generated on the GPU in %.1f s)" % (args.workload, t_gen),
             "config": {"workload": WORKLOADS[args.workload] + "; scale %.3g" % args.scale,
                        "sites": sites, "reads": w.num_reads, "bases": w.num_bases, "mean_depth": depth,
                        "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
@@ -389,6 +400,9 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps, "stat": "median step",
                     "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
+            "cns_text": ({"ms": round(min(text_ms), 2), "rows": sites,
+                          "note": "gsnp_write_cns of the last call to the null device: GPU formatting, download, write"}
+                         if text_ms else None),
             "gpu_launches": head["launches"] * args.steps,
             "kernels_ms": kernel_table(kernel_ms),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -247,6 +247,51 @@ __global__ void calib_count_kernel(int64_t n, const int32_t* __restrict__ pos, c
     }
 }
 
+/* The same histogram with the matching bins (observed base = reference base,
+ * about 99% of the counts) in shared memory: [q - qmin][base][cycle] 32-bit
+ * counters, consecutive cycles in consecutive banks, so a warp's 32 lanes
+ * (32 cycles of one read) add without conflict.  Mismatches go straight to
+ * the global bins.  Each CTA walks reads with a grid stride and adds its
+ * shared counts to the global ones once at the end. */
+__global__ void __launch_bounds__(512) calib_count_smem_kernel(
+    int64_t n, const int32_t* __restrict__ pos, const int32_t* __restrict__ len, const int32_t* __restrict__ hit,
+    const uint8_t* __restrict__ strand, const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual, int pitch,
+    const uint8_t* __restrict__ codes, int64_t chr_len, int qmin, int qmax, int L,
+    unsigned long long* __restrict__ counts) {
+    extern __shared__ uint32_t diag[];
+    const int nq = qmax - qmin + 1;
+    const int nbins = nq * 4 * L;
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) diag[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const int64_t p = pos[r];
+        const int rl = len[r];
+        if (p < 0 || p + rl >= chr_len || hit[r] != 1) continue;
+        const bool minus = strand[r] != '+';
+        for (int c = lane; c < rl; c += 32) {
+            const signed char b = (signed char)seq[r * pitch + c];
+            const signed char qc = (signed char)qual[r * pitch + c];
+            const int ref = codes[p + c];
+            const int cyc = minus ? rl - 1 - c : c;
+            if (b == 'N' || (ref & 12) != 0 || qc < qmin || qc > qmax || cyc >= L) continue;
+            const int obs = (b >> 1) & 3;
+            if (obs == (ref & 3))
+                atomicAdd(diag + ((qc - qmin) * 4 + obs) * L + cyc, 1u);
+            else
+                atomicAdd(counts + ((((qc - qmin) * L + cyc) << 4) | ((ref & 3) << 2) | obs), 1ull);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) {
+        const uint32_t v = diag[i];
+        if (!v) continue;
+        const int cyc = i % L, qb = i / L, base = qb & 3, q = qb >> 2;
+        atomicAdd(counts + (((q * L + cyc) << 4) | (base << 2) | base), (unsigned long long)v);
+    }
+}
+
 }  // namespace gsnp
 
 using namespace gsnp;
@@ -1111,10 +1156,28 @@ int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, d
     CK(cudaMemcpyAsync(d_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload");
     CK(cudaMemcpyAsync(d_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload");
     if (r->n > 0) {
-        const int64_t threads = r->n * 32;
-        calib_count_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-            r->n, d_pos, d_len, d_hit, d_strand, d_seq, d_qual, r->pitch, c->d_codes, c->chr_len,
-            (int)(signed char)p->q_min, (int)(signed char)p->q_max, L, d_counts);
+        /* the matching bins in shared memory when they fit (41 qualities x
+         * 4 bases x 100 cycles: 64 KB), else every bin in global memory */
+        const size_t smem = (size_t)nq * 4 * L * 4;
+        int dev_smem = 0, n_sm = 0;
+        cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, c->device);
+        if (smem <= 160 * 1024 && smem <= (size_t)dev_smem) {
+            CK(cudaFuncSetAttribute(calib_count_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "calibration kernel attribute");
+            const int per_sm = std::max(1, (int)(200 * 1024 / std::max<size_t>(smem, 1)));
+            const int64_t want = (r->n + 15) / 16;
+            const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)n_sm * per_sm, want));
+            calib_count_smem_kernel<<<blocks, 512, smem, c->stream>>>(
+                r->n, d_pos, d_len, d_hit, d_strand, d_seq, d_qual, r->pitch, c->d_codes, c->chr_len,
+                (int)(signed char)p->q_min, (int)(signed char)p->q_max, L, d_counts);
+        } else {
+            const int64_t threads = r->n * 32;
+            calib_count_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+                r->n, d_pos, d_len, d_hit, d_strand, d_seq, d_qual, r->pitch, c->d_codes, c->chr_len,
+                (int)(signed char)p->q_min, (int)(signed char)p->q_max, L, d_counts);
+        }
+        CK(cudaGetLastError(), "calibration kernel");
     }
     std::vector<unsigned long long> counts(nbins);
     CK(cudaMemcpyAsync(counts.data(), d_counts, nbins * 8, cudaMemcpyDeviceToHost, c->stream), "download");
