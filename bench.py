@@ -149,6 +149,18 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+# DRAM traffic per site of the dominant calling kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum of one ncu capture of that kernel on a 10%-scale case
+# of the workload, divided by the sites of the captured launch).  The traffic
+# of a full-size launch is that figure times its sites: a launch reads its
+# tiles' reads once and writes one call per site, so traffic grows with the
+# sites.  Keyed by (workload, kernel kind, record slots); other kernels report
+# no traffic.
+NCU_BYTES_PER_SITE = {
+    ("c1", 2, 40): 150.2,   # call_fast_kernel<40>: 252.9 MB read + 70.8 MB written over 2,154,656 sites
+}
+
+
 def site_bytes(w):
     """Algorithmic bytes of one called site."""
     sites = w.genome_len
@@ -406,7 +418,9 @@ def main():
             "gpu_launches": head["launches"] * args.steps,
             "kernels_ms": kernel_table(kernel_ms),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": (round(NCU_BYTES_PER_SITE[(args.workload,) + dom_key] * dom_sites)
+                                     if (args.workload,) + dom_key in NCU_BYTES_PER_SITE else None),
                          "kernel": "%s<%d>" % (names[dom_key[0]], dom_key[1]), "sites_per_launch": dom_sites,
                          "bytes_per_site": bsite, "peak_source": peak_kind},
             "cpu_baseline": cpu,

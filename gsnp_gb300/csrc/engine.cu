@@ -424,6 +424,32 @@ struct PhaseTimer {
     }
 };
 
+/* GPU timestamps of a call's stages on its streams, printed with the phase
+ * times when GSNP_TIMING is set */
+struct GpuTimeline {
+    bool on;
+    std::vector<std::pair<std::string, cudaEvent_t>> ev;
+    explicit GpuTimeline(bool enabled) : on(enabled) {}
+    ~GpuTimeline() {
+        for (auto& e : ev) cudaEventDestroy(e.second);
+    }
+    void rec(const std::string& name, cudaStream_t s) {
+        if (!on) return;
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, s);
+        ev.emplace_back(name, e);
+    }
+    void print(const char* what) {
+        if (!on || ev.empty()) return;
+        for (auto& e : ev) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev[0].second, e.second) == cudaSuccess)
+                fprintf(stderr, "%s: gpu %-24s %8.2f ms\n", what, e.first.c_str(), ms);
+        }
+    }
+};
+
 int fail(gsnp_context* c, int code, const std::string& msg) {
     if (c) c->error = msg;
     return code;
@@ -803,6 +829,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         c->raw_bytes = std::max<size_t>(raw, 1);
     }
     const int64_t chunk_rows = std::max<int64_t>(1, (n + gsnp_context::kUploadChunks - 1) / gsnp_context::kUploadChunks);
+    GpuTimeline tl(timer.on);
+    tl.rec("start", c->up_stream);
     if (n > 0) {
         CK(cudaMemcpyAsync(c->d_raw_pos, r->pos, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
         CK(cudaMemcpyAsync(c->d_raw_len, r->len, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
@@ -820,6 +848,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
                "upload qual");
         }
         CK(cudaEventRecord(c->ev_chunk[k], c->up_stream), "event");
+        if (k == 0 || k == gsnp_context::kUploadChunks / 2 - 1 || k == gsnp_context::kUploadChunks - 1)
+            tl.rec("uploaded piece " + std::to_string(k), c->up_stream);
     }
     timer.mark("uploads issued");
     auto drain = [&]() {
@@ -942,6 +972,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
                 CK(cudaGetLastError(), "gather kernel");
             }
             CK(cudaEventRecord(c->ev_gather[(size_t)gathered_seg], c->gather_stream), "event");
+            tl.rec("gathered " + std::to_string(gathered_seg), c->gather_stream);
         }
         return GSNP_OK;
     };
@@ -952,9 +983,11 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         if (rc != GSNP_OK) return rc;
         CK(cudaStreamWaitEvent(c->stream, c->ev_gather[(size_t)need], 0), "wait");
         c->n_gathered = segs[(size_t)need].dhi;   /* the rows the kernels of si may read */
+        tl.rec("calling " + std::to_string(si), c->stream);
         return GSNP_OK;
     };
     auto after = [&](size_t si) -> int {
+        tl.rec("called " + std::to_string(si), c->stream);
         if (!out) return GSNP_OK;
         const int64_t s0 = segs[si].t0 * kTile, s1 = std::min(segs[si].t1 * kTile, c->chr_len);
         if (s1 <= s0) return GSNP_OK;
@@ -963,11 +996,15 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(cudaMemcpyAsync(out + s0, c->d_out + s0, (size_t)(s1 - s0) * sizeof(SiteCall), cudaMemcpyDeviceToHost,
                            c->down_stream),
            "download");
+        tl.rec("downloaded " + std::to_string(si), c->down_stream);
         return GSNP_OK;
     };
     int rc2 = run_calling(c, segs, before, after);
     cudaError_t e_up = cudaStreamSynchronize(c->up_stream), e_down = cudaStreamSynchronize(c->down_stream);
     const cudaError_t e_gather = cudaStreamSynchronize(c->gather_stream);
+    tl.rec("end", c->down_stream);
+    cudaStreamSynchronize(c->down_stream);
+    tl.print("gsnp_call_chromosome");
     timer.mark("calling (pipelined)");
     if (rc2 != GSNP_OK) {
         drain();
