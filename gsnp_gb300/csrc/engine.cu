@@ -146,6 +146,8 @@ __global__ void __launch_bounds__(kDepThreads) dep_index_kernel(int64_t n, const
     }
 }
 
+constexpr int kGatherRows = 4;   /* row groups per gather block */
+
 __device__ __forceinline__ uint8_t upper_base(uint8_t b, bool* bad) {
     switch (b) {
         case 'A': case 'a': return 'A';
@@ -169,43 +171,66 @@ __global__ void __launch_bounds__(256) gather_reads_kernel(
     const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual, int pitch, int L, int rows_per_block,
     int32_t* __restrict__ pos, int32_t* __restrict__ lenhit, int32_t* __restrict__ len,
     uint8_t* __restrict__ strand, uint16_t* __restrict__ bq, int* __restrict__ error) {
+    /* kGatherRows groups of rows per block, one row of each group per thread:
+     * the groups' load chains (index, length, bases and qualities) are
+     * independent, so they are in flight together */
     const int per_row = (L + VEC - 1) / VEC;
     const int local = threadIdx.x / per_row, cv = threadIdx.x - local * per_row;
-    const int64_t row = row_begin + (int64_t)blockIdx.x * rows_per_block + local;
+    const int c0 = cv * VEC;
+    const int64_t first = row_begin + (int64_t)blockIdx.x * rows_per_block * kGatherRows + local;
     bool bad = false, bad_idx = false;
-    if (local < rows_per_block && row < row_end) {
-        const int64_t src = idx[row];
-        if (src < 0 || src >= n_raw) {   /* the host and device filters disagree */
-            bad_idx = true;
-        } else {
-            const int32_t rl = rlen[src];
-            if (cv == 0) {
-                pos[row] = rpos[src];
-                len[row] = rl;
-                lenhit[row] = (int32_t)(((uint32_t)(rl & 0xffff) << 16) | ((uint32_t)rhit[src] & 0xffffu));
-                strand[row] = rstrand[src];
-            }
-            const int c0 = cv * VEC;
-            if (VEC == 4) {
-                const uint32_t s4 = *reinterpret_cast<const uint32_t*>(seq + src * pitch + c0);
-                const uint32_t q4 = *reinterpret_cast<const uint32_t*>(qual + src * pitch + c0);
-                uint32_t lo = 0, hi = 0;
+    int64_t src[kGatherRows];
+    bool ok[kGatherRows];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint8_t b = c0 + k < rl ? upper_base((uint8_t)(s4 >> (8 * k)), &bad) : (uint8_t)'A';
-                    const uint32_t v = (uint32_t)b | (((q4 >> (8 * k)) & 0xffu) << 8);
-                    if (k < 2) lo |= v << (16 * k);
-                    else hi |= v << (16 * (k - 2));
-                }
-                *reinterpret_cast<uint2*>(bq + row * L + c0) = make_uint2(lo, hi);
-            } else {
-                uint8_t b = 'A', q = 0;
-                if (c0 < pitch) {
-                    q = qual[src * pitch + c0];
-                    if (c0 < rl) b = upper_base(seq[src * pitch + c0], &bad);
-                }
-                bq[row * L + c0] = (uint16_t)b | ((uint16_t)q << 8);
+    for (int g = 0; g < kGatherRows; ++g) {
+        const int64_t row = first + (int64_t)g * rows_per_block;
+        ok[g] = local < rows_per_block && row < row_end;
+        src[g] = ok[g] ? idx[row] : 0;
+        if (ok[g] && (src[g] < 0 || src[g] >= n_raw)) {   /* the host and device filters disagree */
+            bad_idx = true;
+            ok[g] = false;
+        }
+    }
+    int32_t rl[kGatherRows];
+    uint32_t s4[kGatherRows], q4[kGatherRows];
+#pragma unroll
+    for (int g = 0; g < kGatherRows; ++g) {
+        rl[g] = 0;
+        s4[g] = q4[g] = 0;
+        if (!ok[g]) continue;
+        rl[g] = rlen[src[g]];
+        if (VEC == 4) {
+            s4[g] = *reinterpret_cast<const uint32_t*>(seq + src[g] * pitch + c0);
+            q4[g] = *reinterpret_cast<const uint32_t*>(qual + src[g] * pitch + c0);
+        } else if (c0 < pitch) {
+            s4[g] = seq[src[g] * pitch + c0];
+            q4[g] = qual[src[g] * pitch + c0];
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < kGatherRows; ++g) {
+        if (!ok[g]) continue;
+        const int64_t row = first + (int64_t)g * rows_per_block;
+        if (cv == 0) {
+            pos[row] = rpos[src[g]];
+            len[row] = rl[g];
+            lenhit[row] = (int32_t)(((uint32_t)(rl[g] & 0xffff) << 16) | ((uint32_t)rhit[src[g]] & 0xffffu));
+            strand[row] = rstrand[src[g]];
+        }
+        if (VEC == 4) {
+            uint32_t lo = 0, hi = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint8_t b = c0 + k < rl[g] ? upper_base((uint8_t)(s4[g] >> (8 * k)), &bad) : (uint8_t)'A';
+                const uint32_t v = (uint32_t)b | (((q4[g] >> (8 * k)) & 0xffu) << 8);
+                if (k < 2) lo |= v << (16 * k);
+                else hi |= v << (16 * (k - 2));
             }
+            *reinterpret_cast<uint2*>(bq + row * L + c0) = make_uint2(lo, hi);
+        } else {
+            uint8_t b = 'A';
+            if (c0 < pitch && c0 < rl[g]) b = upper_base((uint8_t)s4[g], &bad);
+            bq[row * L + c0] = (uint16_t)b | ((uint16_t)(c0 < pitch ? q4[g] : 0u) << 8);
         }
     }
     const unsigned any_bad = __ballot_sync(0xffffffffu, bad), any_idx = __ballot_sync(0xffffffffu, bad_idx);
@@ -383,6 +408,11 @@ struct gsnp_context {
     cudaStream_t up_stream = nullptr, down_stream = nullptr, gather_stream = nullptr;
     std::vector<cudaEvent_t> ev_gather;   /* per segment: its reads are gathered */
     cudaEvent_t ev_index = nullptr;       /* the deposited index list is built */
+    /* the depth bins of one pass run side by side, so that one bin's last
+     * wave overlaps the next bin's first */
+    static const int kBinStreams = 3;
+    cudaStream_t bin_stream[kBinStreams] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[kBinStreams] = {};
     cudaEvent_t ev_small = nullptr, ev_seg = nullptr, ev_chunk[kUploadChunks] = {};
     int* d_gerror = nullptr;       /* gather: 2 a base other than ACGT/acgt, 3 index list mismatch */
     /* Pinned host memory mapped into the device: the small values the host
@@ -657,6 +687,61 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
     auto end = [&](int k) {
         if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], c->stream);
     };
+    /* launch records of the bins, timed on the bin's own stream */
+    auto begin_on = [&](int kind, int sl, int64_t tiles, cudaStream_t st) -> int {
+        const int k = begin(kind, sl, tiles);
+        if (k >= 0) cudaEventRecord(c->ev[2 * k], st);
+        return k;
+    };
+    auto end_on = [&](int k, cudaStream_t st) {
+        if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], st);
+    };
+    if (!c->ev_fork) {
+        CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        for (int i = 0; i < gsnp_context::kBinStreams; ++i) {
+            CK(cudaStreamCreateWithFlags(&c->bin_stream[i], cudaStreamNonBlocking), "cudaStreamCreate");
+            CK(cudaEventCreateWithFlags(&c->ev_join[i], cudaEventDisableTiming), "cudaEventCreate");
+        }
+    }
+    /* the non-empty bins of kind in decreasing tile count.  In a call of
+     * several segments, whose bins are small launches, they run side by side
+     * on the bin streams (the context's stream waits for all of them); a
+     * single pass runs them in turn, each launch timed on its own. */
+    const bool side_by_side = segs.size() > 1;
+    auto launch_bins = [&](const CallArgs& args, int kind, int base) -> int {
+        int order[kNumBins], m = 0;
+        for (int b = 0; b < kNumBins; ++b)
+            if (c->h_bin_count[base + b] > 0) order[m++] = b;
+        std::sort(order, order + m, [&](int x, int y) { return c->h_bin_count[base + x] > c->h_bin_count[base + y]; });
+        if (m == 0) return GSNP_OK;
+        if (!side_by_side) {
+            for (int j = 0; j < m; ++j) {
+                const int b = order[j];
+                const int nb = c->h_bin_count[base + b];
+                const int k = begin(kind, bin_slots(b), nb);
+                CK(launch_bin(args, kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, c->stream),
+                   "calling kernel");
+                end(k);
+            }
+            return GSNP_OK;
+        }
+        CK(cudaEventRecord(c->ev_fork, c->stream), "event");
+        const int ns = std::min(m, (int)gsnp_context::kBinStreams);
+        for (int i = 0; i < ns; ++i) CK(cudaStreamWaitEvent(c->bin_stream[i], c->ev_fork, 0), "wait");
+        for (int j = 0; j < m; ++j) {
+            const int b = order[j];
+            cudaStream_t st = c->bin_stream[j % ns];
+            const int nb = c->h_bin_count[base + b];
+            const int k = begin_on(kind, bin_slots(b), nb, st);
+            CK(launch_bin(args, kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, st), "calling kernel");
+            end_on(k, st);
+        }
+        for (int i = 0; i < ns; ++i) {
+            CK(cudaEventRecord(c->ev_join[i], c->bin_stream[i]), "event");
+            CK(cudaStreamWaitEvent(c->stream, c->ev_join[i], 0), "wait");
+        }
+        return GSNP_OK;
+    };
     for (size_t si = 0; si < segs.size(); ++si) {
         const Segment& g = segs[si];
         if (before) {
@@ -676,12 +761,9 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             memcpy(c->h_bin_count, c->h_map + kMapBins, sizeof(c->h_bin_count));
             bool any_fast = false;
             for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
-            for (int b = 0; b < kNumBins; ++b) {
-                if (c->h_bin_count[b] == 0) continue;
-                k = begin(kKindFP64, bin_slots(b), c->h_bin_count[b]);
-                CK(launch_bin(a, kKindFP64, b, c->d_bin_tiles + (int64_t)b * n_tiles, c->h_bin_count[b], c->stream),
-                   "calling kernel");
-                end(k);
+            {
+                const int rc = launch_bins(a, kKindFP64, 0);
+                if (rc != GSNP_OK) return rc;
             }
             if (!any_fast) continue;
             for (int attempt = 0; attempt < 2; ++attempt) {
@@ -689,14 +771,9 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
                 af.n_reads = c->n_gathered;
                 const int first = c->n_launches;
                 CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
-                for (int b = 0; b < kNumBins; ++b) {
-                    const int nb = c->h_bin_count[kNumBins + b];
-                    if (nb == 0) continue;
-                    k = begin(kKindFast, bin_slots(b), nb);
-                    CK(launch_bin(af, kKindFast, b, c->d_bin_tiles + (int64_t)(kNumBins + b) * n_tiles, nb,
-                                  c->stream),
-                       "fast calling kernel");
-                    end(k);
+                {
+                    const int rc = launch_bins(af, kKindFast, kNumBins);
+                    if (rc != GSNP_OK) return rc;
                 }
                 CK(to_map(c, c->d_dcount, kMapDcount, sizeof(c->h_dcount)), "deferred counts");
                 CK(cudaStreamSynchronize(c->stream), "fast calling");
@@ -958,7 +1035,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
                 const int64_t chunk = std::min<int64_t>((g.raw_hi - 1) / chunk_rows, gsnp_context::kUploadChunks - 1);
                 CK(cudaStreamWaitEvent(c->gather_stream, c->ev_chunk[chunk], 0), "wait");
                 const int64_t rows = g.dhi - g.dlo;
-                const unsigned blocks = (unsigned)((rows + rows_per_block - 1) / rows_per_block);
+                const int64_t per_block = (int64_t)rows_per_block * kGatherRows;
+                const unsigned blocks = (unsigned)((rows + per_block - 1) / per_block);
                 if (vec4)
                     gather_reads_kernel<4><<<blocks, 256, 0, c->gather_stream>>>(
                         g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
@@ -1061,6 +1139,14 @@ void gsnp_context_destroy(gsnp_context* c) {
     if (c->h_map) cudaFreeHost(c->h_map);
     if (c->ev_seg) cudaEventDestroy(c->ev_seg);
     if (c->ev_index) cudaEventDestroy(c->ev_index);
+    for (int i = 0; i < gsnp_context::kBinStreams; ++i) {
+        if (c->ev_join[i]) cudaEventDestroy(c->ev_join[i]);
+        if (c->bin_stream[i]) {
+            cudaStreamSynchronize(c->bin_stream[i]);
+            cudaStreamDestroy(c->bin_stream[i]);
+        }
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     for (cudaEvent_t e : c->ev_gather) cudaEventDestroy(e);
     if (c->gather_stream) {
         cudaStreamSynchronize(c->gather_stream);
