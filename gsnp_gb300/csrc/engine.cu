@@ -932,6 +932,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     auto drain = [&]() {
         cudaStreamSynchronize(c->up_stream);
         if (c->gather_stream) cudaStreamSynchronize(c->gather_stream);
+        for (cudaStream_t b : c->bin_stream)
+            if (b) cudaStreamSynchronize(b);
         cudaStreamSynchronize(c->stream);
         cudaStreamSynchronize(c->down_stream);
     };
