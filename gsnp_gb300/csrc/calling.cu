@@ -50,6 +50,14 @@ constexpr unsigned kFull = 0xffffffffu;
 /* bins whose sites keep 4-bit pcr occurrence counts (walk_records) */
 __host__ __device__ constexpr bool kDeepBin(int slots) { return slots >= 96; }
 
+/* The FP32 kernel's 256-slot bin keeps its record columns in global memory
+ * (CallArgs::deep_recs, one slice per CTA) instead of shared memory: 32 KB of
+ * columns per one-warp CTA would allow 6 CTAs per SM, where the pcr counts
+ * alone leave the SM limited by registers only (22.1 against 27.7 ms per c2
+ * step).  The smaller deep bins, and the FP64 kernel's, ran slower that
+ * way and keep shared memory. */
+__host__ __device__ constexpr bool kGlobalRecs(int slots, bool fast) { return fast && slots >= 256; }
+
 /* resident CTAs per SM the calling kernels are compiled for; this caps their
  * registers: 64 for the FP32 kernel (32 warps per SM, a few spilled words
  * cost less than the latency the extra warps hide), 128 for the FP64 one */
@@ -507,8 +515,9 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
 template <int SLOTS>
 __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);
-    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;
+    constexpr bool kGlobal = kGlobalRecs(SLOTS, true);
+    uint32_t* recs_all = kGlobal ? a.deep_recs + (size_t)blockIdx.x * SLOTS * kTile : reinterpret_cast<uint32_t*>(smem);
+    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + (kGlobal ? 0 : SLOTS * kTile);
 
     const int t = threadIdx.x, lane = t & 31;
     const int64_t tile = tiles[blockIdx.x];
@@ -678,10 +687,11 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
 
 static const int kSlots[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
 
-size_t call_smem_bytes(int slots, int L) {
-    /* records [slots][kTile], then the pcr state [nw][kTile] */
+size_t call_smem_bytes(int slots, int L, bool fast) {
+    /* records [slots][kTile] (unless in global memory), then the pcr state
+     * [nw][kTile] */
     const size_t nw = (size_t)pcr_words(L, kDeepBin(slots));
-    return (size_t)slots * kTile * 4 + nw * kTile * 4;
+    return (kGlobalRecs(slots, fast) ? 0 : (size_t)slots * kTile * 4) + nw * kTile * 4;
 }
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
@@ -696,7 +706,7 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_
 
 template <int SLOTS>
 static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles, int count, cudaStream_t stream) {
-    const int smem = (int)call_smem_bytes(SLOTS, a.L);
+    const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
     if (kind == kKindFast) {
         cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         call_fast_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
@@ -730,5 +740,11 @@ cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream) {
 }
 
 int bin_slots(int bin) { return kSlots[bin]; }
+
+/* 32-bit words of global record scratch a launch of `count` tiles of bin
+ * `bin` of kernel `kind` needs */
+int64_t bin_global_words(int kind, int bin, int64_t count) {
+    return kGlobalRecs(kSlots[bin], kind == kKindFast) ? count * kSlots[bin] * kTile : 0;
+}
 
 }  // namespace gsnp

@@ -92,6 +92,7 @@ struct CallArgs {
     int64_t n_tiles;
     int64_t* tile_rng;           /* [n_tiles][2]: reads starting in [s0 - L + 1, s0 + kTile) of each tile */
     int64_t* warp_rng;           /* [n_tiles][2]: reads that can cover each tile's sites */
+    uint32_t* deep_recs;         /* record columns of the deep bins' CTAs, [CTA][SLOTS][kTile] */
     /* the call of a site without records or counts, by site code (16 entries;
      * empty_valid[code] = 0 where it is not a fixed homozygous call) */
     const SiteCall* empty_calls;

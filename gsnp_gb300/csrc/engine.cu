@@ -43,6 +43,7 @@ cudaError_t launch_tile_bounds(const CallArgs& a, int64_t r_begin, int64_t r_end
                                cudaStream_t stream);
 cudaError_t launch_empty_calls(const CallArgs& a, SiteCall* calls, uint8_t* valid, cudaStream_t stream);
 int bin_slots(int bin);
+int64_t bin_global_words(int kind, int bin, int64_t count);
 
 /* ---- device helpers ---- */
 
@@ -390,6 +391,8 @@ struct gsnp_context {
     int64_t dsite_cap = 0, dpool_cap = 0;
     int64_t* d_warp_rng = nullptr;  /* [n_tiles][2] */
     int64_t* d_tile_rng = nullptr;  /* [n_tiles][2] */
+    uint32_t* d_deep = nullptr;     /* record columns of the deep bins' CTAs */
+    int64_t deep_cap = 0;           /* words */
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
@@ -557,7 +560,7 @@ void free_all(gsnp_context* c) {
                     c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_win_host_src, c->d_emit,
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-                    c->d_idx, c->d_dep_off, c->d_gerror};
+                    c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -714,12 +717,28 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             if (c->h_bin_count[base + b] > 0) order[m++] = b;
         std::sort(order, order + m, [&](int x, int y) { return c->h_bin_count[base + x] > c->h_bin_count[base + y]; });
         if (m == 0) return GSNP_OK;
+        /* the deep bins' record columns: a slice of the scratch per launch */
+        int64_t off[kNumBins] = {}, words = 0;
+        for (int j = 0; j < m; ++j) {
+            off[order[j]] = words;
+            words += bin_global_words(kind, order[j], c->h_bin_count[base + order[j]]);
+        }
+        if (words > c->deep_cap) {
+            CK(cudaStreamSynchronize(c->stream), "deep scratch");
+            CK(dev_alloc(&c->d_deep, (size_t)(words + words / 4)), "cudaMalloc deep scratch");
+            c->deep_cap = words + words / 4;
+        }
+        auto with_scratch = [&](int b) {
+            CallArgs la = args;
+            la.deep_recs = c->d_deep + off[b];
+            return la;
+        };
         if (!side_by_side) {
             for (int j = 0; j < m; ++j) {
                 const int b = order[j];
                 const int nb = c->h_bin_count[base + b];
                 const int k = begin(kind, bin_slots(b), nb);
-                CK(launch_bin(args, kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, c->stream),
+                CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, c->stream),
                    "calling kernel");
                 end(k);
             }
@@ -733,7 +752,8 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             cudaStream_t st = c->bin_stream[j % ns];
             const int nb = c->h_bin_count[base + b];
             const int k = begin_on(kind, bin_slots(b), nb, st);
-            CK(launch_bin(args, kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, st), "calling kernel");
+            CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, st),
+               "calling kernel");
             end_on(k, st);
         }
         for (int i = 0; i < ns; ++i) {
