@@ -47,8 +47,16 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-/* bins whose sites keep 4-bit pcr occurrence counts (walk_records) */
-__host__ __device__ constexpr bool kDeepBin(int slots) { return slots >= 96; }
+/* bits of pcr occurrence count per (strand, cycle) key (walk_records) in the
+ * bins of each record-slot capacity, for the FP32 (fast) or the FP64 kernel.
+ * Two bits leave a scan back over the group only for a key seen three
+ * times; at 30x one record in about fourteen repeats a key, and with one bit
+ * the scans of single lanes held the whole warp (c1 at 25% scale:
+ * fast<40> 2.63 -> 2.37 ms, tiles<40> 5.26 -> 4.97 ms).  The FP32 kernel's
+ * 32-slot bin ran 3% slower with them and keeps one bit. */
+__host__ __device__ constexpr int kPcrBits(int slots, bool fast) {
+    return slots >= 96 ? 4 : (fast && slots <= 32) ? 1 : 2;
+}
 
 /* The FP32 kernel's 256-slot bin keeps its record columns in global memory
  * (CallArgs::deep_recs, one slice per CTA) instead of shared memory: 32 KB of
@@ -167,50 +175,78 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
     return pk;
 }
 
-/* Ascending sort of one site's record column.  Up to 32 records: a bitonic
- * network in registers (the column padded with 0xFFFFFFFF, which no record
- * word equals), the same instruction stream in every lane of the warp.
- * Deeper columns: Shell sort with Ciura's gaps (132, 57, 23, 10, 4, 1),
- * whose gapped passes leave the final insertion pass short shifts. */
-__device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
-    if (num <= 32) {
-        uint32_t v[32];
+/* Ascending in-register bitonic network over v[0, T), T a power of two; every
+ * lane runs the same instruction stream. */
+template <int T>
+__device__ __forceinline__ void bitonic_sort(uint32_t* v) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = i < num ? recs[i * kTile] : 0xFFFFFFFFu;
+    for (int k = 2; k <= T; k <<= 1)
 #pragma unroll
-        for (int k = 2; k <= 32; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1)
 #pragma unroll
-            for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int l = i ^ j;
-                    if (l > i) {
-                        const uint32_t a = v[i], b = v[l];
-                        const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
-                        if ((i & k) == 0) { v[i] = lo; v[l] = hi; }
-                        else { v[i] = hi; v[l] = lo; }
-                    }
+            for (int i = 0; i < T; ++i) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t a = v[i], b = v[l];
+                    const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+                    if ((i & k) == 0) { v[i] = lo; v[l] = hi; }
+                    else { v[i] = hi; v[l] = lo; }
                 }
-#pragma unroll
-        for (int i = 0; i < 32; ++i)
-            if (i < num) recs[i * kTile] = v[i];
-        return;
-    }
-    /* Ciura's gaps below the column length, each a constant of the unrolled loop */
-#pragma unroll
-    for (int gi = 0; gi < 6; ++gi) {
-        const int h = gi == 0 ? 132 : gi == 1 ? 57 : gi == 2 ? 23 : gi == 3 ? 10 : gi == 4 ? 4 : 1;
-        if (h >= num) continue;
-        for (int i = h; i < num; ++i) {
-            const uint32_t w = recs[i * kTile];
-            int j = i;
-            while (j >= h) {
-                const uint32_t prev = recs[(j - h) * kTile];
-                if (prev <= w) break;
-                recs[j * kTile] = prev;
-                j -= h;
             }
-            recs[j * kTile] = w;
+}
+
+/* Merge the ascending v[0, cnt) (cnt <= T) into the ascending column prefix
+ * recs[0, P), from the back: each v[j], largest first, moves the prefix
+ * records above it up by the number of v entries still to place, then takes
+ * its slot.  A write at slot k = i + (entries left) never reaches a prefix
+ * record not yet moved, so no scratch is needed; v is indexed by unrolled
+ * constants only, so it stays in registers. */
+template <int T>
+__device__ __forceinline__ void merge_back(uint32_t* recs, int P, const uint32_t* v, int cnt) {
+    int i = P - 1, k = P + cnt - 1;
+#pragma unroll
+    for (int j = T - 1; j >= 0; --j) {
+        if (j < cnt) {
+            const uint32_t x = v[j];
+            while (i >= 0) {
+                const uint32_t h = recs[i * kTile];
+                if (h <= x) break;
+                recs[k * kTile] = h;
+                --k;
+                --i;
+            }
+            recs[k * kTile] = x;
+            --k;
+        }
+    }
+}
+
+__host__ __device__ constexpr int pow2_at_least(int n) { return n <= 1 ? 1 : 2 * pow2_at_least((n + 1) / 2); }
+
+/* Ascending sort of one site's record column of at most SLOTS records.  The
+ * first 32 records are sorted by a bitonic network in registers (padded with
+ * 0xFFFFFFFF, which no record word equals), so that every lane of the warp
+ * runs the same instructions whatever its depth.  Deeper columns take the rest
+ * in chunks of C records: each chunk is sorted the same way and merged into
+ * the sorted prefix from the back.  C is the bin's excess over 32 rounded up
+ * to a power of two (8 for the 40-slot bin), at most 32. */
+template <int SLOTS>
+__device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
+    uint32_t v[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = i < num ? recs[i * kTile] : 0xFFFFFFFFu;
+    bitonic_sort<32>(v);
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+        if (i < num) recs[i * kTile] = v[i];
+    if constexpr (SLOTS > 32) {
+        constexpr int C = pow2_at_least(SLOTS - 32) < 32 ? pow2_at_least(SLOTS - 32) : 32;
+        for (int c0 = 32; c0 < num; c0 += C) {
+            const int cnt = num - c0 < C ? num - c0 : C;
+#pragma unroll
+            for (int i = 0; i < C; ++i) v[i] = i < cnt ? recs[(c0 + i) * kTile] : 0xFFFFFFFFu;
+            bitonic_sort<C>(v);
+            merge_back<C>(recs, c0, v, cnt);
         }
     }
 }
@@ -473,7 +509,7 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
     if (!active) return;
     uint32_t* recs = recs_all + t;
     uint32_t* seen = seen_all + t;
-    sort_column(recs, p.num);
+    sort_column<SLOTS>(recs, p.num);
 
     double tl[16];
 #pragma unroll
@@ -486,7 +522,7 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
             for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = srcp[i];
         }
     } else {
-        likelihood_fp64<kDeepBin(SLOTS)>(a, recs, seen, kTile, p.num, tl);
+        likelihood_fp64<kPcrBits(SLOTS, false)>(a, recs, seen, kTile, p.num, tl);
         if (wflags & kWinKeepLik) {
             double* dst = a.lik_keep + site * 10;
 #pragma unroll
@@ -533,13 +569,13 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
     const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs_all + t).unpack();
     uint32_t* recs = recs_all + t;
     uint32_t* seen = seen_all + t;
-    if (active) sort_column(recs, p.num);
+    if (active) sort_column<SLOTS>(recs, p.num);
 
     uint8_t dflags = 0;
     if (active) {
         if (wflags & kWinKeepCounts) store_counts(a, site, p);
         /* adjusted quality of each record, written over its occurrence byte */
-        walk_records<true, kDeepBin(SLOTS)>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
+        walk_records<true, kPcrBits(SLOTS, true)>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
             recs[i * kTile] = (recs[i * kTile] & ~0xffu) | (uint32_t)qa;
         });
         /* FP32 sums, four records per compensated step (the grouping of
@@ -648,12 +684,12 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
     double tl[16], eps[16];
 #pragma unroll
     for (int g = 0; g < 16; ++g) { tl[g] = 0.0; eps[g] = 0.0; }
-    likelihood_fp32<true>(a, recs, seen, 1, p.num, tl, eps);
+    likelihood_fp32<4>(a, recs, seen, 1, p.num, tl, eps);
     if (d.flags & kCallSampled) {
         double t64[16];
 #pragma unroll
         for (int g = 0; g < 16; ++g) t64[g] = 0.0;
-        likelihood_fp64<true>(a, recs, seen, 1, p.num, t64);
+        likelihood_fp64<4>(a, recs, seen, 1, p.num, t64);
         double m = 0.0;
 #pragma unroll
         for (int g = 0; g < 16; ++g) m = fmax(m, fabs(t64[g] - tl[g]));
@@ -667,7 +703,7 @@ __global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t 
     SiteCall call;
     if (!site_posterior<true>(a, ori, p, tl, eps, lp, recs, 1, nq, &call)) {
         /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
-        likelihood_fp64<true>(a, recs, seen, 1, p.num, tl);
+        likelihood_fp64<4>(a, recs, seen, 1, p.num, tl);
         site_posterior<true>(a, ori, p, tl, nullptr, lp, recs, 1, nq, &call);
         call.flags |= kCallFixup;
         atomicAdd(a.stats + 1, 1ull);
@@ -690,7 +726,7 @@ static const int kSlots[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
 size_t call_smem_bytes(int slots, int L, bool fast) {
     /* records [slots][kTile] (unless in global memory), then the pcr state
      * [nw][kTile] */
-    const size_t nw = (size_t)pcr_words(L, kDeepBin(slots));
+    const size_t nw = (size_t)pcr_words(L, kPcrBits(slots, fast));
     return (kGlobalRecs(slots, fast) ? 0 : (size_t)slots * kTile * 4) + nw * kTile * 4;
 }
 

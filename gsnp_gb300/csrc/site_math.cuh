@@ -78,25 +78,28 @@ static_assert(sizeof(PackedPileup) == 32, "PackedPileup is 32 bytes");
  * says every record's occurrence field is 1 (the tile kernels' own pileup),
  * so that f may overwrite the low byte of record i.
  *
- * The per-site state at `seen` is one of:
- *   a bit per (strand, cycle) key, pcr_words(L, false) words: a repeated key
- *   counts its earlier occurrences by a scan back over the group, which is
- *   cheap where repeats are rare;
- *   with COUNTS, a 4-bit occurrence count per key, pcr_words(L, true) words,
- *   for deep sites where reads starting together repeat keys often.  The
- *   count saturates at 15; that is exact when tmax <= 16, since every tmp
- *   of 16 or more then gives q_adj = 1.  With a larger tmax the walk falls
- *   back to the bits and the scan. */
-__host__ __device__ __forceinline__ int pcr_words(int L, bool counts) {
-    return counts ? (2 * L + 7) >> 3 : (2 * L + 31) >> 5;
+ * The per-site state at `seen` is a BITS-wide saturating occurrence count per
+ * (strand, cycle) key, pcr_words(L, BITS) words.  Below saturation the count
+ * is tmp itself; a saturated count is resolved by a scan back over the group,
+ * except that with 4-bit counts and tmax <= 16 every tmp of 15 or more gives
+ * q_adj = 1 whatever its exact value.  One bit per key is the least state;
+ * two bits make the scan rare at moderate depth (a key seen three times);
+ * four bits serve deep sites, where reads starting together repeat keys
+ * often. */
+__host__ __device__ __forceinline__ int pcr_words(int L, int bits) {
+    const int per = 32 / bits;
+    return (2 * L + per - 1) / per;
 }
 
-template <bool UNIT_OCC, bool COUNTS = false, class F>
+template <bool UNIT_OCC, int BITS = 1, class F>
 __device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
                                              int num, F&& f) {
+    static_assert(BITS == 1 || BITS == 2 || BITS == 4, "1, 2 or 4 bits per key");
+    constexpr int kPer = 32 / BITS;
+    constexpr uint32_t kMax = (1u << BITS) - 1u;
     const int L = a.L;
-    const bool counts = COUNTS && a.tmax <= 16;
-    const int nw = pcr_words(L, counts);
+    const int nw = pcr_words(L, BITS);
+    const bool sat_exact = BITS == 4 && a.tmax <= 16;
     int gdc = -1, last_o = -1, gstart = 0;
     for (int i = 0; i < num; ++i) {
         const uint32_t w = recs[i * stride];
@@ -110,26 +113,21 @@ __device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* 
             last_o = o;
         }
         const int occ = UNIT_OCC ? 1 : rec_occ(w);
-        int tmp = 0;
-        if (counts) {
-            uint32_t* cw = seen + (key >> 3) * stride;
-            const int sh = (key & 7) * 4;
-            const uint32_t word = *cw;
-            tmp = (int)((word >> sh) & 15u);
-            const uint32_t next = (uint32_t)min(tmp + occ, 15);
-            *cw = (word & ~(15u << sh)) | (next << sh);
-        } else {
-            uint32_t* sw = seen + (key >> 5) * stride;
-            const uint32_t bit = 1u << (key & 31);
-            const uint32_t word = *sw;
-            if (word & bit) {
-                for (int j = gstart; j < i; ++j) {
-                    const uint32_t wj = recs[j * stride];
-                    if (((wj ^ w) & 0x1ff00u) == 0) tmp += UNIT_OCC ? 1 : rec_occ(wj);
-                }
-            } else {
-                *sw = word | bit;
+        uint32_t* cw = seen + (key / kPer) * stride;
+        const int sh = (key % kPer) * BITS;
+        const uint32_t word = *cw;
+        const uint32_t cnt = (word >> sh) & kMax;
+        int tmp = (int)cnt;
+        if (cnt == kMax && !sat_exact) {
+            tmp = 0;
+            for (int j = gstart; j < i; ++j) {
+                const uint32_t wj = recs[j * stride];
+                if (((wj ^ w) & 0x1ff00u) == 0) tmp += UNIT_OCC ? 1 : rec_occ(wj);
             }
+        }
+        if (cnt != kMax) {
+            const uint32_t next = min(cnt + (uint32_t)occ, kMax);
+            *cw = (word & ~(kMax << sh)) | (next << sh);
         }
         const int q = rec_q(w);
         for (int k = 0; k < occ; ++k) {
@@ -144,13 +142,13 @@ __device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* 
 }
 
 /* FP64 sums in the reference's order: the plain form and the fixup */
-template <bool COUNTS = false>
+template <int BITS = 1>
 __device__ __forceinline__ void likelihood_fp64(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
                                                 int num, double* tl) {
     double s[10];
 #pragma unroll
     for (int i = 0; i < 10; ++i) s[i] = 0.0;
-    walk_records<false, COUNTS>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
+    walk_records<false, BITS>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
         const double2* row = reinterpret_cast<const double2*>(a.lik64 + ((size_t)(qa * a.L + coord) * 4 + o) * 10);
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
@@ -195,14 +193,14 @@ __device__ __forceinline__ void lik32_row(const CallArgs& a, int qa, int coord, 
     x[8] = x2.x; x[9] = x2.y;
 }
 
-template <bool COUNTS = false>
+template <int BITS = 1>
 __device__ __forceinline__ void likelihood_fp32(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
                                                 int num, double* tl, double* eps) {
     Kahan10 k;
     k.init();
     float g0[10], g1[10];
     int pos = 0;   /* position of the next term in its group of four */
-    walk_records<false, COUNTS>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
+    walk_records<false, BITS>(a, recs, seen, stride, num, [&](int, int qa, int coord, int o) {
         float x[10];
         lik32_row(a, qa, coord, o, x);
         switch (pos) {
