@@ -157,7 +157,7 @@ def load_peaks():
 # sites.  Keyed by (workload, kernel kind, record slots); other kernels report
 # no traffic.
 NCU_BYTES_PER_SITE = {
-    ("c1", 2, 40): 150.2,   # call_fast_kernel<40>: 252.9 MB read + 70.8 MB written over 2,154,656 sites
+    ("c1", 2, 40): 150.6,   # call_fast_kernel<40>: 324.6 MB (dram__bytes.sum) over 2,154,656 sites
 }
 
 
