@@ -745,6 +745,14 @@ static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles,
     const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
     if (kind == kKindFast) {
         cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        /* The 40-slot bin runs faster with 72% of the SM's shared memory
+         * carved out (about 21 resident CTAs) than with the carveout that
+         * fits the most CTAs: the L1 left beside 29 CTAs holds too little of
+         * the likelihood table, whose loads are the longest stall (c1 at 25%
+         * scale: 2.02 -> 1.90 ms).  The other bins ran as fast or slower
+         * with 58-86%. */
+        if (SLOTS == 40)
+            cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 72);
         call_fast_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
     } else {
         cudaFuncSetAttribute(call_tiles_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
