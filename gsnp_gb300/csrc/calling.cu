@@ -9,11 +9,12 @@
  *   kernel/batchsort.cu:245-291         batchSortMP2 (per-site sort)
  *   kernel/likelihood_kernel.cu:168-256 likelihoodSparse_kernel
  *   kernel/posterior_kernel.cu:635-866  posterior_kernel, posterior_kernel2
- * Here the records of a site never leave shared memory: they are inserted in
- * sorted order as the pileup produces them ([slot][site] layout, so a warp's
- * accesses fall in 32 distinct banks whatever slot each lane is at), the
- * likelihood walks them in that order, and only the 32-byte SiteCall leaves the
- * SM.
+ * Here the records of a site stay on the SM: the pileup appends them to the
+ * site's column ([slot][site] layout, so a warp's accesses fall in 32 distinct
+ * banks whatever slot each lane is at), the column is sorted in place
+ * (column.cuh), the likelihood walks it in that order, and only the 32-byte
+ * SiteCall leaves the SM.  (The FP32 kernel's 256-slot bin keeps its columns
+ * in a global scratch slice per CTA, read through L1.)
  *
  * The pileup of a site is every deposited read that covers it, in (start, file)
  * order.  That equals the reference's window-resident pileup: its carried-over
@@ -85,9 +86,9 @@ __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v)
 /* Pileup of one warp's 32 consecutive sites (kernel/update_kernel.cu:260-325).
  * Reads [r_lo, r_hi) are those starting in [w0 - L + 1, w0 + 31]; their
  * positions, lengths and strands are loaded 32 at a time and broadcast, and
- * each lane takes the reads that cover its own site.  Records are inserted so
- * that the column stays in ascending order.  Lanes with !active only keep the
- * warp's loop going. */
+ * each lane takes the reads that cover its own site.  Records are appended to
+ * the site's column in pileup order.  Lanes with !active only keep the warp's
+ * loop going. */
 template <int SLOTS>
 __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
                                                    bool active, uint32_t* recs) {
@@ -173,82 +174,6 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
     pk.dep_uni = (uint16_t)dep_uni;
     pk.num = (uint16_t)num;
     return pk;
-}
-
-/* Ascending in-register bitonic network over v[0, T), T a power of two; every
- * lane runs the same instruction stream. */
-template <int T>
-__device__ __forceinline__ void bitonic_sort(uint32_t* v) {
-#pragma unroll
-    for (int k = 2; k <= T; k <<= 1)
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-            for (int i = 0; i < T; ++i) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const uint32_t a = v[i], b = v[l];
-                    const uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
-                    if ((i & k) == 0) { v[i] = lo; v[l] = hi; }
-                    else { v[i] = hi; v[l] = lo; }
-                }
-            }
-}
-
-/* Merge the ascending v[0, cnt) (cnt <= T) into the ascending column prefix
- * recs[0, P), from the back: each v[j], largest first, moves the prefix
- * records above it up by the number of v entries still to place, then takes
- * its slot.  A write at slot k = i + (entries left) never reaches a prefix
- * record not yet moved, so no scratch is needed; v is indexed by unrolled
- * constants only, so it stays in registers. */
-template <int T>
-__device__ __forceinline__ void merge_back(uint32_t* recs, int P, const uint32_t* v, int cnt) {
-    int i = P - 1, k = P + cnt - 1;
-#pragma unroll
-    for (int j = T - 1; j >= 0; --j) {
-        if (j < cnt) {
-            const uint32_t x = v[j];
-            while (i >= 0) {
-                const uint32_t h = recs[i * kTile];
-                if (h <= x) break;
-                recs[k * kTile] = h;
-                --k;
-                --i;
-            }
-            recs[k * kTile] = x;
-            --k;
-        }
-    }
-}
-
-__host__ __device__ constexpr int pow2_at_least(int n) { return n <= 1 ? 1 : 2 * pow2_at_least((n + 1) / 2); }
-
-/* Ascending sort of one site's record column of at most SLOTS records.  The
- * first 32 records are sorted by a bitonic network in registers (padded with
- * 0xFFFFFFFF, which no record word equals), so that every lane of the warp
- * runs the same instructions whatever its depth.  Deeper columns take the rest
- * in chunks of C records: each chunk is sorted the same way and merged into
- * the sorted prefix from the back.  C is the bin's excess over 32 rounded up
- * to a power of two (8 for the 40-slot bin), at most 32. */
-template <int SLOTS>
-__device__ __forceinline__ void sort_column(uint32_t* recs, int num) {
-    uint32_t v[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = i < num ? recs[i * kTile] : 0xFFFFFFFFu;
-    bitonic_sort<32>(v);
-#pragma unroll
-    for (int i = 0; i < 32; ++i)
-        if (i < num) recs[i * kTile] = v[i];
-    if constexpr (SLOTS > 32) {
-        constexpr int C = pow2_at_least(SLOTS - 32) < 32 ? pow2_at_least(SLOTS - 32) : 32;
-        for (int c0 = 32; c0 < num; c0 += C) {
-            const int cnt = num - c0 < C ? num - c0 : C;
-#pragma unroll
-            for (int i = 0; i < C; ++i) v[i] = i < cnt ? recs[(c0 + i) * kTile] : 0xFFFFFFFFu;
-            bitonic_sort<C>(v);
-            merge_back<C>(recs, c0, v, cnt);
-        }
-    }
 }
 
 /* dbSNP row of each flagged site of a tile: the rows before the tile plus the

@@ -66,7 +66,7 @@ struct CallArgs {
     int64_t chr_len;
     const DbSnpEntry* snp;       /* sorted by position, one row per site flagged in ori */
     int64_t n_snp;
-    const int32_t* tile_snp;     /* [n_tiles]: dbSNP rows before each 128-site tile */
+    const int32_t* tile_snp;     /* [n_tiles]: dbSNP rows before each tile */
     const double* snp_lp;        /* [n_snp][16] log10 prior of each dbSNP site (refine mode) */
     const float* snp_lp32;       /* [n_snp][12] the same in FP32, by table column */
     /* tables */

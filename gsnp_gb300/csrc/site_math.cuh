@@ -1,14 +1,10 @@
 /*
  * site_math.cuh - per-site arithmetic of the caller shared by every calling
- * kernel: the dependency-adjusted record walk, the FP64 and FP32 likelihood
- * sums, the rank-sum test and the posterior.
+ * kernel: the FP64 and FP32 likelihood sums over the dependency-adjusted
+ * record walk (column.cuh), the rank-sum test and the posterior.
  *
  * A site's records are 32-bit words in ascending order, `stride` words apart
- * (the tile kernels keep them in a [slot][site] shared-memory column).  The
- * pcr-dependency state of a site is a bitset of 2L bits (strand, cycle), also
- * `stride` words apart; a repeated (strand, cycle) within one observed-base
- * group is counted by scanning the group's earlier records, which replaces the
- * reference's per-site byte counter array (kernel/likelihood_kernel.cu:200-232).
+ * (the tile kernels keep them in a [slot][site] column).
  */
 #ifndef GSNP_SITE_MATH_CUH
 #define GSNP_SITE_MATH_CUH
@@ -17,6 +13,7 @@
 #include <stdint.h>
 
 #include "calling.cuh"
+#include "column.cuh"
 
 namespace gsnp {
 
@@ -67,79 +64,6 @@ struct PackedPileup {
     }
 };
 static_assert(sizeof(PackedPileup) == 32, "PackedPileup is 32 bytes");
-
-/* ------------------------------------------------------------------------ */
-/* record walk (kernel/likelihood_kernel.cu:187-255)                          */
-/* ------------------------------------------------------------------------ */
-
-/* Walk one site's sorted records: per observed-base group, tmp counts the
- * earlier occurrences of the record's (strand, cycle) and gdc the distinct
- * ones; f(i, q_adj, cycle, base) is called once per occurrence.  UNIT_OCC
- * says every record's occurrence field is 1 (the tile kernels' own pileup),
- * so that f may overwrite the low byte of record i.
- *
- * The per-site state at `seen` is a BITS-wide saturating occurrence count per
- * (strand, cycle) key, pcr_words(L, BITS) words.  Below saturation the count
- * is tmp itself; a saturated count is resolved by a scan back over the group,
- * except that with 4-bit counts and tmax <= 16 every tmp of 15 or more gives
- * q_adj = 1 whatever its exact value.  One bit per key is the least state;
- * two bits make the scan rare at moderate depth (a key seen three times);
- * four bits serve deep sites, where reads starting together repeat keys
- * often. */
-__host__ __device__ __forceinline__ int pcr_words(int L, int bits) {
-    const int per = 32 / bits;
-    return (2 * L + per - 1) / per;
-}
-
-template <bool UNIT_OCC, int BITS = 1, class F>
-__device__ __forceinline__ void walk_records(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
-                                             int num, F&& f) {
-    static_assert(BITS == 1 || BITS == 2 || BITS == 4, "1, 2 or 4 bits per key");
-    constexpr int kPer = 32 / BITS;
-    constexpr uint32_t kMax = (1u << BITS) - 1u;
-    const int L = a.L;
-    const int nw = pcr_words(L, BITS);
-    const bool sat_exact = BITS == 4 && a.tmax <= 16;
-    int gdc = -1, last_o = -1, gstart = 0;
-    for (int i = 0; i < num; ++i) {
-        const uint32_t w = recs[i * stride];
-        const int o = rec_base(w);
-        const int coord = rec_coord(w);
-        const int key = rec_strand(w) * L + coord;
-        if (o != last_o) {
-            for (int k = 0; k < nw; ++k) seen[k * stride] = 0u;
-            gstart = i;
-            gdc = -1;
-            last_o = o;
-        }
-        const int occ = UNIT_OCC ? 1 : rec_occ(w);
-        uint32_t* cw = seen + (key / kPer) * stride;
-        const int sh = (key % kPer) * BITS;
-        const uint32_t word = *cw;
-        const uint32_t cnt = (word >> sh) & kMax;
-        int tmp = (int)cnt;
-        if (cnt == kMax && !sat_exact) {
-            tmp = 0;
-            for (int j = gstart; j < i; ++j) {
-                const uint32_t wj = recs[j * stride];
-                if (((wj ^ w) & 0x1ff00u) == 0) tmp += UNIT_OCC ? 1 : rec_occ(wj);
-            }
-        }
-        if (cnt != kMax) {
-            const uint32_t next = min(cnt + (uint32_t)occ, kMax);
-            *cw = (word & ~(kMax << sh)) | (next << sh);
-        }
-        const int q = rec_q(w);
-        for (int k = 0; k < occ; ++k) {
-            if (tmp == 0) gdc += 1;
-            tmp++;
-            const int qa = (tmp < a.tmax && gdc < a.gmax)
-                               ? (int)__ldg(a.qadj + ((size_t)tmp * a.gmax + gdc) * 65 + q)
-                               : 1;
-            f(i, qa, coord, o);
-        }
-    }
-}
 
 /* FP64 sums in the reference's order: the plain form and the fixup */
 template <int BITS = 1>
