@@ -668,19 +668,26 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_
 template <int SLOTS>
 static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles, int count, cudaStream_t stream) {
     const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
+    cudaError_t e;
     if (kind == kKindFast) {
-        cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
         /* The 40-slot bin runs faster with 72% of the SM's shared memory
          * carved out (about 21 resident CTAs) than with the carveout that
          * fits the most CTAs: the L1 left beside 29 CTAs holds too little of
          * the likelihood table, whose loads are the longest stall (c1 at 25%
          * scale: 2.02 -> 1.90 ms).  The other bins ran as fast or slower
-         * with 58-86%. */
-        if (SLOTS == 40)
-            cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 72);
+         * with 58-86%.  The carveout is a hint: a refusal only costs speed,
+         * and its error is cleared so that it is not taken for the
+         * launch's. */
+        if (SLOTS == 40 &&
+            cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 72) !=
+                cudaSuccess)
+            (void)cudaGetLastError();
         call_fast_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
     } else {
-        cudaFuncSetAttribute(call_tiles_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(call_tiles_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
         call_tiles_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
     }
     return cudaGetLastError();

@@ -210,7 +210,8 @@ int dict_compress_device(const T* d_in, size_t n, void* d_scratch, size_t scratc
     int hflags = 0;
     cudaMemcpyAsync(&d, count, 8, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(&hflags, flags, 4, cudaMemcpyDeviceToHost, stream);
-    cudaError_t e = cudaStreamSynchronize(stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
         *err = cudaGetErrorString(e);
         return 1;
@@ -223,7 +224,11 @@ int dict_compress_device(const T* d_in, size_t n, void* d_scratch, size_t scratc
     while (md < d) md <<= 1;
     if (md > d) cudaMemsetAsync(keys + d, 0xff, (md - d) * 8, stream);
     if (md <= 8192) {
-        cudaFuncSetAttribute(bitonic_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 8);
+        e = cudaFuncSetAttribute(bitonic_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 8);
+        if (e != cudaSuccess) {
+            *err = cudaGetErrorString(e);
+            return 1;
+        }
         bitonic_smem_kernel<<<1, 1024, md * 8, stream>>>(keys, (int)md);
     } else {
         for (size_t k = 2; k <= md; k <<= 1)
@@ -242,7 +247,10 @@ int dict_compress_device(const T* d_in, size_t n, void* d_scratch, size_t scratc
     std::vector<uint64_t> hk(d);
     cudaMemcpyAsync(h_words, words, nw * 4, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hk.data(), keys, d * 8, cudaMemcpyDeviceToHost, stream);
-    e = cudaStreamSynchronize(stream);
+    /* a launch refused for its configuration is reported here, not by the
+     * synchronisation */
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
         *err = cudaGetErrorString(e);
         return 1;

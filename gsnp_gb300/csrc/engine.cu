@@ -506,6 +506,23 @@ cudaError_t dev_alloc(T** p, size_t count) {
     return cudaMalloc((void**)p, count * sizeof(T));
 }
 
+/* device buffers of one call, freed when it returns, on every path */
+struct CallTemps {
+    std::vector<void*> ptrs;
+    CallTemps() = default;
+    CallTemps(const CallTemps&) = delete;
+    CallTemps& operator=(const CallTemps&) = delete;
+    ~CallTemps() {
+        for (void* q : ptrs) cudaFree(q);
+    }
+    template <class T>
+    cudaError_t alloc(T** q, size_t bytes) {
+        const cudaError_t e = cudaMalloc((void**)q, bytes);
+        if (e == cudaSuccess) ptrs.push_back(*q);
+        return e;
+    }
+};
+
 /* host threads for the per-alignment pass of the window replay:
  * GSNP_HOST_THREADS, else every hardware thread (at most 64) */
 int host_threads() {
@@ -1286,13 +1303,14 @@ int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, d
     int32_t *d_pos = nullptr, *d_len = nullptr, *d_hit = nullptr;
     uint8_t *d_strand = nullptr, *d_seq = nullptr, *d_qual = nullptr;
     const size_t raw = (size_t)r->n * r->pitch;
-    CK(cudaMalloc((void**)&d_counts, nbins * 8), "cudaMalloc");
-    CK(cudaMalloc((void**)&d_pos, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
-    CK(cudaMalloc((void**)&d_len, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
-    CK(cudaMalloc((void**)&d_hit, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
-    CK(cudaMalloc((void**)&d_strand, std::max<int64_t>(r->n, 1)), "cudaMalloc");
-    CK(cudaMalloc((void**)&d_seq, std::max<size_t>(raw, 1)), "cudaMalloc");
-    CK(cudaMalloc((void**)&d_qual, std::max<size_t>(raw, 1)), "cudaMalloc");
+    CallTemps tmp;
+    CK(tmp.alloc(&d_counts, nbins * 8), "cudaMalloc");
+    CK(tmp.alloc(&d_pos, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
+    CK(tmp.alloc(&d_len, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
+    CK(tmp.alloc(&d_hit, std::max<int64_t>(r->n, 1) * 4), "cudaMalloc");
+    CK(tmp.alloc(&d_strand, std::max<int64_t>(r->n, 1)), "cudaMalloc");
+    CK(tmp.alloc(&d_seq, std::max<size_t>(raw, 1)), "cudaMalloc");
+    CK(tmp.alloc(&d_qual, std::max<size_t>(raw, 1)), "cudaMalloc");
     CK(cudaMemsetAsync(d_counts, 0, nbins * 8, c->stream), "memset");
     CK(cudaMemcpyAsync(d_pos, r->pos, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
     CK(cudaMemcpyAsync(d_len, r->len, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
@@ -1327,8 +1345,6 @@ int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, d
     std::vector<unsigned long long> counts(nbins);
     CK(cudaMemcpyAsync(counts.data(), d_counts, nbins * 8, cudaMemcpyDeviceToHost, c->stream), "download");
     CK(cudaStreamSynchronize(c->stream), "calibration");
-    cudaFree(d_counts); cudaFree(d_pos); cudaFree(d_len); cudaFree(d_hit);
-    cudaFree(d_strand); cudaFree(d_seq); cudaFree(d_qual);
     for (size_t i = 0; i < 256UL * 256UL * 16UL; ++i) pm[i] = 1.0;
     calibration_fill(*p, counts.data(), pm);
     return GSNP_OK;
