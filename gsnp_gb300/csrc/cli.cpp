@@ -30,6 +30,7 @@
 #include <fstream>
 #include <iostream>
 #include <map>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -201,14 +202,49 @@ void load_dbsnp(const std::string& path, std::map<std::string, Chromosome>* chrs
 
 /* ---- SOAP alignments (cpp/soap_snp.h:132-169) ---- */
 
+/* An array of a trivially copyable type left uninitialised, so that the
+ * threads that fill it are the first to touch its pages. */
+template <class T>
+struct RawArray {
+    std::unique_ptr<T[]> p;
+    void allocate(size_t count) { p.reset(new T[count > 0 ? count : 1]); }
+    T* data() { return p.get(); }
+    T& operator[](size_t i) { return p[i]; }
+    const T& operator[](size_t i) const { return p[i]; }
+};
+
 struct Reads {
-    std::vector<int32_t> pos, len, hit;
-    std::vector<uint8_t> strand;
-    std::vector<uint8_t> seq, qual;   /* L bytes per alignment */
+    size_t n = 0;                     /* alignments kept */
+    RawArray<int32_t> pos, len, hit;
+    RawArray<uint8_t> strand;
+    RawArray<uint8_t> seq, qual;      /* L bytes per alignment */
+    RawArray<uint16_t> chr_id;
     std::vector<std::string> chr;     /* distinct chromosome names, in order of first use */
-    std::vector<uint16_t> chr_id;
     std::string bad;                  /* first error */
 };
+
+/* One thread's share of the file: whole lines [begin, end), written to the
+ * output from row `first` on. */
+struct Chunk {
+    const char* begin = nullptr;
+    const char* end = nullptr;
+    size_t lines = 0;                 /* its lines: a bound on its alignments */
+    size_t first = 0;                 /* output row of its first alignment */
+    size_t kept = 0;                  /* alignments parsed */
+    std::vector<std::string> chr;     /* its chromosome names, in order of first use */
+    std::string bad;                  /* its first error */
+};
+
+size_t count_lines(const char* b, const char* e) {
+    size_t n = 0;
+    while (b < e) {
+        const char* nl = (const char*)memchr(b, '\n', (size_t)(e - b));
+        ++n;
+        if (!nl) break;
+        b = nl + 1;
+    }
+    return n;
+}
 
 bool next_token(const char*& p, const char* end, const char** tok, size_t* len) {
     while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
@@ -232,14 +268,15 @@ bool to_int(const char* t, size_t n, int* v) {
     return true;
 }
 
-/* Parse lines [begin, end) into r; the reference's stream extraction skips a
- * line whose fields do not parse. */
-void parse_chunk(const char* begin, const char* end, int L, Reads* r) {
+/* Parse the lines of chunk c into rows c->first, c->first + 1, ... of out;
+ * the reference's stream extraction skips a line whose fields do not parse.
+ * Row padding past the read length is 'A' and quality 0. */
+void parse_chunk(Chunk* c, int L, Reads* out) {
     std::string read, qual;
-    const char* p = begin;
-    while (p < end) {
-        const char* eol = (const char*)memchr(p, '\n', (size_t)(end - p));
-        if (!eol) eol = end;
+    const char* p = c->begin;
+    while (p < c->end) {
+        const char* eol = (const char*)memchr(p, '\n', (size_t)(c->end - p));
+        if (!eol) eol = c->end;
         const char* q = p;
         p = eol + 1;
         const char* tok[11];
@@ -251,11 +288,14 @@ void parse_chunk(const char* begin, const char* end, int L, Reads* r) {
         if (!to_int(tok[3], tl[3], &hit) || !to_int(tok[5], tl[5], &read_len) || !to_int(tok[8], tl[8], &position) ||
             !to_int(tok[9], tl[9], &mismatch))
             continue;
-        read.assign(tok[1], tl[1]);
-        qual.assign(tok[2], tl[2]);
+        const char* rs = tok[1];
+        const char* qs = tok[2];
+        size_t rn = tl[1], qn = tl[2];
         if (mismatch > 100) {
             int indel_pos;
             if (nt < 11 || !to_int(tok[10], tl[10], &indel_pos)) continue;
+            read.assign(tok[1], tl[1]);
+            qual.assign(tok[2], tl[2]);
             if (mismatch > 200) {
                 const int n = mismatch - 200;
                 const std::string ns(n > 0 ? n : 0, 'N');
@@ -266,28 +306,38 @@ void parse_chunk(const char* begin, const char* end, int L, Reads* r) {
                 read = read.substr(0, indel_pos) + read.substr(indel_pos + n, read_len - indel_pos - n);
                 qual = qual.substr(0, indel_pos) + qual.substr(indel_pos + n, read_len - indel_pos - n);
             }
+            rs = read.data();
+            qs = qual.data();
+            rn = read.size();
+            qn = qual.size();
         }
-        if (read_len < 0 || read_len > L || (int)read.size() < read_len || (int)qual.size() < read_len) {
-            if (r->bad.empty()) r->bad = "alignment longer than -L or than its sequence field";
+        if (read_len < 0 || read_len > L || rn < (size_t)read_len || qn < (size_t)read_len) {
+            if (c->bad.empty()) c->bad = "alignment longer than -L or than its sequence field";
             continue;
         }
-        const std::string chr(tok[7], tl[7]);
         size_t cid = 0;
-        while (cid < r->chr.size() && r->chr[cid] != chr) ++cid;
-        if (cid == r->chr.size()) r->chr.push_back(chr);
-        r->chr_id.push_back((uint16_t)cid);
-        r->pos.push_back(position - 1);
-        r->len.push_back(read_len);
-        r->hit.push_back(hit);
-        r->strand.push_back((uint8_t)tok[6][0]);
-        const size_t off = r->seq.size();
-        r->seq.resize(off + L, 'A');
-        r->qual.resize(off + L, 0);
-        memcpy(&r->seq[off], read.data(), (size_t)read_len);
-        memcpy(&r->qual[off], qual.data(), (size_t)read_len);
+        while (cid < c->chr.size() && (c->chr[cid].size() != tl[7] || memcmp(c->chr[cid].data(), tok[7], tl[7])))
+            ++cid;
+        if (cid == c->chr.size()) c->chr.emplace_back(tok[7], tl[7]);
+        const size_t k = c->first + c->kept++;
+        out->chr_id[k] = (uint16_t)cid;
+        out->pos[k] = position - 1;
+        out->len[k] = read_len;
+        out->hit[k] = hit;
+        out->strand[k] = (uint8_t)tok[6][0];
+        uint8_t* sp = out->seq.data() + k * (size_t)L;
+        uint8_t* qp = out->qual.data() + k * (size_t)L;
+        memcpy(sp, rs, (size_t)read_len);
+        memset(sp + read_len, 'A', (size_t)(L - read_len));
+        memcpy(qp, qs, (size_t)read_len);
+        memset(qp + read_len, 0, (size_t)(L - read_len));
     }
 }
 
+/* Parse a SOAP file on every hardware thread straight into the output
+ * arrays: the lines of each thread's share are counted first, so that each
+ * share has its rows before it is parsed.  Only lines that do not parse
+ * leave gaps, closed afterwards. */
 void load_soap(const std::string& path, int L, Reads* out) {
     const int fd = open(path.c_str(), O_RDONLY);
     if (fd < 0) die("No such file or directory:" + path, 1);
@@ -301,40 +351,69 @@ void load_soap(const std::string& path, int L, Reads* out) {
     const char* data = (const char*)mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
     if (data == MAP_FAILED) die("cannot map " + path);
     const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-    std::vector<const char*> cut(nt + 1);
-    cut[0] = data;
-    cut[nt] = data + size;
-    for (unsigned t = 1; t < nt; ++t) {
-        const char* c = data + size * t / nt;
-        if (c < cut[t - 1]) c = cut[t - 1];
-        const char* nl = (const char*)memchr(c, '\n', (size_t)(data + size - c));
-        cut[t] = nl ? nl + 1 : data + size;
+    std::vector<Chunk> ch(nt);
+    const char* prev = data;
+    for (unsigned t = 0; t < nt; ++t) {
+        ch[t].begin = prev;
+        const char* c = t + 1 == nt ? data + size : data + size * (t + 1) / nt;
+        if (c < prev) c = prev;
+        if (t + 1 < nt) {
+            const char* nl = (const char*)memchr(c, '\n', (size_t)(data + size - c));
+            c = nl ? nl + 1 : data + size;
+        }
+        ch[t].end = prev = c;
     }
-    std::vector<Reads> part(nt);
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; ++t) th.emplace_back(parse_chunk, cut[t], cut[t + 1], L, &part[t]);
-    for (auto& x : th) x.join();
+    auto on_threads = [&](auto&& f) {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t) th.emplace_back(f, t);
+        for (auto& x : th) x.join();
+    };
+    on_threads([&](unsigned t) { ch[t].lines = count_lines(ch[t].begin, ch[t].end); });
+    size_t rows = 0;
+    for (Chunk& c : ch) {
+        c.first = rows;
+        rows += c.lines;
+    }
+    out->pos.allocate(rows);
+    out->len.allocate(rows);
+    out->hit.allocate(rows);
+    out->strand.allocate(rows);
+    out->chr_id.allocate(rows);
+    out->seq.allocate(rows * (size_t)L);
+    out->qual.allocate(rows * (size_t)L);
+    on_threads([&](unsigned t) { parse_chunk(&ch[t], L, out); });
     munmap((void*)data, size);
     close(fd);
-    for (Reads& r : part) {
-        if (out->bad.empty() && !r.bad.empty()) out->bad = r.bad;
-        std::vector<uint16_t> remap(r.chr.size());
-        for (size_t i = 0; i < r.chr.size(); ++i) {
+    /* chromosome ids of each share to the file's list of names */
+    std::vector<std::vector<uint16_t>> remap(nt);
+    for (unsigned t = 0; t < nt; ++t) {
+        if (out->bad.empty() && !ch[t].bad.empty()) out->bad = ch[t].bad;
+        for (const std::string& name : ch[t].chr) {
             size_t k = 0;
-            while (k < out->chr.size() && out->chr[k] != r.chr[i]) ++k;
-            if (k == out->chr.size()) out->chr.push_back(r.chr[i]);
-            remap[i] = (uint16_t)k;
+            while (k < out->chr.size() && out->chr[k] != name) ++k;
+            if (k == out->chr.size()) out->chr.push_back(name);
+            remap[t].push_back((uint16_t)k);
         }
-        for (uint16_t id : r.chr_id) out->chr_id.push_back(remap[id]);
-        out->pos.insert(out->pos.end(), r.pos.begin(), r.pos.end());
-        out->len.insert(out->len.end(), r.len.begin(), r.len.end());
-        out->hit.insert(out->hit.end(), r.hit.begin(), r.hit.end());
-        out->strand.insert(out->strand.end(), r.strand.begin(), r.strand.end());
-        out->seq.insert(out->seq.end(), r.seq.begin(), r.seq.end());
-        out->qual.insert(out->qual.end(), r.qual.begin(), r.qual.end());
-        std::vector<uint8_t>().swap(r.seq);
-        std::vector<uint8_t>().swap(r.qual);
     }
+    on_threads([&](unsigned t) {
+        for (size_t i = ch[t].first; i < ch[t].first + ch[t].kept; ++i) out->chr_id[i] = remap[t][out->chr_id[i]];
+    });
+    /* close the gaps of skipped lines, share by share in file order (a
+     * share's rows only move down) */
+    size_t n = 0;
+    for (const Chunk& c : ch) {
+        if (n != c.first && c.kept > 0) {
+            memmove(&out->pos[n], &out->pos[c.first], c.kept * sizeof(int32_t));
+            memmove(&out->len[n], &out->len[c.first], c.kept * sizeof(int32_t));
+            memmove(&out->hit[n], &out->hit[c.first], c.kept * sizeof(int32_t));
+            memmove(&out->strand[n], &out->strand[c.first], c.kept);
+            memmove(&out->chr_id[n], &out->chr_id[c.first], c.kept * sizeof(uint16_t));
+            memmove(out->seq.data() + n * (size_t)L, out->seq.data() + c.first * (size_t)L, c.kept * (size_t)L);
+            memmove(out->qual.data() + n * (size_t)L, out->qual.data() + c.first * (size_t)L, c.kept * (size_t)L);
+        }
+        n += c.kept;
+    }
+    out->n = n;
 }
 
 /* ---- calibration matrix files (cpp/matrix.cc:215-241) ---- */
@@ -391,12 +470,13 @@ int main(int argc, char** argv) {
     Reads reads;
     load_soap(o.soap, p.read_length, &reads);
     if (!reads.bad.empty()) die("!!!ERROR: " + reads.bad);
-    if (reads.pos.empty()) die("!!!ERROR: no usable alignment.");
-    const std::string chr_name = reads.chr[reads.chr_id.back()];
+    if (reads.n == 0) die("!!!ERROR: no usable alignment.");
+    const uint16_t last_chr = reads.chr_id[reads.n - 1];
+    const std::string chr_name = reads.chr[last_chr];
     auto it = chrs.find(chr_name);
     if (it == chrs.end()) die("Assertion Failed: Chromosome: !" + chr_name + "! NOT found", 255);
-    for (size_t i = 0; i < reads.pos.size(); ++i)
-        if (reads.chr_id[i] != reads.chr_id.back() && reads.pos[i] >= 0)
+    for (size_t i = 0; i < reads.n; ++i)
+        if (reads.chr_id[i] != last_chr && reads.pos[i] >= 0)
             die("!!!ERROR: alignments on more than one chromosome (" + reads.chr[reads.chr_id[i]] + ", " + chr_name +
                 "); call one chromosome per run");
     Chromosome& chr = it->second;
@@ -409,7 +489,7 @@ int main(int argc, char** argv) {
     check(ctx, gsnp_load_reference(ctx, chr.codes.data(), (int64_t)chr.codes.size(), snp.data(), (int64_t)snp.size()),
           "reference");
 
-    const int64_t n = (int64_t)reads.pos.size();
+    const int64_t n = (int64_t)reads.n;
     gsnp_reads r{};
     r.n = n;
     r.pos = reads.pos.data();
