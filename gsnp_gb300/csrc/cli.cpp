@@ -334,7 +334,7 @@ void parse_chunk(Chunk* c, int L, Reads* out) {
     }
 }
 
-/* Parse a SOAP file on every hardware thread straight into the output
+/* Parse a SOAP file on the host threads straight into the output
  * arrays: the lines of each thread's share are counted first, so that each
  * share has its rows before it is parsed.  Only lines that do not parse
  * leave gaps, closed afterwards. */
@@ -350,7 +350,12 @@ void load_soap(const std::string& path, int L, Reads* out) {
     }
     const char* data = (const char*)mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
     if (data == MAP_FAILED) die("cannot map " + path);
-    const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    /* GSNP_HOST_THREADS, else every hardware thread (at most 64), as the
+     * library's host passes */
+    const char* env = getenv("GSNP_HOST_THREADS");
+    int want = env ? atoi(env) : 0;
+    if (want <= 0) want = (int)std::thread::hardware_concurrency();
+    const unsigned nt = (unsigned)std::max(1, std::min(want, 64));
     std::vector<Chunk> ch(nt);
     const char* prev = data;
     for (unsigned t = 0; t < nt; ++t) {

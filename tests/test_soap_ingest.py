@@ -5,8 +5,8 @@ fields, 1-based positions made 0-based, an N insertion of mismatch - 200
 bases (mismatch > 200) or a deletion of mismatch - 100 bases (mismatch > 100)
 at the indel position; lines whose fields do not parse are skipped.  Files
 with and without a final newline, with empty and blank lines, tabs or
-spaces, and more than one chromosome name, on every thread count the
-machine has (each thread takes a share of the lines)."""
+spaces, and more than one chromosome name, with the lines shared among 1, 3
+and 64 threads (GSNP_HOST_THREADS)."""
 import os
 import random
 import subprocess
@@ -97,8 +97,11 @@ def soap_check(tmp_path_factory, native_lib):
     return exe
 
 
-def run_loader(exe, path, L):
-    r = subprocess.run([exe, path, str(L)], capture_output=True, text=True, timeout=120)
+def run_loader(exe, path, L, threads=None):
+    env = dict(os.environ)
+    if threads:
+        env["GSNP_HOST_THREADS"] = str(threads)
+    r = subprocess.run([exe, path, str(L)], capture_output=True, text=True, timeout=120, env=env)
     assert r.returncode == 0, r.stderr
     out = r.stdout.split("\n")
     assert out[-1] == "" and out[-2].startswith("bad ") and out[-3].startswith("padding ")
@@ -112,13 +115,14 @@ def run_loader(exe, path, L):
 @pytest.mark.parametrize("seed,n,L,ending,with_bad", [(1, 4000, 50, "\n", False), (2, 4000, 100, "", False),
                                                      (3, 3000, 100, "\n\n\n", True), (4, 1, 35, "", False),
                                                      (5, 7, 100, "\n", False)])
-def test_soap_loader_matches_reference_parse(seed, n, L, ending, with_bad, tmp_path, soap_check):
+@pytest.mark.parametrize("threads", [1, 3, 64])
+def test_soap_loader_matches_reference_parse(seed, n, L, ending, with_bad, threads, tmp_path, soap_check):
     rng = random.Random(seed)
     lines = make_lines(rng, n, L, with_bad)
     path = str(tmp_path / "in.soap")
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + ending)
-    rows, padding, bad = run_loader(soap_check, path, L)
+    rows, padding, bad = run_loader(soap_check, path, L, threads)
     want_rows, want_bad = reference_parse(lines, L)
     assert padding == "ok"
     assert bad == want_bad
