@@ -148,47 +148,217 @@ void parse_args(int argc, char** argv, Options* o) {
 
 struct Chromosome {
     std::vector<uint8_t> codes;   /* (base >> 1) & 7, bit 3 = dbSNP */
-    std::map<uint32_t, gsnp_snp> snp;
+    std::vector<gsnp_snp> snp;    /* by position, the first row of each position */
 };
 
-void load_fasta(const std::string& path, std::map<std::string, Chromosome>* chrs) {
-    std::ifstream in(path);
-    if (!in) die("No such file or directory:" + path, 1);
-    std::string line, name;
-    Chromosome* cur = nullptr;
-    while (std::getline(in, line)) {
-        if (!line.empty() && line[0] == '>') {
-            std::string::size_type i = 1;
-            while (i != line.size() && !isspace((unsigned char)line[i])) ++i;
-            name = line.substr(1, i - 1);
-            auto r = chrs->emplace(name, Chromosome());
-            /* a repeated name keeps the entry and takes the later sequence,
-             * as the reference's loader does */
-            if (!r.second) std::cerr << "Insert Chromosome " << name << " Failed!\n";
-            cur = &r.first->second;
-            cur->codes.clear();
-        } else if (cur) {
-            for (char ch : line) cur->codes.push_back((uint8_t)((((unsigned char)ch) >> 1) & 7));
-        }
-    }
+bool next_token(const char*& p, const char* end, const char** tok, size_t* len) {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    if (p >= end) return false;
+    *tok = p;
+    while (p < end && *p != ' ' && *p != '\t' && *p != '\r') ++p;
+    *len = (size_t)(p - *tok);
+    return true;
 }
 
+bool to_int(const char* t, size_t n, int* v) {
+    char buf[32];
+    if (n == 0 || n >= sizeof(buf)) return false;
+    memcpy(buf, t, n);
+    buf[n] = 0;
+    char* e = nullptr;
+    errno = 0;
+    const long x = strtol(buf, &e, 10);
+    if (e == buf || errno) return false;
+    *v = (int)x;
+    return true;
+}
+
+/* A read-only mapping of a whole file (empty: data == nullptr). */
+struct MappedFile {
+    const char* data = nullptr;
+    size_t size = 0;
+    explicit MappedFile(const std::string& path) {
+        const int fd = open(path.c_str(), O_RDONLY);
+        if (fd < 0) die("No such file or directory:" + path, 1);
+        struct stat st;
+        fstat(fd, &st);
+        size = (size_t)st.st_size;
+        if (size > 0) {
+            void* m = mmap(nullptr, size, PROT_READ, MAP_PRIVATE, fd, 0);
+            if (m == MAP_FAILED) die("cannot map " + path);
+            data = (const char*)m;
+        }
+        close(fd);
+    }
+    ~MappedFile() {
+        if (data) munmap((void*)data, size);
+    }
+    MappedFile(const MappedFile&) = delete;
+    MappedFile& operator=(const MappedFile&) = delete;
+};
+
+/* Every byte of a line after a '>' line is a base of that chromosome, coded
+ * (byte >> 1) & 7; the name is the header up to the first space
+ * (cpp/chromosome.cc:172-205).  A sequence replaces its chromosome's codes
+ * when the next header comes, or at the end of the file if it is not empty:
+ * a repeated name takes the later sequence, except an empty one at the end. */
+void load_fasta(const std::string& path, std::map<std::string, Chromosome>* chrs) {
+    const MappedFile f(path);
+    const char* p = f.data;
+    const char* const end = f.data + f.size;
+    Chromosome* cur = nullptr;
+    std::vector<uint8_t> seq;
+    while (p < end) {
+        const char* eol = (const char*)memchr(p, '\n', (size_t)(end - p));
+        if (!eol) eol = end;
+        if (p < eol && *p == '>') {
+            if (cur) cur->codes.swap(seq);
+            seq.clear();
+            const char* q = p + 1;
+            while (q < eol && !isspace((unsigned char)*q)) ++q;
+            const std::string name(p + 1, (size_t)(q - p - 1));
+            auto r = chrs->emplace(name, Chromosome());
+            if (!r.second) std::cerr << "Insert Chromosome " << name << " Failed!\n";
+            cur = &r.first->second;
+        } else if (cur && eol > p) {
+            const size_t k = seq.size(), n = (size_t)(eol - p);
+            seq.resize(k + n);
+            uint8_t* d = seq.data() + k;
+            for (size_t i = 0; i < n; ++i) d[i] = (uint8_t)((((unsigned char)p[i]) >> 1) & 7);
+        }
+        p = eol + 1;
+    }
+    if (cur && !seq.empty()) cur->codes.swap(seq);
+}
+
+/* A decimal in its plain form, [+-]digits[.digits][(e|E)[+-]digits], to the
+ * nearest double; false if the form is not plain.  With at most 15
+ * significant digits and a power of ten up to 1e22, the digits and the power
+ * are exact doubles and one correctly rounded multiply or divide gives the
+ * nearest double (Clinger's fast path, "How to read floating point numbers
+ * accurately", 1990); anything else goes to strtod. */
+bool plain_decimal(const char* t, size_t n, double* out) {
+    size_t i = 0;
+    bool neg = false;
+    if (i < n && (t[i] == '+' || t[i] == '-')) neg = t[i++] == '-';
+    uint64_t m = 0;
+    int sig = 0, exp10 = 0;
+    size_t digits = 0;
+    auto take = [&](char ch, bool frac) {
+        if (sig == 0 && ch == '0') {
+            if (frac) --exp10;
+            return;
+        }
+        if (sig < 19) {
+            m = m * 10 + (uint64_t)(ch - '0');
+            if (frac) --exp10;
+        } else if (!frac) {
+            ++exp10;
+        }
+        ++sig;
+    };
+    while (i < n && isdigit((unsigned char)t[i])) take(t[i++], false), ++digits;
+    if (i < n && t[i] == '.') {
+        ++i;
+        while (i < n && isdigit((unsigned char)t[i])) take(t[i++], true), ++digits;
+    }
+    if (digits == 0) return false;
+    if (i < n && (t[i] == 'e' || t[i] == 'E')) {
+        ++i;
+        bool eneg = false;
+        if (i < n && (t[i] == '+' || t[i] == '-')) eneg = t[i++] == '-';
+        size_t ed = 0;
+        int e = 0;
+        while (i < n && isdigit((unsigned char)t[i])) {
+            if (e < 100000) e = e * 10 + (t[i] - '0');
+            ++i, ++ed;
+        }
+        if (ed == 0) return false;
+        exp10 += eneg ? -e : e;
+    }
+    if (i != n) return false;
+    static const double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                      1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+    if (sig <= 15 && exp10 >= -22 && exp10 <= 22) {
+        const double v = (double)m;
+        const double x = exp10 < 0 ? v / kPow10[-exp10] : v * kPow10[exp10];
+        *out = neg ? -x : x;
+        return true;
+    }
+    char buf[64];
+    if (n >= sizeof(buf)) return false;
+    memcpy(buf, t, n);
+    buf[n] = 0;
+    /* out of range: the stream's own answer differs from strtod's */
+    errno = 0;
+    const double x = strtod(buf, nullptr);
+    if (errno == ERANGE) return false;
+    *out = x;
+    return true;
+}
+
+/* A dbSNP row "chr pos hapmap validated indel fA fC fT fG ..." whose fields
+ * all have their plain form (pos digits, flags 0 or 1, frequencies plain
+ * decimals, no whitespace but spaces, tabs and CR) gives what the stream
+ * extraction gives; false leaves the row to that extraction. */
+bool parse_snp_row(const char* p, const char* e, std::string* name, size_t* pos, bool* flag, double* f) {
+    for (const char* q = p; q < e; ++q)
+        if (isspace((unsigned char)*q) && *q != ' ' && *q != '\t' && *q != '\r') return false;
+    const char* tok;
+    size_t n;
+    if (!next_token(p, e, &tok, &n)) return false;
+    name->assign(tok, n);
+    if (!next_token(p, e, &tok, &n) || n > 18) return false;
+    size_t v = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (!isdigit((unsigned char)tok[i])) return false;
+        v = v * 10 + (size_t)(tok[i] - '0');
+    }
+    *pos = v;
+    for (int k = 0; k < 3; ++k) {
+        if (!next_token(p, e, &tok, &n) || n != 1 || (tok[0] != '0' && tok[0] != '1')) return false;
+        flag[k] = tok[0] == '1';
+    }
+    for (int k = 0; k < 4; ++k) {
+        double x;
+        if (!next_token(p, e, &tok, &n) || !plain_decimal(tok, n, &x)) return false;
+        f[k] = x;
+    }
+    return true;
+}
+
+/* The known-SNP rows (cpp/chromosome.cc:207-221).  The name, the position
+ * and the SNP fields live across rows there: a field that fails to parse
+ * leaves it and the fields after it as the previous row left them (a blank
+ * row repeats the previous row at the position before it). */
 void load_dbsnp(const std::string& path, std::map<std::string, Chromosome>* chrs) {
-    std::ifstream in(path);
-    if (!in) die("No such file or directory:" + path, 1);
-    std::string line;
+    const MappedFile file(path);
+    const char* p = file.data;
+    const char* const end = file.data + file.size;
     bool hapmap = false, validated = false, indel = false;
     double f[4] = {0, 0, 0, 0};
-    while (std::getline(in, line)) {
-        std::istringstream s(line);
-        std::string name;
-        std::string::size_type pos = 0;
-        s >> name >> pos;
-        s >> hapmap >> validated >> indel >> f[0] >> f[1] >> f[2] >> f[3];
-        auto it = chrs->find(name);
-        if (it == chrs->end()) continue;
+    std::string name;
+    std::string::size_type pos = 0;
+    auto last = chrs->end();
+    while (p < end) {
+        const char* eol = (const char*)memchr(p, '\n', (size_t)(end - p));
+        if (!eol) eol = end;
+        bool flag[3];
+        if (parse_snp_row(p, eol, &name, &pos, flag, f)) {
+            hapmap = flag[0];
+            validated = flag[1];
+            indel = flag[2];
+        } else {
+            /* the stream extraction itself */
+            std::istringstream s(std::string(p, (size_t)(eol - p)));
+            s >> name >> pos;
+            s >> hapmap >> validated >> indel >> f[0] >> f[1] >> f[2] >> f[3];
+        }
+        p = eol + 1;
+        if (last == chrs->end() || last->first != name) last = chrs->find(name);
+        if (last == chrs->end()) continue;
         pos -= 1;
-        Chromosome& c = it->second;
+        Chromosome& c = last->second;
         if (pos >= c.codes.size()) continue;
         gsnp_snp r{};
         r.pos = (uint32_t)pos;
@@ -196,7 +366,16 @@ void load_dbsnp(const std::string& path, std::map<std::string, Chromosome>* chrs
         r.hapmap = hapmap;
         r.indel = indel;
         for (int i = 0; i < 4; ++i) r.freq[i] = f[i];
-        if (c.snp.emplace((uint32_t)pos, r).second) c.codes[pos] |= 8;
+        c.snp.push_back(r);
+        c.codes[pos] |= 8;
+    }
+    /* the rows of each chromosome by position; where a position repeats, its
+     * first row counts, as the first insertion into the reference's map */
+    for (auto& kv : *chrs) {
+        std::vector<gsnp_snp>& v = kv.second.snp;
+        std::stable_sort(v.begin(), v.end(), [](const gsnp_snp& x, const gsnp_snp& y) { return x.pos < y.pos; });
+        v.erase(std::unique(v.begin(), v.end(), [](const gsnp_snp& x, const gsnp_snp& y) { return x.pos == y.pos; }),
+                v.end());
     }
 }
 
@@ -244,28 +423,6 @@ size_t count_lines(const char* b, const char* e) {
         b = nl + 1;
     }
     return n;
-}
-
-bool next_token(const char*& p, const char* end, const char** tok, size_t* len) {
-    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
-    if (p >= end) return false;
-    *tok = p;
-    while (p < end && *p != ' ' && *p != '\t' && *p != '\r') ++p;
-    *len = (size_t)(p - *tok);
-    return true;
-}
-
-bool to_int(const char* t, size_t n, int* v) {
-    char buf[32];
-    if (n == 0 || n >= sizeof(buf)) return false;
-    memcpy(buf, t, n);
-    buf[n] = 0;
-    char* e = nullptr;
-    errno = 0;
-    const long x = strtol(buf, &e, 10);
-    if (e == buf || errno) return false;
-    *v = (int)x;
-    return true;
 }
 
 /* Parse the lines of chunk c into rows c->first, c->first + 1, ... of out;
@@ -489,8 +646,7 @@ int main(int argc, char** argv) {
     gsnp_context* ctx = nullptr;
     if (gsnp_context_create(0, &ctx) != GSNP_OK) die("!!!ERROR: no CUDA device");
     std::vector<gsnp_snp> snp;
-    snp.reserve(chr.snp.size());
-    for (const auto& kv : chr.snp) snp.push_back(kv.second);
+    snp.assign(chr.snp.begin(), chr.snp.end());
     check(ctx, gsnp_load_reference(ctx, chr.codes.data(), (int64_t)chr.codes.size(), snp.data(), (int64_t)snp.size()),
           "reference");
 

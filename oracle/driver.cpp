@@ -113,11 +113,14 @@ void load_genome(std::ifstream& fasta, std::ifstream* known_snp, Genome* g) {
     }
     if (seq.length() != 0 && g->chr.find(current) != g->chr.end()) g->chr[current].binarize(seq);
     if (known_snp && *known_snp) {
+        /* the name, the position and the SNP fields live across rows, as
+         * there (:207-210): a field that fails to parse keeps the previous
+         * row's value */
         SnpInfo form;
+        std::string name;
+        std::string::size_type pos = 0;
         for (std::string buff; std::getline(*known_snp, buff);) {
             std::istringstream s(buff);
-            std::string name;
-            std::string::size_type pos = 0;
             s >> name >> pos;
             s >> form.hapmap >> form.validated >> form.indel >> form.freq[0] >> form.freq[1] >> form.freq[2] >> form.freq[3];
             auto it = g->chr.find(name);

@@ -79,3 +79,20 @@ def test_cli_matrix_input_and_fp64_form(tmp_path, oracle_bin, native_lib):
     assert r1.returncode == 0, r1.stderr
     del ref["mat"]
     compare("c1 -I", got, ref)
+
+
+@pytest.mark.gpu
+def test_cli_irregular_reference_files(tmp_path, oracle_bin, native_lib):
+    """Known-SNP rows that do not parse, blank rows, repeated positions and a
+    repeated chromosome name with no sequence (malformed_inputs.py), read as
+    the reference reads them (cpp/chromosome.cc:172-221)."""
+    from malformed_inputs import corrupt_workload_inputs
+    w = synth.make_workload("c1", scale=0.004)
+    paths = synth.write_inputs(w, str(tmp_path))
+    corrupt_workload_inputs(paths, w.chr_name, w.genome_len, seed=11)
+    flags = flags_for(w, paths)
+    r0, ref = run(oracle_bin, paths, flags, str(tmp_path / "oracle"))
+    assert r0.returncode == 0, r0.stderr
+    r1, got = run(build.CLI, paths, flags, str(tmp_path / "gsnp"))
+    assert r1.returncode == 0, r1.stderr
+    compare("c1 irregular reference files", got, ref)

@@ -52,6 +52,23 @@ def test_restated_driver_matches_reference_host(name, scale, compress, tmp_path,
         assert a[f] == b[f], f
 
 
+def test_irregular_reference_files_match_reference_host(tmp_path, ref_bin, oracle_bin):
+    """Known-SNP rows that do not parse, blank rows, repeated positions and a
+    repeated chromosome name with no sequence (malformed_inputs.py): the
+    reference's loader keeps its name, position and SNP fields across rows
+    (cpp/chromosome.cc:207-221)."""
+    from malformed_inputs import corrupt_workload_inputs
+    w = synth.make_workload("c1", scale=0.002)
+    paths = synth.write_inputs(w, str(tmp_path))
+    corrupt_workload_inputs(paths, w.chr_name, w.genome_len, seed=11)
+    flags = [f for f in w.cli_flags(paths.get("dbsnp")) if f != "-C"]
+    a = run(ref_bin, paths, flags, str(tmp_path / "ref"))
+    b = run(oracle_bin, paths, flags, str(tmp_path / "oracle"))
+    assert sorted(a) == sorted(b)
+    for f in a:
+        assert a[f] == b[f], f
+
+
 def test_matrix_file_matches_reference_host(tmp_path, ref_bin, oracle_bin):
     w = synth.make_workload("c0", scale=0.03)
     paths = synth.write_inputs(w, str(tmp_path))
