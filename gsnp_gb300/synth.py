@@ -12,6 +12,11 @@ caller is measured on:
   c4  250 Mbp genome, one 3 Mbp N block, 100 bp reads at 40x, rare runs of
       5 low-quality cycles
 
+and one more shape for parity tests only:
+
+  c5  c1 with long reads, 150/200/250 bp under -L 250: the widest read rows
+      and per-site dependency state the record layout allows
+
 Every random quantity is drawn from a counter-based SplitMix64 stream keyed by
 (seed, stream id, element index).  The draws therefore do not depend on numpy's
 Generator implementation or on how the work is chunked, and the same seed gives
@@ -113,6 +118,8 @@ CONFIGS: Dict[str, Config] = {
                  q_max_char="|"),
     "c4": Config("c4", 250_000_000, 40.0, [100], n_runs=[3_000_000], lowq_clusters=1e-4,
                  flags=["-L", "100", "-t", "-u", "-C"]),
+    "c5": Config("c5", 50_000_000, 30.0, [150, 200, 250], dbsnp_frac=0.01,
+                 flags=["-L", "250", "-t", "-u", "-2"]),
 }
 
 

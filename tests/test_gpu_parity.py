@@ -5,7 +5,8 @@ files, runs the same alignments through the C ABI (calibration, tables, whole
 chromosome call) and compares the cns text.  The shapes cover the window
 quirks: c4 has an N block longer than a window (gap windows, stale host
 counts), c2 has deep hotspots (record cap, deep tile bins) and mixed read
-lengths, c1/c3 carry dbSNP priors and c3 qualities up to 60.
+lengths, c1/c3 carry dbSNP priors and c3 qualities up to 60, c5 has reads of
+150-250 bp under -L 250 (the widest read rows and dependency state).
 """
 import os
 
@@ -16,7 +17,7 @@ from gsnp_gb300 import api, synth
 
 from oracle_run import first_diff, flags_for, oracle_outputs
 
-CASES = [("c0", 0.1), ("c1", 0.004), ("c2", 0.01), ("c3", 0.004), ("c4", 0.0101)]
+CASES = [("c0", 0.1), ("c1", 0.004), ("c2", 0.01), ("c3", 0.004), ("c4", 0.0101), ("c5", 0.004)]
 
 
 @pytest.mark.gpu
@@ -38,7 +39,8 @@ def test_cns_text_matches_oracle(name, scale, tmp_path, oracle_bin, native_lib):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name,scale", [("c0", 0.1), ("c1", 0.004), ("c2", 0.01), ("c3", 0.004), ("c4", 0.0101)])
+@pytest.mark.parametrize("name,scale", [("c0", 0.1), ("c1", 0.004), ("c2", 0.01), ("c3", 0.004), ("c4", 0.0101),
+                                        ("c5", 0.004)])
 def test_fp32_fixup_form_matches_oracle(name, scale, tmp_path, oracle_bin, native_lib):
     """FP32 compensated sums with FP64 recomputation near decision boundaries
     must give the same cns bytes as the FP64 form and the oracle."""

@@ -40,7 +40,7 @@ def run(exe, paths, flags, out_dir):
 
 @pytest.mark.parametrize("name,scale,compress", [
     ("c0", 0.05, False), ("c0", 0.05, True), ("c1", 0.002, False), ("c1", 0.002, True),
-    ("c2", 0.004, False), ("c3", 0.002, False), ("c4", 0.0101, False)])
+    ("c2", 0.004, False), ("c3", 0.002, False), ("c4", 0.0101, False), ("c5", 0.004, False)])
 def test_restated_driver_matches_reference_host(name, scale, compress, tmp_path, ref_bin, oracle_bin):
     w = synth.make_workload(name, scale=scale)
     paths = synth.write_inputs(w, str(tmp_path))
