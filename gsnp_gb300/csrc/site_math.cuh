@@ -5,12 +5,38 @@
  *
  * A site's records are 32-bit words in ascending order, `stride` words apart
  * (the tile kernels keep them in a [slot][site] column).
+ *
+ * Outside nvcc (the CPU checks of this arithmetic) the device intrinsics it
+ * uses are the host's own IEEE operations, each rounded to nearest like the
+ * _rn intrinsics; host code is built with -ffp-contract=off so that no
+ * multiply and add are fused.
  */
 #ifndef GSNP_SITE_MATH_CUH
 #define GSNP_SITE_MATH_CUH
 
 #include <math.h>
 #include <stdint.h>
+
+#if !defined(__CUDACC__)
+#include <string.h>
+
+#include <vector_types.h>   /* float4, double2 and the function qualifiers */
+#ifndef __noinline__
+#define __noinline__          /* only device code size depends on it */
+#endif
+static inline float __fadd_rn(float x, float y) { return x + y; }
+static inline float __fsub_rn(float x, float y) { return x - y; }
+static inline float __fmul_rn(float x, float y) { return x * y; }
+static inline int __float2int_rz(float x) { return (int)x; }
+static inline double __dsqrt_rn(double x) { return sqrt(x); }
+static inline long long __double_as_longlong(double x) {
+    long long v;
+    memcpy(&v, &x, sizeof v);
+    return v;
+}
+template <class T>
+static inline T __ldg(const T* p) { return *p; }
+#endif
 
 #include "calling.cuh"
 #include "column.cuh"
@@ -224,7 +250,7 @@ __device__ __noinline__ double rank_test(const double* p_rank, int q_max_min, co
      * q_max - q_min + 1 keep rank 0 as in the reference */
     double Ta = 0.0, Tb = 0.0;
     int rank = 0;
-    const int top = min(64, q_max_min + 1);
+    const int top = q_max_min + 1 < 64 ? q_max_min + 1 : 64;
     for (int q = 0; q <= top; ++q) {
         const int c = ca[q] + cb[q];
         /* an empty bin adds +0.0 to the non-negative sums: skipping it is
