@@ -6,7 +6,10 @@ before the failed one).
 The reference exits on these inputs: unsorted alignments with "Errors in
 sorting:<pos><<previous pos>" (cpp/call_genotype.cc:516-523), a read longer
 than -L and a base other than ACGT/acgt through its asserts
-(kernel/compress_kernel.cu:121-123).
+(kernel/compress_kernel.cu:121-123).  A site covered by more than 65535
+alignments is this build's capacity limit (its per-site counts are 16-bit):
+the kernels raise the device error word and the call returns
+GSNP_ERR_CAPACITY.
 """
 import numpy as np
 import pytest
@@ -15,7 +18,7 @@ from gsnp_gb300 import api, synth
 
 from oracle_run import flags_for
 
-GSNP_ERR_UNSORTED, GSNP_ERR_INPUT = 5, 6
+GSNP_ERR_CAPACITY, GSNP_ERR_UNSORTED, GSNP_ERR_INPUT = 4, 5, 6
 
 
 def bad_reads(w, kind):
@@ -31,6 +34,12 @@ def bad_reads(w, kind):
         seq[i, 3] = ord("X")
     elif kind == "no_position":
         pos[:] = -1
+    elif kind == "too_deep":
+        # 70,000 copies of one alignment, next to it in file order
+        rep = np.ones(len(pos), dtype=np.int64)
+        rep[i] = 70_000
+        pos, length, hit, strand = (np.repeat(x, rep) for x in (pos, length, hit, strand))
+        seq, qual = np.repeat(seq, rep, axis=0), np.repeat(qual, rep, axis=0)
     return pos, length, hit, strand, seq, qual
 
 
@@ -38,7 +47,8 @@ def bad_reads(w, kind):
 @pytest.mark.parametrize("kind,code,text", [("unsorted", GSNP_ERR_UNSORTED, "Errors in sorting:"),
                                             ("too_long", GSNP_ERR_INPUT, "longer than -L"),
                                             ("bad_base", GSNP_ERR_INPUT, "unknown base"),
-                                            ("no_position", GSNP_ERR_INPUT, "non-negative position")])
+                                            ("no_position", GSNP_ERR_INPUT, "non-negative position"),
+                                            ("too_deep", GSNP_ERR_CAPACITY, "more than 65535 alignments")])
 @pytest.mark.parametrize("into", [False, True])
 def test_input_error_then_valid_call(kind, code, text, into, native_lib, monkeypatch):
     monkeypatch.setenv("GSNP_SEGMENTS", "4")
