@@ -1167,7 +1167,13 @@ int gsnp_context_create(int device, gsnp_context** out) {
 void gsnp_context_destroy(gsnp_context* c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    /* every stream finished before any buffer it may use is freed */
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < gsnp_context::kBinStreams; ++i)
+        if (c->bin_stream[i]) cudaStreamSynchronize(c->bin_stream[i]);
+    if (c->gather_stream) cudaStreamSynchronize(c->gather_stream);
+    if (c->up_stream) cudaStreamSynchronize(c->up_stream);
+    if (c->down_stream) cudaStreamSynchronize(c->down_stream);
     free_all(c);
     if (c->h_text) cudaFreeHost(c->h_text);
     for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i)
