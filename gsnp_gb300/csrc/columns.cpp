@@ -25,9 +25,11 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "dict.h"
@@ -57,7 +59,84 @@ struct Files {
 
 /* dict.cu's codec on the host: dict = the distinct values ascending (-0.0
  * and +0.0 one entry, -0.0 when any -0.0 occurs), words = each value's index
- * packed MSB-first, floor(32 / bits) per word, the last word right-aligned */
+ * packed MSB-first, floor(32 / bits) per word, the last word right-aligned.
+ * The distinct values and each input's index come from a presence table over
+ * the value range for integers of a narrow range (qualities, counts, depths,
+ * run lengths: one pass each, no sort), from a hash table of the distinct
+ * values otherwise; both give the indices the sorted dictionary's
+ * lower_bound gives. */
+template <class T>
+bool pack_indices(const uint32_t* idx, size_t n, unsigned long d, uint32_t* words, unsigned long* n_words,
+                  std::string* err) {
+    const int bits = dict_bits(d);
+    const size_t per = (size_t)floor(32 / (double)bits);
+    const size_t nw = (size_t)ceil(n / (double)per);
+    if (*n_words < nw) {
+        *err = "numWordOutData < numWordCompressed";
+        return false;
+    }
+    for (size_t w = 0; w < nw; ++w) {
+        const size_t first = w * per, cnt = (w == nw - 1) ? n - first : per;
+        uint32_t out = 0;
+        for (size_t i = 0; i < cnt; ++i) out = (out << bits) | idx[first + i];
+        words[w] = out;
+    }
+    *n_words = (unsigned long)nw;
+    return true;
+}
+
+/* integer values within [lo, lo + span): indices through a dense table */
+template <class T>
+void dense_dict(const T* in, size_t n, int64_t lo, size_t span, std::vector<T>* d, std::vector<uint32_t>* idx) {
+    thread_local std::vector<uint32_t> slot;
+    if (slot.size() < span) slot.resize(span);
+    std::fill(slot.begin(), slot.begin() + (ptrdiff_t)span, 0u);
+    for (size_t i = 0; i < n; ++i) slot[(size_t)((int64_t)in[i] - lo)] = 1u;
+    d->clear();
+    for (size_t v = 0; v < span; ++v)
+        if (slot[v]) {
+            slot[v] = (uint32_t)d->size();
+            d->push_back((T)((int64_t)v + lo));
+        }
+    idx->resize(n);
+    for (size_t i = 0; i < n; ++i) (*idx)[i] = slot[(size_t)((int64_t)in[i] - lo)];
+}
+
+/* any values: distinct values through an open-addressing table of their
+ * bit patterns (+0.0 standing for both zeros), sorted, then indexed */
+template <class T>
+void hashed_dict(const T* in, size_t n, std::vector<T>* d, std::vector<uint32_t>* idx) {
+    static_assert(sizeof(T) <= 8, "values of at most 64 bits");
+    auto key = [](T v) {
+        uint64_t k = 0;
+        if (v == (T)0) v = (T)0;   /* -0.0 and +0.0: one key */
+        memcpy(&k, &v, sizeof(T));
+        return k;
+    };
+    size_t cap = 64;
+    while (cap < 2 * n) cap <<= 1;
+    std::vector<uint64_t> keys(cap);
+    std::vector<uint32_t> val(cap, 0xffffffffu);
+    auto find = [&](uint64_t k) {
+        size_t h = (size_t)((k * 0x9e3779b97f4a7c15ull) >> 17) & (cap - 1);
+        while (val[h] != 0xffffffffu && keys[h] != k) h = (h + 1) & (cap - 1);
+        return h;
+    };
+    d->clear();
+    for (size_t i = 0; i < n; ++i) {
+        const size_t h = find(key(in[i]));
+        if (val[h] == 0xffffffffu) {
+            keys[h] = key(in[i]);
+            val[h] = 0;
+            d->push_back(in[i] == (T)0 ? (T)0 : in[i]);
+        }
+    }
+    std::sort(d->begin(), d->end());
+    for (size_t r = 0; r < d->size(); ++r) val[find(key((*d)[r]))] = (uint32_t)r;
+    idx->resize(n);
+    for (size_t i = 0; i < n; ++i) (*idx)[i] = val[find(key(in[i]))];
+}
+
 template <class T>
 bool host_dict(const T* in, size_t n, uint32_t* words, unsigned long* n_words, T* dict, unsigned long* n_dict,
                std::string* err) {
@@ -70,34 +149,32 @@ bool host_dict(const T* in, size_t n, uint32_t* words, unsigned long* n_words, T
         *n_words = 0;
         return true;
     }
-    std::vector<T> d(in, in + n);
-    std::sort(d.begin(), d.end());
-    d.erase(std::unique(d.begin(), d.end()), d.end());
+    thread_local std::vector<T> d;
+    thread_local std::vector<uint32_t> idx;
+    bool dense = false;
+    if (std::is_integral<T>::value) {
+        int64_t lo = (int64_t)in[0], hi = lo;
+        for (size_t i = 1; i < n; ++i) {
+            lo = std::min<int64_t>(lo, (int64_t)in[i]);
+            hi = std::max<int64_t>(hi, (int64_t)in[i]);
+        }
+        const uint64_t span = (uint64_t)(hi - lo) + 1;
+        if (span <= std::max<uint64_t>(1u << 16, 4 * (uint64_t)n) && span <= (1u << 24)) {
+            dense_dict(in, n, lo, (size_t)span, &d, &idx);
+            dense = true;
+        }
+    }
+    if (!dense) hashed_dict(in, n, &d, &idx);
+    /* the zero entry is -0.0 when any input is -0.0 */
     for (T& v : d)
-        if (v == (T)0) {
+        if (v == (T)0 && std::is_floating_point<T>::value) {
             bool neg = false;
             for (size_t i = 0; i < n && !neg; ++i) neg = in[i] == (T)0 && std::signbit((double)in[i]);
             v = neg ? (T)(-0.0) : (T)0;
         }
-    const int bits = dict_bits((unsigned long)d.size());
-    const size_t per = (size_t)floor(32 / (double)bits);
-    const size_t nw = (size_t)ceil(n / (double)per);
-    if (*n_words < nw) {
-        *err = "numWordOutData < numWordCompressed";
-        return false;
-    }
-    for (size_t w = 0; w < nw; ++w) {
-        const size_t first = w * per, cnt = (w == nw - 1) ? n - first : per;
-        uint32_t out = 0;
-        for (size_t i = 0; i < cnt; ++i) {
-            const uint32_t idx = (uint32_t)(std::lower_bound(d.begin(), d.end(), in[first + i]) - d.begin());
-            out = (out << bits) | idx;
-        }
-        words[w] = out;
-    }
+    if (!pack_indices<T>(idx.data(), n, (unsigned long)d.size(), words, n_words, err)) return false;
     std::copy(d.begin(), d.end(), dict);
     *n_dict = (unsigned long)d.size();
-    *n_words = (unsigned long)nw;
     return true;
 }
 
@@ -128,7 +205,7 @@ std::vector<uint32_t> pack2(const std::vector<char>& c) {
 template <class T>
 unsigned rle(std::vector<T>& data, std::vector<uint32_t>& runs) {
     const size_t n = data.size();
-    runs.assign(n, 0);
+    runs.resize(n);
     if (n == 0) return 0;
     size_t r = 0, start = 0;
     for (size_t i = 1; i <= n; ++i)
@@ -205,11 +282,13 @@ private:
     /* one column of Column_RLEDict (cpp/compress.h:495-868) */
     template <class T>
     bool rle_dict(std::vector<T>& col, std::string* err) {
-        std::vector<uint32_t> runlen;
+        /* per-thread buffers: every entry read back is written first */
+        thread_local std::vector<uint32_t> runlen, cval, clen, dlen;
+        thread_local std::vector<T> dval;
         const unsigned runs = rle(col, runlen);
-        std::vector<uint32_t> cval(runs + 1), clen(runs + 1);
-        std::vector<T> dval(runs + 1);
-        std::vector<uint32_t> dlen(runs + 1);
+        for (std::vector<uint32_t>* v : {&cval, &clen, &dlen})
+            if (v->size() < runs + 1) v->resize(runs + 1);
+        if (dval.size() < runs + 1) dval.resize(runs + 1);
         unsigned long nwv = runs, ndv = kDictCap, nwl = runs, ndl = kDictCap;
         if (!dict_.compress(col.data(), runs, cval.data(), &nwv, dval.data(), &ndv, err)) return false;
         if (!dict_.compress(runlen.data(), runs, clen.data(), &nwl, dlen.data(), &ndl, err)) return false;
@@ -226,28 +305,25 @@ private:
         const int flag = all_n ? 1 : 0;
         f_.put(f_.frle, &flag, sizeof(int));
         if (flag) return true;
+        /* the six columns in one pass over the rows, then each encoded */
         const size_t n = rows.size();
-        std::vector<int> col(n);
-        std::vector<double> dcol(n);
-        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].q_cns : 0;
-        if (!rle_dict(col, err)) return false;
-        col.resize(n);
-        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].avg1 : 0;
-        if (!rle_dict(col, err)) return false;
-        col.resize(n);
-        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].cu1 : 0;
-        if (!rle_dict(col, err)) return false;
-        col.resize(n);
-        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? rows[j].ca1 : 0;
-        if (!rle_dict(col, err)) return false;
-        col.resize(n);
-        for (size_t j = 0; j < n; ++j) col[j] = rows[j].called() ? (int)rows[j].depth : 0;
-        if (!rle_dict(col, err)) return false;
+        thread_local std::vector<int> c5, c7, c8, c9, c14;
+        thread_local std::vector<double> c16;
+        for (std::vector<int>* v : {&c5, &c7, &c8, &c9, &c14}) v->resize(n);
+        c16.resize(n);
         for (size_t j = 0; j < n; ++j) {
             const CnsRow& r = rows[j];
-            dcol[j] = r.called() ? (r.depth == 0 ? 255 : (double)r.repeat / r.depth) : 255.0;
+            const bool called = r.called();
+            c5[j] = called ? r.q_cns : 0;
+            c7[j] = called ? r.avg1 : 0;
+            c8[j] = called ? r.cu1 : 0;
+            c9[j] = called ? r.ca1 : 0;
+            c14[j] = called ? (int)r.depth : 0;
+            c16[j] = called ? (r.depth == 0 ? 255 : (double)r.repeat / r.depth) : 255.0;
         }
-        return rle_dict(dcol, err);
+        for (std::vector<int>* v : {&c5, &c7, &c8, &c9, &c14})
+            if (!rle_dict(*v, err)) return false;
+        return rle_dict(c16, err);
     }
 
     /* Column_10 (cpp/compress.h:759-897) */
@@ -299,9 +375,9 @@ private:
         f_.put(f_.f111213, e13id.data(), 4 * e13id.size());
         f_.put(f_.f111213, e13.data(), 4 * e13.size());
         f_.put(f_.f111213, cid.data(), 4 * cid.size());
+        thread_local std::vector<uint32_t> words(kWin);
+        thread_local std::vector<int> dict(kWin);
         for (std::vector<int>* v : {&c11, &c12, &c13}) {
-            std::vector<uint32_t> words(kWin);
-            std::vector<int> dict(kWin);
             unsigned long dp[2] = {(unsigned long)kWin, (unsigned long)kWin};
             if (!dict_.compress(v->data(), v->size(), words.data(), &dp[0], dict.data(), &dp[1], err)) return false;
             f_.put(f_.f111213, dp, sizeof(dp));
@@ -317,20 +393,21 @@ private:
         f_.put(f_.f1517, &flag, sizeof(int));
         if (flag) return;
         const size_t n = rows.size();
-        std::vector<int> id;
+        std::vector<int> id, snp;
         std::vector<double> val;
-        for (size_t j = 0; j < n; ++j)
-            if (rows[j].called() && rows[j].rank_sum != 1.0) { id.push_back((int)j); val.push_back(rows[j].rank_sum); }
+        for (size_t j = 0; j < n; ++j) {
+            const CnsRow& r = rows[j];
+            if (!r.called()) continue;
+            if (r.rank_sum != 1.0) { id.push_back((int)j); val.push_back(r.rank_sum); }
+            if (r.ori & 8) snp.push_back((int)j);
+        }
         int cnt = (int)id.size();
         f_.put(f_.f1517, &cnt, sizeof(int));
         f_.put(f_.f1517, id.data(), 4 * id.size());
         f_.put(f_.f1517, val.data(), 8 * val.size());
-        id.clear();
-        for (size_t j = 0; j < n; ++j)
-            if (rows[j].called() && (rows[j].ori & 8)) id.push_back((int)j);
-        cnt = (int)id.size();
+        cnt = (int)snp.size();
         f_.put(f_.f1517, &cnt, sizeof(int));
-        f_.put(f_.f1517, id.data(), 4 * id.size());
+        f_.put(f_.f1517, snp.data(), 4 * snp.size());
     }
 };
 
@@ -370,13 +447,27 @@ int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* 
         for (int64_t w = 0; w < plan.n_windows; ++w)
             fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1),
                     (unsigned long)plan.call_len[w]);
-        /* windows in batches: encoded in parallel, written in order */
+        /* windows in batches: encoded in parallel, written in order by one
+         * writer thread while the next batch is encoded (two buffer sets) */
         const int nt = std::max(1, threads);
         const size_t batch = (size_t)nt * 2;
-        std::vector<Files> out(batch);
+        std::vector<Files> out[2] = {std::vector<Files>(batch), std::vector<Files>(batch)};
         std::vector<std::string> errs(batch);
-        for (int64_t w0 = 0; w0 < plan.n_windows && rc == 0; w0 += (int64_t)batch) {
+        std::thread writer;
+        std::atomic<bool> write_ok(true);
+        auto write_batch = [&](int set, size_t k) {
+            for (size_t i = 0; i < k; ++i) {
+                const Files& o = out[set][i];
+                const std::string* parts[5] = {&o.f346, &o.frle, &o.f10, &o.f111213, &o.f1517};
+                for (int f = 0; f < 5; ++f)
+                    if (!parts[f]->empty() && fwrite(parts[f]->data(), 1, parts[f]->size(), fb[f]) != parts[f]->size())
+                        write_ok = false;
+            }
+        };
+        int set = 0;
+        for (int64_t w0 = 0; w0 < plan.n_windows && rc == 0; w0 += (int64_t)batch, set ^= 1) {
             const size_t k = (size_t)std::min<int64_t>((int64_t)batch, plan.n_windows - w0);
+            std::vector<Files>& cur = out[set];
             std::atomic<size_t> next(0);
             std::atomic<bool> ok(true);
             auto work = [&]() {
@@ -386,8 +477,8 @@ int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* 
                     const int64_t len = plan.call_len[w];
                     rows.resize((size_t)len);
                     for (int64_t j = 0; j < len; ++j) rows[(size_t)j] = resolve_row(plan, w, j, codes, calls, counts);
-                    out[i].clear();
-                    Writer wr(dict, out[i]);
+                    cur[i].clear();
+                    Writer wr(dict, cur[i]);
                     if (!wr.window(rows, &errs[i])) ok = false;
                 }
             };
@@ -395,6 +486,8 @@ int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* 
             for (int t = 1; t < std::min<int>(nt, (int)k); ++t) pool.emplace_back(work);
             work();
             for (auto& th : pool) th.join();
+            /* the previous batch's writes end before this batch's follow */
+            if (writer.joinable()) writer.join();
             if (!ok) {
                 for (const std::string& e : errs)
                     if (!e.empty()) {
@@ -405,15 +498,13 @@ int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* 
                 rc = 1;
                 break;
             }
-            for (size_t i = 0; i < k && rc == 0; ++i) {
-                const std::string* parts[5] = {&out[i].f346, &out[i].frle, &out[i].f10, &out[i].f111213,
-                                               &out[i].f1517};
-                for (int f = 0; f < 5; ++f)
-                    if (!parts[f]->empty() && fwrite(parts[f]->data(), 1, parts[f]->size(), fb[f]) != parts[f]->size()) {
-                        *err = "write failed";
-                        rc = 1;
-                    }
-            }
+            if (!write_ok) break;
+            writer = std::thread(write_batch, set, k);
+        }
+        if (writer.joinable()) writer.join();
+        if (rc == 0 && !write_ok) {
+            *err = "write failed";
+            rc = 1;
         }
     } else if (rc == 0) {
         /* text mode: the column files exist and are empty, the table says 0 windows */
