@@ -28,6 +28,8 @@
 #include <cstddef>
 #include <cstring>
 #include <string>
+#include <condition_variable>
+#include <mutex>
 #include <thread>
 #include <type_traits>
 #include <vector>
@@ -447,63 +449,79 @@ int write_columns(const WindowPlan& plan, const uint8_t* codes, const SiteCall* 
         for (int64_t w = 0; w < plan.n_windows; ++w)
             fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1),
                     (unsigned long)plan.call_len[w]);
-        /* windows in batches: encoded in parallel, written in order by one
-         * writer thread while the next batch is encoded (two buffer sets) */
+        /* windows encoded by persistent workers, taken in order from a
+         * counter, at most `ahead` windows beyond the last one written; one
+         * writer thread writes them in window order and frees each block */
         const int nt = std::max(1, threads);
-        const size_t batch = (size_t)nt * 2;
-        std::vector<Files> out[2] = {std::vector<Files>(batch), std::vector<Files>(batch)};
-        std::vector<std::string> errs(batch);
-        std::thread writer;
-        std::atomic<bool> write_ok(true);
-        auto write_batch = [&](int set, size_t k) {
-            for (size_t i = 0; i < k; ++i) {
-                const Files& o = out[set][i];
-                const std::string* parts[5] = {&o.f346, &o.frle, &o.f10, &o.f111213, &o.f1517};
-                for (int f = 0; f < 5; ++f)
-                    if (!parts[f]->empty() && fwrite(parts[f]->data(), 1, parts[f]->size(), fb[f]) != parts[f]->size())
-                        write_ok = false;
+        const int64_t nwin = plan.n_windows;
+        const int64_t ahead = 4 * (int64_t)nt;
+        std::vector<Files> out((size_t)nwin);
+        std::vector<uint8_t> done((size_t)nwin, 0);
+        std::mutex m;
+        std::condition_variable cv_done, cv_written;
+        int64_t written = 0;
+        bool failed = false;
+        std::string first_err;
+        std::atomic<int64_t> next(0);
+        auto fail_with = [&](const std::string& e) {
+            std::lock_guard<std::mutex> g(m);
+            if (!failed) first_err = e;
+            failed = true;
+            cv_done.notify_all();
+            cv_written.notify_all();
+        };
+        auto work = [&]() {
+            std::vector<CnsRow> rows;
+            std::string e;
+            for (int64_t w; (w = next.fetch_add(1)) < nwin;) {
+                {
+                    std::unique_lock<std::mutex> g(m);
+                    cv_written.wait(g, [&] { return failed || w < written + ahead; });
+                    if (failed) return;
+                }
+                const int64_t len = plan.call_len[w];
+                rows.resize((size_t)len);
+                for (int64_t j = 0; j < len; ++j) rows[(size_t)j] = resolve_row(plan, w, j, codes, calls, counts);
+                Writer wr(dict, out[(size_t)w]);
+                if (!wr.window(rows, &e)) {
+                    fail_with(e.empty() ? std::string("write failed") : e);
+                    return;
+                }
+                std::lock_guard<std::mutex> g(m);
+                done[(size_t)w] = 1;
+                cv_done.notify_all();
             }
         };
-        int set = 0;
-        for (int64_t w0 = 0; w0 < plan.n_windows && rc == 0; w0 += (int64_t)batch, set ^= 1) {
-            const size_t k = (size_t)std::min<int64_t>((int64_t)batch, plan.n_windows - w0);
-            std::vector<Files>& cur = out[set];
-            std::atomic<size_t> next(0);
-            std::atomic<bool> ok(true);
-            auto work = [&]() {
-                std::vector<CnsRow> rows;
-                for (size_t i; (i = next.fetch_add(1)) < k;) {
-                    const int64_t w = w0 + (int64_t)i;
-                    const int64_t len = plan.call_len[w];
-                    rows.resize((size_t)len);
-                    for (int64_t j = 0; j < len; ++j) rows[(size_t)j] = resolve_row(plan, w, j, codes, calls, counts);
-                    cur[i].clear();
-                    Writer wr(dict, cur[i]);
-                    if (!wr.window(rows, &errs[i])) ok = false;
+        auto write_all = [&]() {
+            for (int64_t w = 0; w < nwin; ++w) {
+                {
+                    std::unique_lock<std::mutex> g(m);
+                    cv_done.wait(g, [&] { return failed || done[(size_t)w]; });
+                    if (failed) return;
                 }
-            };
-            std::vector<std::thread> pool;
-            for (int t = 1; t < std::min<int>(nt, (int)k); ++t) pool.emplace_back(work);
-            work();
-            for (auto& th : pool) th.join();
-            /* the previous batch's writes end before this batch's follow */
-            if (writer.joinable()) writer.join();
-            if (!ok) {
-                for (const std::string& e : errs)
-                    if (!e.empty()) {
-                        *err = e;
-                        break;
+                Files& o = out[(size_t)w];
+                std::string* parts[5] = {&o.f346, &o.frle, &o.f10, &o.f111213, &o.f1517};
+                for (int f = 0; f < 5; ++f) {
+                    if (!parts[f]->empty() &&
+                        fwrite(parts[f]->data(), 1, parts[f]->size(), fb[f]) != parts[f]->size()) {
+                        fail_with("write failed");
+                        return;
                     }
-                if (err->empty()) *err = "write failed";
-                rc = 1;
-                break;
+                    std::string().swap(*parts[f]);
+                }
+                std::lock_guard<std::mutex> g(m);
+                written = w + 1;
+                cv_written.notify_all();
             }
-            if (!write_ok) break;
-            writer = std::thread(write_batch, set, k);
-        }
-        if (writer.joinable()) writer.join();
-        if (rc == 0 && !write_ok) {
-            *err = "write failed";
+        };
+        std::thread writer(write_all);
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+        work();
+        for (auto& th : pool) th.join();
+        writer.join();
+        if (failed) {
+            *err = first_err;
             rc = 1;
         }
     } else if (rc == 0) {
