@@ -151,11 +151,30 @@ struct Chromosome {
     std::vector<gsnp_snp> snp;    /* by position, the first row of each position */
 };
 
+inline bool is_sep(char c) { return c == ' ' || c == '\t' || c == '\r'; }
+
+/* The first space, tab or CR in [p, end).  Eight bytes at a time while none
+ * of them is one (a byte equal to x makes (w ^ x-bytes) have a zero byte,
+ * which (v - 0x01..) & ~v & 0x80.. detects exactly), then byte by byte. */
+inline const char* find_sep(const char* p, const char* end) {
+    auto has_zero = [](uint64_t v) { return (v - 0x0101010101010101ull) & ~v & 0x8080808080808080ull; };
+    while (end - p >= 8) {
+        uint64_t w;
+        memcpy(&w, p, 8);
+        if (has_zero(w ^ 0x2020202020202020ull) | has_zero(w ^ 0x0909090909090909ull) |
+            has_zero(w ^ 0x0d0d0d0d0d0d0d0dull))
+            break;
+        p += 8;
+    }
+    while (p < end && !is_sep(*p)) ++p;
+    return p;
+}
+
 bool next_token(const char*& p, const char* end, const char** tok, size_t* len) {
-    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    while (p < end && is_sep(*p)) ++p;
     if (p >= end) return false;
     *tok = p;
-    while (p < end && *p != ' ' && *p != '\t' && *p != '\r') ++p;
+    p = find_sep(p, end);
     *len = (size_t)(p - *tok);
     return true;
 }
