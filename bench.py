@@ -30,6 +30,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -370,6 +371,24 @@ def main():
             text_ms = []
             break
 
+    # ---- the -C files of the last call, informational ----
+    columns = None
+    cdir = tempfile.mkdtemp(prefix="gsnp_bench_columns_")
+    try:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        rc = caller.lib.gsnp_write_columns(caller.ctx, w.chr_name.encode(), os.path.join(cdir, "cns").encode())
+        ms = (time.perf_counter() - t1) * 1e3
+        files = [os.path.join(cdir, f) for f in os.listdir(cdir)]
+        columns = ({"ms": round(ms, 2), "bytes": sum(os.path.getsize(f) for f in files), "files": len(files),
+                    "note": "gsnp_write_columns of the last call: download, window encoding on the host threads, "
+                            "write to a temporary directory"}
+                   if rc == 0 else {"error": "gsnp_write_columns returned %d" % rc})
+    except Exception as e:   # informational only: never costs the bench line
+        columns = {"error": repr(e)[:200]}
+    finally:
+        shutil.rmtree(cdir, ignore_errors=True)
+
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
     bsite = site_bytes(w)
@@ -415,6 +434,7 @@ def main():
             "cns_text": ({"ms": round(min(text_ms), 2), "rows": sites,
                           "note": "gsnp_write_cns of the last call to the null device: GPU formatting, download, write"}
                          if text_ms else None),
+            "cns_columns": columns,
             "gpu_launches": head["launches"] * args.steps,
             "kernels_ms": kernel_table(kernel_ms),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

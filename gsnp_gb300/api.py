@@ -82,6 +82,7 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_call_chromosome": (ctypes.c_int, [_P, ctypes.POINTER(Reads)]),
         "gsnp_call_chromosome_into": (ctypes.c_int, [_P, ctypes.POINTER(Reads), _P]),
         "gsnp_write_cns": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p]),
+        "gsnp_write_columns": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p]),
         "gsnp_recall_resident": (ctypes.c_int, [_P]),
         "gsnp_fetch_sites": (ctypes.c_int, [_P, _I64, _I64, _P]),
         "gsnp_format_cns": (ctypes.c_int, [_P, ctypes.c_char_p, _P, ctypes.POINTER(_I64)]),
