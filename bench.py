@@ -373,8 +373,9 @@ def main():
 
     # ---- the -C files of the last call, informational ----
     columns = None
-    cdir = tempfile.mkdtemp(prefix="gsnp_bench_columns_")
+    cdir = None
     try:
+        cdir = tempfile.mkdtemp(prefix="gsnp_bench_columns_")
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         rc = caller.lib.gsnp_write_columns(caller.ctx, w.chr_name.encode(), os.path.join(cdir, "cns").encode())
@@ -387,7 +388,8 @@ def main():
     except Exception as e:   # informational only: never costs the bench line
         columns = {"error": repr(e)[:200]}
     finally:
-        shutil.rmtree(cdir, ignore_errors=True)
+        if cdir:
+            shutil.rmtree(cdir, ignore_errors=True)
 
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
