@@ -34,6 +34,7 @@
 #include <sstream>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "gsnp_gb300.h"
@@ -430,6 +431,7 @@ struct Chunk {
     size_t first = 0;                 /* output row of its first alignment */
     size_t kept = 0;                  /* alignments parsed */
     std::vector<std::string> chr;     /* its chromosome names, in order of first use */
+    std::unordered_map<std::string, uint32_t> chr_id;   /* name -> index in chr */
     std::string bad;                  /* its first error */
 };
 
@@ -449,6 +451,7 @@ size_t count_lines(const char* b, const char* e) {
  * Row padding past the read length is 'A' and quality 0. */
 void parse_chunk(Chunk* c, int L, Reads* out) {
     std::string read, qual;
+    size_t last_cid = (size_t)-1;
     const char* p = c->begin;
     while (p < c->end) {
         const char* eol = (const char*)memchr(p, '\n', (size_t)(c->end - p));
@@ -491,10 +494,25 @@ void parse_chunk(Chunk* c, int L, Reads* out) {
             if (c->bad.empty()) c->bad = "alignment longer than -L or than its sequence field";
             continue;
         }
-        size_t cid = 0;
-        while (cid < c->chr.size() && (c->chr[cid].size() != tl[7] || memcmp(c->chr[cid].data(), tok[7], tl[7])))
-            ++cid;
-        if (cid == c->chr.size()) c->chr.emplace_back(tok[7], tl[7]);
+        /* the previous line's name first (lines of one chromosome follow
+         * each other), then the chunk's table of names */
+        size_t cid = last_cid;
+        if (cid >= c->chr.size() || c->chr[cid].size() != tl[7] || memcmp(c->chr[cid].data(), tok[7], tl[7])) {
+            std::string name(tok[7], tl[7]);
+            auto it = c->chr_id.find(name);
+            if (it != c->chr_id.end()) {
+                cid = it->second;
+            } else {
+                cid = c->chr.size();
+                if (cid > 0xffff) {   /* ids are 16-bit; one chromosome per run is the contract anyway */
+                    if (c->bad.empty()) c->bad = "more than 65536 chromosome names";
+                    continue;
+                }
+                c->chr_id.emplace(name, (uint32_t)cid);
+                c->chr.push_back(std::move(name));
+            }
+            last_cid = cid;
+        }
         const size_t k = c->first + c->kept++;
         out->chr_id[k] = (uint16_t)cid;
         out->pos[k] = position - 1;
@@ -567,12 +585,20 @@ void load_soap(const std::string& path, int L, Reads* out) {
     close(fd);
     /* chromosome ids of each share to the file's list of names */
     std::vector<std::vector<uint16_t>> remap(nt);
+    std::unordered_map<std::string, size_t> file_id;
     for (unsigned t = 0; t < nt; ++t) {
         if (out->bad.empty() && !ch[t].bad.empty()) out->bad = ch[t].bad;
         for (const std::string& name : ch[t].chr) {
-            size_t k = 0;
-            while (k < out->chr.size() && out->chr[k] != name) ++k;
-            if (k == out->chr.size()) out->chr.push_back(name);
+            auto it = file_id.find(name);
+            size_t k;
+            if (it != file_id.end()) {
+                k = it->second;
+            } else {
+                k = out->chr.size();
+                file_id.emplace(name, k);
+                out->chr.push_back(name);
+            }
+            if (k > 0xffff && out->bad.empty()) out->bad = "more than 65536 chromosome names";
             remap[t].push_back((uint16_t)k);
         }
     }

@@ -136,3 +136,23 @@ def test_soap_loader_empty_file(tmp_path, soap_check):
     open(path, "w").close()
     rows, padding, bad = run_loader(soap_check, path, 100)
     assert rows == [] and padding == "ok" and bad == ""
+
+
+@pytest.mark.parametrize("threads", [1, 3, 64])
+def test_soap_loader_many_chromosome_names(threads, tmp_path, soap_check):
+    """Names are looked up through a table, not a scan: 2,000 names keep
+    their alignments apart; more than 65,536 (the ids are 16-bit) are an
+    input error."""
+    rng = random.Random(7)
+    for n_names, want_bad in ((2000, ""), (65537, "more than 65536 chromosome names")):
+        lines = []
+        for i in range(n_names):
+            seq = "".join(rng.choice("ACGT") for _ in range(20))
+            lines.append("\t".join([f"r{i}", seq, "I" * 20, "1", "a", "20", "+", f"contig{i}", str(1 + i), "0"]))
+        path = str(tmp_path / f"names{n_names}.soap")
+        with open(path, "w") as fh:
+            fh.write("\n".join(lines) + "\n")
+        rows, padding, bad = run_loader(soap_check, path, 20, threads)
+        assert bad == want_bad
+        if not want_bad:
+            assert [(r[0], r[4]) for r in rows] == [(i, f"contig{i}") for i in range(n_names)]
