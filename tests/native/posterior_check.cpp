@@ -18,7 +18,8 @@
  *
  * Sites: hom-ref, hom-alt, het and low-fraction mixtures at depths 1 to 255,
  * qualities 0 to 40 with errors at their rates, repeated (strand, cycle)
- * keys, a few N reference codes; rank-sum on.  A deterministic seed per run.
+ * keys, a few N reference codes, every tenth site monoploid (-m); rank-sum
+ * on.  A deterministic seed per run.
  * Prints "sites <n> fp32-decided <f> bounded-decided <b> max-relerr <r>
  * adversarial <a> decided <d>" and exits 0, or names the first failing site
  * and exits 1.
@@ -162,6 +163,7 @@ int main(int argc, char** argv) {
                 return 1;
             }
         }
+        a.monoploid = site % 10 == 0;   /* -m: homozygous genotypes only */
         double lp[16];
         load_log_prior(a, -1, ori, lp);
         auto nq = [&](int b) { return (int)((b * 7 + site) % 40); };
