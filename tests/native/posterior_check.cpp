@@ -18,8 +18,9 @@
  *
  * Sites: hom-ref, hom-alt, het and low-fraction mixtures at depths 1 to 255,
  * qualities 0 to 40 with errors at their rates, repeated (strand, cycle)
- * keys, a few N reference codes, every tenth site monoploid (-m); rank-sum
- * on.  A deterministic seed per run.
+ * keys, a few N reference codes, every tenth site monoploid (-m), one in
+ * fifty a known-SNP site with its own prior row (-2); rank-sum on.  A
+ * deterministic seed per run.
  * Prints "sites <n> fp32-decided <f> bounded-decided <b> max-relerr <r>
  * adversarial <a> decided <d>" and exits 0, or names the first failing site
  * and exits 1.
@@ -55,6 +56,30 @@ void make_p_matrix(const gsnp_params& p, std::vector<double>* pm) {
 }
 
 bool same(const SiteCall& x, const SiteCall& y) { return same_call(x, y); }
+
+/* the prior row of one known-SNP site, as snp_log_prior_kernel forms it:
+ * the novel priors of its reference base, with each listed genotype's
+ * prior replaced (cpp/prior.cc:45-97, the device form) */
+void snp_row(const CallArgs& a, uint8_t ori, bool validated, bool hapmap, const double* freq, double* lp,
+             float* lp32) {
+    for (int i = 0; i < 16; ++i) lp[i] = a.log_prior[((ori & 7) << 4) + i];
+    const int t_base = ori & 3;
+    for (int a1 = 0; a1 != 4; ++a1)
+        for (int a2 = a1; a2 != 4; ++a2) {
+            if (!(freq[a1] > 0 && freq[a2] > 0)) continue;
+            double pr;
+            if (!hapmap) {
+                if (a1 == a2 && a1 == t_base) pr = 1;
+                else if (a1 == t_base || a2 == t_base) pr = validated ? a.het_val : a.het_unval;
+                else if (a1 == a2) pr = validated ? a.althom_val : a.althom_unval;
+                else pr = validated ? a.het_val : a.het_unval;
+            } else {
+                pr = (a1 == a2 ? 1.0 : 2.0 * a.het_val) * freq[a1] * freq[a2];
+            }
+            lp[(a1 << 2) | a2] = gsnp_cr_log10(pr);
+        }
+    for (int t = 0; t < 12; ++t) lp32[t] = t < 10 ? (float)lp[genotype_of(t)] : 0.f;
+}
 
 void print_call(const char* tag, const SiteCall& c) {
     printf("  %s type1 %d base1 %d base2 %d q %d avg %d/%d cu %d/%d ca %d/%d rs %.17g flags %d\n", tag, c.type1,
@@ -111,6 +136,7 @@ int main(int argc, char** argv) {
     a.althom_val = p.althom_val;
     a.althom_unval = p.althom_unval;
     a.precision = 1;
+    a.refine = 1;
 
     std::mt19937_64 rng(seed);
     auto uni = [&](double lo, double hi) { return std::uniform_real_distribution<double>(lo, hi)(rng); };
@@ -164,15 +190,30 @@ int main(int argc, char** argv) {
             }
         }
         a.monoploid = site % 10 == 0;   /* -m: homozygous genotypes only */
+        /* a known-SNP site (-2): its own prior row */
+        static double snp_lp[16];
+        static float snp_lp32[12];
+        uint8_t code = ori;
+        int64_t row = -1;
+        if (below(50) == 0 && ori < 4) {
+            double freq[4] = {0, 0, 0, 0};
+            freq[ref] = uni(0.3, 1.0);
+            freq[alt] = below(3) ? 1.0 - freq[ref] : 0.0;
+            snp_row(a, ori, below(2) == 0, below(3) == 0, freq, snp_lp, snp_lp32);
+            a.snp_lp = snp_lp;
+            a.snp_lp32 = snp_lp32;
+            code = (uint8_t)(ori | 8);
+            row = 0;
+        }
         double lp[16];
-        load_log_prior(a, -1, ori, lp);
+        load_log_prior(a, row, code, lp);
         auto nq = [&](int b) { return (int)((b * 7 + site) % 40); };
         SiteCall want;
-        site_posterior<false>(a, ori, sp, tl64, nullptr, lp, recs.data(), 1, nq, &want);
+        site_posterior<false>(a, code, sp, tl64, nullptr, lp, recs.data(), 1, nq, &want);
         float s[10];
         for (int k = 0; k < 10; ++k) s[k] = (float)tl32[genotype_of(k)];
         SiteCall got;
-        if (fast_posterior(a, -1, ori, sp, s, sp.num, &got)) {
+        if (fast_posterior(a, row, code, sp, s, sp.num, &got)) {
             ++fast_decided;
             if (!same(got, want)) {
                 printf("site %ld: fast_posterior differs from the FP64 posterior (num %d, ori %d)\n", site, sp.num,
@@ -182,7 +223,7 @@ int main(int argc, char** argv) {
                 return 1;
             }
         }
-        if (site_posterior<false>(a, ori, sp, tl32, eps, lp, recs.data(), 1, nq, &got)) {
+        if (site_posterior<false>(a, code, sp, tl32, eps, lp, recs.data(), 1, nq, &got)) {
             ++bounded_decided;
             if (!same(got, want)) {
                 printf("site %ld: bounded posterior differs from the FP64 posterior (num %d, ori %d)\n", site,
@@ -234,11 +275,11 @@ int main(int argc, char** argv) {
             }
             ++adv_sites;
             SiteCall w64, w32;
-            site_posterior<false>(a, ori, sp, t64, nullptr, lp, recs.data(), 1, nq, &w64);
+            site_posterior<false>(a, code, sp, t64, nullptr, lp, recs.data(), 1, nq, &w64);
             float s32[10];
             for (int k = 0; k < 10; ++k) s32[k] = (float)t32[genotype_of(k)];
             bool decided = false;
-            if (fast_posterior(a, -1, ori, sp, s32, sp.num, &w32)) {
+            if (fast_posterior(a, row, code, sp, s32, sp.num, &w32)) {
                 decided = true;
                 if (!same(w32, w64)) {
                     printf("site %ld variant %d: fast_posterior differs on adversarial sums (num %d)\n", site,
@@ -248,7 +289,7 @@ int main(int argc, char** argv) {
                     return 1;
                 }
             }
-            if (site_posterior<false>(a, ori, sp, t32, e32, lp, recs.data(), 1, nq, &w32)) {
+            if (site_posterior<false>(a, code, sp, t32, e32, lp, recs.data(), 1, nq, &w32)) {
                 decided = true;
                 if (!same(w32, w64)) {
                     printf("site %ld variant %d: bounded posterior differs on adversarial sums (num %d)\n", site,
