@@ -23,6 +23,7 @@
 #include <functional>
 #include <string>
 #include <thread>
+#include <memory>
 #include <vector>
 
 #include "calling.cuh"
@@ -1413,12 +1414,15 @@ int gsnp_get_stats(gsnp_context* c, uint64_t* s, int n) {
 namespace gsnp {
 namespace {
 
-int fetch_results(gsnp_context* c, std::vector<SiteCall>* calls, std::vector<SiteCounts>* counts) {
-    calls->resize((size_t)c->chr_len);
-    CK(cudaMemcpy(calls->data(), c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost), "fetch");
+/* the calls (and counts) of the whole chromosome in host memory; the arrays
+ * are left uninitialised, since the copies fill every entry (a zero fill of
+ * 1.6 GB at 50 Mbp would cost more than the copy) */
+int fetch_results(gsnp_context* c, std::unique_ptr<SiteCall[]>* calls, std::unique_ptr<SiteCounts[]>* counts) {
+    calls->reset(new SiteCall[(size_t)c->chr_len]);
+    CK(cudaMemcpy(calls->get(), c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost), "fetch");
     if (c->have_counts) {
-        counts->resize((size_t)c->chr_len);
-        CK(cudaMemcpy(counts->data(), c->d_counts, (size_t)c->chr_len * sizeof(SiteCounts), cudaMemcpyDeviceToHost),
+        counts->reset(new SiteCounts[(size_t)c->chr_len]);
+        CK(cudaMemcpy(counts->get(), c->d_counts, (size_t)c->chr_len * sizeof(SiteCounts), cudaMemcpyDeviceToHost),
            "fetch");
     }
     return GSNP_OK;
@@ -1537,8 +1541,8 @@ extern "C" int gsnp_write_cns(gsnp_context* c, const char* chr_name, const char*
 extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const char* base_path) {
     if (!c || !base_path) return fail(c, GSNP_ERR_ARG, "null argument");
     cudaSetDevice(c->device);
-    std::vector<SiteCall> calls;
-    std::vector<SiteCounts> counts;
+    std::unique_ptr<SiteCall[]> calls;
+    std::unique_ptr<SiteCounts[]> counts;
     std::string err;
     HostDictCodec dict;
     if (!chr_name) {
@@ -1551,7 +1555,7 @@ extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const c
     if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
     const int rc = fetch_results(c, &calls, &counts);
     if (rc != GSNP_OK) return rc;
-    if (write_columns(c->plan, c->h_codes.data(), calls.data(), c->have_counts ? counts.data() : nullptr, chr_name,
+    if (write_columns(c->plan, c->h_codes.data(), calls.get(), c->have_counts ? counts.get() : nullptr, chr_name,
                       base_path, dict, host_threads(), &err) != 0)
         return fail(c, GSNP_ERR_INPUT, err);
     return GSNP_OK;
