@@ -330,23 +330,39 @@ int dict_compress_prealloc(const T* h_in, size_t n, void* d_scratch, size_t scra
     cudaError_t e = cudaMemcpyAsync(in, h_in, n * sizeof(T), cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(table, 0xff, cap * 8, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, 16, stream);
-    if (e != cudaSuccess) return 1;
+    if (e != cudaSuccess) {
+        (void)cudaStreamSynchronize(stream);
+        return 1;
+    }
     insert_kernel<T><<<blocks(n, 256), 256, 0, stream>>>(in, n, table, cap - 1, flags);
     compact_kernel<<<blocks(cap, 256), 256, 0, stream>>>(table, cap, keys, count);
+    /* every return after work was queued waits for the stream first, so
+     * that no kernel of this call still uses the scratch when it returns */
+    auto fail = [&](int rc) {
+        (void)cudaStreamSynchronize(stream);
+        return rc;
+    };
     unsigned long long d = 0;
     int hflags = 0;
-    e = cudaMemcpyAsync(&d, count, 8, cudaMemcpyDeviceToHost, stream);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&d, count, 8, cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hflags, flags, 4, cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess) return 1;
+    if (e != cudaSuccess) return fail(1);
     if (hflags & 2) return 4;
+    /* the word count follows from the distinct count: check the caller's
+     * capacity before anything more is queued */
+    const int bits = dict_bits((unsigned long)d);
+    const int per_word = (int)floor(32 / (double)bits);
+    const unsigned long nw = (unsigned long)ceil(n / (double)per_word);
+    if (*n_words < nw) return 4;
     size_t md = 1;
     while (md < d) md <<= 1;
-    if (md > d && cudaMemsetAsync(keys + d, 0xff, (md - d) * 8, stream) != cudaSuccess) return 1;
+    if (md > d && cudaMemsetAsync(keys + d, 0xff, (md - d) * 8, stream) != cudaSuccess) return fail(1);
     if (md <= 8192) {
         if (cudaFuncSetAttribute(bitonic_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 8) !=
             cudaSuccess)
-            return 1;
+            return fail(1);
         bitonic_smem_kernel<<<1, 1024, md * 8, stream>>>(keys, (int)md);
     } else {
         for (size_t k = 2; k <= md; k <<= 1)
@@ -354,17 +370,13 @@ int dict_compress_prealloc(const T* h_in, size_t n, void* d_scratch, size_t scra
                 bitonic_global_kernel<<<blocks(md, 256), 256, 0, stream>>>(keys, md, k, j);
     }
     index_kernel<T><<<blocks(n, 256), 256, 0, stream>>>(in, n, keys, d, idx);
-    const int bits = dict_bits((unsigned long)d);
-    const int per_word = (int)floor(32 / (double)bits);
-    const unsigned long nw = (unsigned long)ceil(n / (double)per_word);
-    if (*n_words < nw) return 4;
     pack_kernel<<<blocks(nw, 256), 256, 0, stream>>>(idx, n, bits, per_word, nw, words);
     values_kernel<T><<<blocks(d, 256), 256, 0, stream>>>(keys, d, flags, vals);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_words, words, nw * 4, cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_dict, vals, d * sizeof(T), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess) return 1;
+    if (e != cudaSuccess) return fail(1);
     *n_dict = (unsigned long)d;
     *n_words = nw;
     return 0;

@@ -5,17 +5,23 @@
  * whose free device memory is held by another allocator (a caching allocator
  * that reserved it), or a streaming writer that must not call cudaMalloc or
  * cudaFree, which synchronise the whole device and stall the work of other
- * streams.  The codec's scratch is a file-scope device array reserved when the
- * module loads, sized for the reference's dictionary capacity of 32 x 8192
- * values; nothing is allocated per call, on the device or the host.
+ * streams.  The codec's scratch is a file-scope device array, sized for the
+ * reference's dictionary capacity of 32 x 8192 values; nothing is allocated per
+ * call, on the device or the host.
  *
- * The first call on each device looks up the array's device address with
- * cudaGetSymbolAddress (that device current) and keeps it; make that first
- * call before any stream capture.  Every call clears the parts of the scratch
- * that must start cleared (the hash table and the counters) on the caller's
- * stream, so nothing needs to be zero beforehand.  All calls on one device
- * share the one scratch array: calls that overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller.
+ * The array is reserved on a device when this library's device code is loaded
+ * there.  With CUDA's lazy module loading (the default) that happens on the
+ * first call on the device, which looks up the array's device address with
+ * cudaGetSymbolAddress (that device current) and keeps it.  So make one call
+ * first - a call with n = 0 does only this set-up - before another allocator
+ * takes the free device memory, and before any stream capture.  The kept
+ * address does not survive cudaDeviceReset: do not use this entry point on a
+ * device after resetting it.  Every call clears the parts of the scratch that
+ * must start cleared (the hash table and the counters) on the caller's stream,
+ * so nothing needs to be zero beforehand.  All calls on one device share the
+ * one scratch array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Every return, errors
+ * included, comes after the call's device work on that stream has finished.
  */
 #include <cuda_runtime.h>
 

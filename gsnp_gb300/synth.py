@@ -562,6 +562,25 @@ def write_soap(w: Workload, path: str) -> None:
             f.write(soap_lines(w, r0, min(w.num_reads, r0 + CH)))
 
 
+def workload_digest(w: Workload) -> str:
+    """SHA-256 over every array of the workload, in a fixed order and layout.
+
+    The text files of write_inputs are a function of these arrays, so equal
+    digests mean the same input files; the digest is cheap to take where the
+    multi-gigabyte text files are not written (the GPU generator).
+    """
+    import hashlib
+    h = hashlib.sha256()
+    h.update(w.chr_name.encode() + b"\0")
+    for a, dt in ((w.ref, "u1"), (w.pos, "<i4"), (w.length, "<i4"), (w.hit, "<i4"), (w.strand, "u1"),
+                  (w.seq, "u1"), (w.qual, "u1"), (w.mismatch, "<i4"), (w.db_pos, "<i8"), (w.db_hapmap, "u1"),
+                  (w.db_validated, "u1"), (w.db_freq, "<f8")):
+        b = np.ascontiguousarray(a, dtype=dt)
+        h.update(np.asarray(b.shape, dtype="<i8").tobytes())
+        h.update(memoryview(b).cast("B"))
+    return h.hexdigest()
+
+
 def write_inputs(w: Workload, directory: str) -> Dict[str, str]:
     """Write ref.fa, reads.soap and (when present) dbsnp.txt under `directory`."""
     os.makedirs(directory, exist_ok=True)

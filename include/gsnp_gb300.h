@@ -226,16 +226,22 @@ int gsnp_get_stats(gsnp_context* ctx, uint64_t* stats, int n);
  * cannot allocate device memory on their path - a process whose free device
  * memory is held by another allocator, or a streaming writer that must not
  * call cudaMalloc/cudaFree because they synchronise the device.  Its scratch
- * is a static device array reserved when the library loads (12.6 MB), so it
- * takes at most 262,144 values (32 x 8192, the reference's dictionary
- * capacity); larger inputs return GSNP_ERR_CAPACITY without touching the
- * device.  values: n host values of the given GSNP_DICT_* type; *n_words and
- * *n_dict hold the capacities of words and dict on entry and the counts on
- * return.  Runs on the current device and the given cudaStream_t (NULL: the
- * legacy default stream) and returns when the outputs are in host memory.
- * The first call on a device looks up the scratch array's address; make it
- * before any stream capture.  Every call clears the scratch it needs on the
- * stream; calls that overlap on one GPU race and must be serialised. */
+ * is a static device array of 12.6 MB, so it takes at most 262,144 values
+ * (32 x 8192, the reference's dictionary capacity); larger inputs return
+ * GSNP_ERR_CAPACITY without touching the device.  values: n host values of
+ * the given GSNP_DICT_* type.  *n_words and *n_dict hold the capacities of
+ * words and dict on entry and the counts on return; as with
+ * cuda_dictCompression, dict must have room for n values (not just the
+ * distinct ones), else the call returns GSNP_ERR_CAPACITY, as it does when
+ * words is too small for the packed indices.  Runs on the current device and
+ * the given cudaStream_t (NULL: the legacy default stream) and returns, on
+ * success and on error, once its work on that stream is done.
+ * The scratch is reserved on a device by the first call there (CUDA loads the
+ * library's device code lazily): make one call first - n = 0 does only that
+ * set-up - before another allocator takes the free memory, and before any
+ * stream capture.  Do not call it on a device after cudaDeviceReset.  Every
+ * call clears the scratch it needs on the stream; calls that overlap on one
+ * GPU race and must be serialised. */
 int gsnp_dict_compress_static(int type, const void* values, uint64_t n, uint32_t* words, uint64_t* n_words,
                               void* dict, uint64_t* n_dict, void* stream);
 

@@ -10,6 +10,21 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 
+def reference_tree():
+    """The reference source tree: $GSNP_REFERENCE, else the tree that
+    __graft_entry__.build() compiled oracle/_ref from (recorded in
+    oracle/_ref/reference_tree), else None."""
+    env = os.environ.get("GSNP_REFERENCE")
+    if env:
+        return env if os.path.isdir(env) else None
+    rec = os.path.join(ROOT, "oracle", "_ref", "reference_tree")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            path = f.read().strip()
+        return path if os.path.isdir(path) else None
+    return None
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103a) device")
 

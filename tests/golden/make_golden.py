@@ -13,7 +13,15 @@ digests of the inputs and of every output file (cns text, the -C files, the
 turns the files back into text, and that text's digest is recorded too.  The reference tree is needed to run this script;
 the tests that read golden.json are not.
 
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+With --full it makes tests/golden/golden_full.json instead: the full-size
+30x workloads (c1 with its -C files, and c3), each recorded by the digest of
+the generator's arrays (synth.workload_digest) rather than of the
+multi-gigabyte text files, so that a GPU test can check its own regenerated
+input without writing them.
+
+    python tests/golden/make_golden.py [--ref /path/to/reference] [--full]
+
+The reference tree is taken from --ref, else from $GSNP_REFERENCE.
 """
 import argparse
 import hashlib
@@ -43,6 +51,14 @@ def sha(data: bytes) -> str:
     return hashlib.sha256(data).hexdigest()
 
 
+def sha_path(path: str) -> str:
+    h = hashlib.sha256()
+    with open(path, "rb") as fh:
+        for block in iter(lambda: fh.read(1 << 24), b""):
+            h.update(block)
+    return h.hexdigest()
+
+
 def case_flags(w, paths, compress):
     flags = [f for f in w.cli_flags(paths.get("dbsnp")) if f != "-C"]
     if compress:
@@ -70,20 +86,69 @@ def run_and_digest(binary, paths, flags, out_dir):
     out = {}
     for f in sorted(os.listdir(out_dir)):
         if f.startswith("cns") or f == "mat":
-            with open(os.path.join(out_dir, f), "rb") as fh:
-                out[f] = sha(fh.read())
+            out[f] = sha_path(os.path.join(out_dir, f))
     return out
+
+
+# full-size cases: (case id, config, -C)
+FULL_CASES = [
+    ("c1_full_text", "c1", False),
+    ("c1_full_C", "c1", True),
+    ("c3_full_text", "c3", False),
+]
+
+
+def run_full(ref_bin, ref_decompress):
+    """Full-size cases: the inputs are written once per config and each case's
+    reference run goes in a process of its own, side by side."""
+    import concurrent.futures as cf
+    from gsnp_gb300 import synth
+    golden = {}
+    for name in sorted({c[1] for c in FULL_CASES}):
+        cases = [c for c in FULL_CASES if c[1] == name]
+        with tempfile.TemporaryDirectory() as d:
+            w = synth.make_workload(name, scale=1.0)
+            wd = synth.workload_digest(w)
+            paths = synth.write_inputs(w, d)
+            runs = {}
+            with cf.ThreadPoolExecutor(len(cases)) as ex:
+                for cid, _, compress in cases:
+                    flags = case_flags(w, paths, compress)
+                    runs[cid] = (flags, ex.submit(run_and_digest, ref_bin, paths, flags, os.path.join(d, cid)))
+                for cid, _, compress in cases:
+                    flags, fut = runs[cid]
+                    outs = fut.result()
+                    if compress:
+                        text = os.path.join(d, cid + ".decompressed")
+                        subprocess.run([ref_decompress, os.path.join(d, cid, "cns"), text], check=True,
+                                       capture_output=True)
+                        outs["decompressed"] = sha_path(text)
+                        os.unlink(text)
+                    golden[cid] = {"config": name, "scale": 1.0, "compress": compress,
+                                   "flags": [f if not os.path.isabs(f) else os.path.basename(f) for f in flags],
+                                   "workload_sha256": wd, "sites": w.genome_len, "reads": w.num_reads,
+                                   "outputs": outs}
+                    print(cid, len(outs), "files", flush=True)
+            del w
+    with open(os.path.join(HERE, "golden_full.json"), "w") as f:
+        json.dump(golden, f, indent=1, sort_keys=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GSNP_REFERENCE"))
+    ap.add_argument("--full", action="store_true")
     args = ap.parse_args()
+    if not args.ref:
+        sys.exit("give the reference tree with --ref or $GSNP_REFERENCE")
     r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "ref-decompress", "REF=" + args.ref])
     if r.returncode:
         sys.exit("cannot build the reference host code")
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "gsnp_ref")
     ref_decompress = os.path.join(ROOT, "oracle", "_ref", "gsnp_ref_decompress")
+    if args.full:
+        run_full(ref_bin, ref_decompress)
+        return
     golden = {}
     for cid, name, scale, compress in CASES:
         with tempfile.TemporaryDirectory(dir=HERE) as d:

@@ -54,8 +54,9 @@ def test_backend_library_exports_reference_symbols(native_lib):
 def test_reference_host_objects_link_against_backend(native_lib):
     """The reference's own host objects (compiled in place from its sources)
     link against libgsnp_backend.so with no unresolved symbol."""
-    ref = os.environ.get("GSNP_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "cpp")):
+    from conftest import reference_tree
+    ref = reference_tree()
+    if ref is None or not os.path.isdir(os.path.join(ref, "cpp")):
         pytest.skip("reference sources not present")
     r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref-link", "REF=" + ref],
                        capture_output=True, text=True)

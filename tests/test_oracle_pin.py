@@ -8,18 +8,19 @@ import subprocess
 
 import pytest
 
+from conftest import reference_tree
 from gsnp_gb300 import synth
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "gsnp_ref")
-REF_TREE = "/root/reference"
 
 
 @pytest.fixture(scope="module")
 def ref_bin():
-    if not os.path.isdir(REF_TREE):
-        pytest.skip("reference tree not mounted")
-    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref", "REF=" + REF_TREE],
+    tree = reference_tree()
+    if tree is None:
+        pytest.skip("reference tree not mounted ($GSNP_REFERENCE)")
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref", "REF=" + tree],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     return REF_BIN
