@@ -57,6 +57,15 @@ DeviceState g;
 
 }  // namespace
 
+OracleBackendView oracle_backend_view() {
+    OracleBackendView v;
+    v.records = g.sparse.data();
+    v.num = g.num.data();
+    v.dep_uni = g.dep_uni.data();
+    v.type_likely = g.type_likely.data();
+    return v;
+}
+
 void GPUInit() {}
 
 void GSNPKernelInit(const unsigned long winSize, const int readLength, const double pcr_dependency,

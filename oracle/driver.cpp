@@ -776,6 +776,16 @@ int soap2cns(const Params& para, const ReadStore& rs, Genome* genome, const doub
 
 }  // namespace
 
+void oracle_rank_table(double* p_rank) { rank_table_gen(p_rank); }
+
+void oracle_prior_table(double het_novel, double althom_novel, bool transition_dominant, double* p_prior) {
+    Params para;
+    para.het_novel = het_novel;
+    para.althom_novel = althom_novel;
+    para.transition_dominant = transition_dominant;
+    prior_gen(para, p_prior);
+}
+
 int oracle_main(int argc, char** argv) {
     GPUInit();
     Params para;

@@ -154,6 +154,23 @@ unsigned int oracle_rle(T* data, unsigned long n, R* run_length) {
     return (unsigned int)runs;
 }
 
+/* ---- test access to the restated backend's window state ---- */
+
+/* The private "device" arrays of oracle/backend.cpp, for the check of the
+ * backend against the reference's CPU twins (oracle/gold/check.cpp). */
+struct OracleBackendView {
+    const unsigned int* records;   /* [site][GSNP_MAX_RECORDS_PER_SITE] */
+    const unsigned int* num;       /* records per site */
+    const int* dep_uni;
+    const double* type_likely;     /* [site][GSNP_LIKELY_SIZE] */
+};
+OracleBackendView oracle_backend_view();
+
+/* the restated driver's tables: Prob_matrix::rank_table_gen
+ * (cpp/rank_sum.cc:3-42) and Prob_matrix::prior_gen (cpp/prior.cc:3-43) */
+void oracle_rank_table(double* p_rank);
+void oracle_prior_table(double het_novel, double althom_novel, bool transition_dominant, double* p_prior);
+
 /* ---- restated host driver (cpp/main.cc, cpp/call_genotype.cc, ...) ---- */
 
 /* SOAPsnp command line; returns the process exit status. */
