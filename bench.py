@@ -358,7 +358,54 @@ def main():
     # and a step that meets their traffic is reported in step_ms, not averaged in
     e2e_s = max_over_ranks(max(statistics.median(e2e_times), 1e-9))
     e2e_value = world * sites / e2e_s
+
+    # ---- end to end with the cns text, the output the reference's pass writes ----
+    # each step: upload and call (gsnp_call_chromosome), then the text of every
+    # site formatted on the GPU, downloaded and written (gsnp_write_cns, to the
+    # null device)
+    text_times = []
+    for i in range(1 + e2e_steps):
+        barrier()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        caller.call(reads)
+        rc = caller.lib.gsnp_write_cns(caller.ctx, w.chr_name.encode(), os.devnull.encode())
+        torch.cuda.synchronize()
+        if rc != 0:
+            text_times = []
+            break
+        if i > 0:
+            text_times.append(time.perf_counter() - t1)
+    e2e_text = None
+    if text_times:
+        h2d_t, d2h_t = caller.transfer_bytes()
+        ts = max_over_ranks(statistics.median(text_times))
+        e2e_text = {"value": world * sites / ts, "unit": UNIT, "h2d_bytes_per_step": int(h2d_t),
+                    "d2h_bytes_per_step": int(d2h_t), "steps": e2e_steps, "stat": "median step",
+                    "step_ms": [round(t * 1e3, 2) for t in text_times],
+                    "note": "gsnp_call_chromosome + gsnp_write_cns (cns text of every site to the null device)"}
     sampler.__exit__(None, None, None)
+
+    # ---- parity of the headline form at full size: the cns text of the last
+    # call against the digest of the reference host code's text for the same
+    # workload (tests/golden/golden_full.json), after the timed region ----
+    parity = None
+    try:
+        gpath = os.path.join(ROOT, "tests", "golden", "golden_full.json")
+        golden = json.load(open(gpath)) if os.path.exists(gpath) else {}
+        cid = next((k for k, g in golden.items() if g["config"] == args.workload and not g["compress"]
+                    and args.scale == g["scale"]), None)
+        if cid is not None:
+            import hashlib
+            wd = synth.workload_digest(w) == golden[cid]["workload_sha256"]
+            text = caller.format_cns(w.chr_name)
+            match = hashlib.sha256(text).hexdigest() == golden[cid]["outputs"]["cns"]
+            parity = {"golden": cid, "workload_digest_match": wd, "cns_digest_match": match,
+                      "rows": text.count(b"\n"), "cns_rows_differing": 0 if (wd and match) else None,
+                      "form": args.precision}
+            del text
+    except Exception as e:   # informational: never costs the bench line
+        parity = {"error": repr(e)[:200]}
 
     # ---- the cns text of the last call (what the reference's pass writes), informational ----
     text_ms = []
@@ -433,6 +480,8 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps, "stat": "median step",
                     "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
+            "e2e_text": e2e_text,
+            "cns_parity": parity,
             "cns_text": ({"ms": round(min(text_ms), 2), "rows": sites,
                           "note": "gsnp_write_cns of the last call to the null device: GPU formatting, download, write"}
                          if text_ms else None),
