@@ -91,7 +91,7 @@ __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v)
  * loop going. */
 template <int SLOTS>
 __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
-                                                   bool active, uint32_t* recs) {
+                                                   bool active, uint32_t* recs, bool* report_overflow = nullptr) {
     /* records are appended in pileup order; sort_column puts them in
      * ascending order after the pileup */
     const int lane = threadIdx.x & 31;
@@ -163,7 +163,8 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
             }
         }
     }
-    if (overflow) atomicExch(a.error, 2);
+    if (report_overflow) *report_overflow = overflow;
+    else if (overflow) atomicExch(a.error, 2);
     if (depth > 0xffff) atomicExch(a.error, 1);
     PackedPileup pk;
     pk.cu4 = cu4;
@@ -314,16 +315,19 @@ static_assert(kClassifyThreads % kTile == 0, "a classify CTA holds whole tiles")
 
 __global__ void __launch_bounds__(kClassifyThreads) classify_tiles_kernel(CallArgs a, int pass, int64_t t_begin,
                                                                           int64_t t_end, int* bin_count,
-                                                                          int32_t* bin_tiles) {
+                                                                          int32_t* bin_tiles,
+                                                                          const int32_t* __restrict__ list) {
     __shared__ int32_t spos[kClassifyTiles][kClassifyStage];
     __shared__ int smax[kClassifyThreads / 32];
     __shared__ int sbin_count[2 * kNumBins], sbin_base[2 * kNumBins];
     const int lt = threadIdx.x / kTile, tt = threadIdx.x % kTile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t tile = t_begin + (int64_t)blockIdx.x * kClassifyTiles + lt;
+    /* the tiles [t_begin, t_end), or with a list the tiles list[t_begin, t_end) */
+    const int64_t idx = t_begin + (int64_t)blockIdx.x * kClassifyTiles + lt;
     if (threadIdx.x < 2 * kNumBins) sbin_count[threadIdx.x] = 0;
+    bool part = idx < t_end;
+    const int64_t tile = list ? (part ? (int64_t)list[idx] : 0) : idx;
     const int64_t s0 = tile * kTile;
-    bool part = tile < t_end;
     uint8_t wflags = 0;
     if (part) {
         wflags = a.win_flags[(int)(s0 / kWin)];
@@ -468,34 +472,14 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
 /* the fast calling kernel                                                   */
 /* ------------------------------------------------------------------------ */
 
-/* Sites whose call is not proven in FP32 (and every 4096th site, sampled for
- * the FP32 accuracy figure) are appended to the deferred pool: counts and the
- * sorted records with their occurrence byte restored.  The append counters
- * keep counting past the capacities so that the host can size the pool and
- * run the pass again. */
+/* The FP32 work on one site of a tile after its pileup and sort: the
+ * dependency walk, the compensated sums, the FP32 posterior, and the append
+ * of the site to the deferred pool when its call is not proven.  Every lane
+ * of the warp calls it (the appends are warp-aggregated). */
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    constexpr bool kGlobal = kGlobalRecs(SLOTS, true);
-    uint32_t* recs_all = kGlobal ? a.deep_recs + (size_t)blockIdx.x * SLOTS * kTile : reinterpret_cast<uint32_t*>(smem);
-    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + (kGlobal ? 0 : SLOTS * kTile);
-
-    const int t = threadIdx.x, lane = t & 31;
-    const int64_t tile = tiles[blockIdx.x];
-    const int64_t s0 = tile * kTile;
-    const int win = (int)(s0 / kWin);
-    const uint8_t wflags = a.win_flags[win];
-    const int64_t r_lo = a.warp_rng[tile * 2];
-    const int64_t r_hi = a.warp_rng[tile * 2 + 1];
-    const int64_t site = s0 + t;
-    const bool active = site < a.chr_len;
-    const uint8_t ori = active ? __ldg(a.ori + site) : 0;
-    const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
-    const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs_all + t).unpack();
-    uint32_t* recs = recs_all + t;
-    uint32_t* seen = seen_all + t;
-    if (active) sort_column<SLOTS>(recs, p.num);
-
+__device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool active, uint8_t ori, uint8_t wflags,
+                                          int32_t snp_row, const SitePileup& p, uint32_t* recs, uint32_t* seen) {
+    const int lane = threadIdx.x & 31;
     uint8_t dflags = 0;
     if (active) {
         if (wflags & kWinKeepCounts) store_counts(a, site, p);
@@ -583,6 +567,105 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
     for (int i = 0; i < p.num; ++i) dst[i] = (recs[i * kTile] & ~0xffu) | 1u;
 }
 
+/* Sites whose call is not proven in FP32 (and every 4096th site, sampled for
+ * the FP32 accuracy figure) are appended to the deferred pool: counts and the
+ * sorted records with their occurrence byte restored.  The append counters
+ * keep counting past the capacities so that the host can size the pool and
+ * run the pass again. */
+template <int SLOTS>
+__global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    constexpr bool kGlobal = kGlobalRecs(SLOTS, true);
+    uint32_t* recs_all = kGlobal ? a.deep_recs + (size_t)blockIdx.x * SLOTS * kTile : reinterpret_cast<uint32_t*>(smem);
+    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + (kGlobal ? 0 : SLOTS * kTile);
+
+    const int t = threadIdx.x;
+    const int64_t tile = tiles[blockIdx.x];
+    const int64_t s0 = tile * kTile;
+    const int win = (int)(s0 / kWin);
+    const uint8_t wflags = a.win_flags[win];
+    const int64_t r_lo = a.warp_rng[tile * 2];
+    const int64_t r_hi = a.warp_rng[tile * 2 + 1];
+    const int64_t site = s0 + t;
+    const bool active = site < a.chr_len;
+    const uint8_t ori = active ? __ldg(a.ori + site) : 0;
+    const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
+    const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs_all + t).unpack();
+    uint32_t* recs = recs_all + t;
+    uint32_t* seen = seen_all + t;
+    if (active) sort_column<SLOTS>(recs, p.num);
+
+    fast_site<SLOTS>(a, site, active, ori, wflags, snp_row, p, recs, seen);
+}
+
+/* ------------------------------------------------------------------------ */
+/* the persistent FP32 calling kernel                                        */
+/* ------------------------------------------------------------------------ */
+
+/* Column sort for a tile whose deepest column holds tile_max records
+ * (warp-uniform): the chunk network past the first 32 records is sized for
+ * the tile, not for the kernel's slot capacity. */
+template <int SLOTS>
+__device__ __forceinline__ void sort_column_upto(uint32_t* recs, int num, int tile_max) {
+    if (tile_max <= 32) sort_column<32>(recs, num);
+    else if (tile_max <= 40) sort_column<40>(recs, num);
+    else if (tile_max <= 48 || SLOTS <= 48) sort_column<(SLOTS < 48 ? SLOTS : 48)>(recs, num);
+    else sort_column<SLOTS>(recs, num);
+}
+
+/* One launch over the FP32 windows' tiles of a segment: each warp takes
+ * kStreamChunk consecutive tiles at a time from a counter, so the tiles in
+ * flight are neighbours and the read rows they share are fetched from DRAM
+ * about once and then served by L2.  The grid is sized to the resident CTAs,
+ * whatever the segment's length.  A tile whose window needs the FP64 form
+ * (its likelihood is kept for, or taken from, another window), or one with a
+ * site of more than SLOTS records, is appended to the leftover list for the
+ * binned kernels instead. */
+template <int SLOTS>
+__global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(CallArgs a, StreamQueue q) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* seen_all = recs_all + SLOTS * kTile;
+    const int t = threadIdx.x;
+    uint32_t* recs = recs_all + t;
+    uint32_t* seen = seen_all + t;
+    const int64_t n = q.t_end - q.t_begin;
+    for (;;) {
+        unsigned long long first = 0;
+        if (t == 0) first = atomicAdd(q.next, (unsigned long long)kStreamChunk);
+        first = __shfl_sync(kFull, first, 0);
+        if ((int64_t)first >= n) break;
+        const int64_t last = min((int64_t)first + kStreamChunk, n);
+        for (int64_t k = (int64_t)first; k < last; ++k) {
+            const int64_t tile = q.t_begin + k;
+            const int64_t s0 = tile * kTile;
+            const int win = (int)(s0 / kWin);
+            const uint8_t wflags = a.win_flags[win];
+            if (wflags & (kWinKeepLik | kWinExternalLik)) {
+                if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
+                continue;
+            }
+            const int64_t r_lo = a.tile_rng[tile * 2];
+            const int64_t r_hi = a.tile_rng[tile * 2 + 1];
+            const int64_t site = s0 + t;
+            const bool active = site < a.chr_len;
+            const uint8_t ori = active ? __ldg(a.ori + site) : 0;
+            const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
+            bool overflow = false;
+            const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs, &overflow).unpack();
+            if (__any_sync(kFull, overflow)) {
+                if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
+                continue;
+            }
+            int tile_max = active ? p.num : 0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) tile_max = max(tile_max, __shfl_xor_sync(kFull, tile_max, off));
+            if (active) sort_column_upto<SLOTS>(recs, p.num, tile_max);
+            fast_site<SLOTS>(a, site, active, ori, wflags, snp_row, p, recs, seen);
+        }
+    }
+}
+
 /* The FP64 pass over the deferred sites, one thread per site: the FP32 sums
  * again (the same pairing, hence the same values) with the double-precision
  * bound checks, then the FP64 sums where those fail.  Sampled sites also get
@@ -656,13 +739,51 @@ size_t call_smem_bytes(int slots, int L, bool fast) {
 }
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
-                            int32_t* d_bin_tiles, cudaStream_t stream) {
+                            int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list) {
     cudaError_t e = cudaMemsetAsync(d_bin_count, 0, sizeof(int) * 2 * kNumBins, stream);
     if (e != cudaSuccess) return e;
     const unsigned blocks = (unsigned)((t_end - t_begin + kClassifyTiles - 1) / kClassifyTiles);
     if (blocks == 0) return cudaSuccess;
-    classify_tiles_kernel<<<blocks, kClassifyThreads, 0, stream>>>(a, pass, t_begin, t_end, d_bin_count, d_bin_tiles);
+    classify_tiles_kernel<<<blocks, kClassifyThreads, 0, stream>>>(a, pass, t_begin, t_end, d_bin_count, d_bin_tiles,
+                                                                   list);
     return cudaGetLastError();
+}
+
+size_t stream_smem_bytes(int slots, int L) { return call_smem_bytes(slots, L, true); }
+
+template <int SLOTS>
+static cudaError_t launch_stream_one(const CallArgs& a, const StreamQueue& q, int ctas, cudaStream_t stream) {
+    const int smem = (int)stream_smem_bytes(SLOTS, a.L);
+    cudaError_t e = cudaFuncSetAttribute(call_stream_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    call_stream_kernel<SLOTS><<<ctas, kTile, smem, stream>>>(a, q);
+    return cudaGetLastError();
+}
+
+/* resident CTAs of the persistent kernel of `slots` record slots on one SM */
+int stream_ctas_per_sm(int slots, int L) {
+    int n = 0;
+    const int smem = (int)stream_smem_bytes(slots, L);
+    cudaError_t e;
+    if (slots <= 48) {
+        e = cudaFuncSetAttribute(call_stream_kernel<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, call_stream_kernel<48>, kTile, smem);
+    } else {
+        e = cudaFuncSetAttribute(call_stream_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, call_stream_kernel<64>, kTile, smem);
+    }
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
+/* The persistent FP32 kernel over q's tiles with `ctas` CTAs; slots is 48 or
+ * 64.  q.next and q.n_leftover must be zero. */
+cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int ctas, cudaStream_t stream) {
+    if (q.t_end <= q.t_begin) return cudaSuccess;
+    return slots <= 48 ? launch_stream_one<48>(a, q, ctas, stream) : launch_stream_one<64>(a, q, ctas, stream);
 }
 
 template <int SLOTS>

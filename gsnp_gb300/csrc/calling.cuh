@@ -28,6 +28,7 @@ enum CallKind : int {
     kKindFP64 = 1,      /* FP64 likelihood, every site of the tile */
     kKindFast = 2,      /* FP32 likelihood and posterior, hard sites deferred */
     kKindDeferred = 3,  /* FP64 pass over the sites the fast kernel deferred */
+    kKindStream = 4,    /* the persistent FP32 kernel over a segment's tiles */
 };
 
 /* A site the fast kernel left to the FP64 pass: its pileup counts and the
@@ -51,6 +52,17 @@ enum WindowFlags : uint8_t {
     kWinKeepCounts = 1,   /* a later gap window shows this window's host counts */
     kWinKeepLik = 2,      /* a later window reuses this window's likelihood */
     kWinExternalLik = 4,  /* likelihood comes from another window (or zeros) */
+};
+
+/* tiles a warp of the persistent FP32 kernel takes per counter increment */
+constexpr int kStreamChunk = 2;
+
+/* work queue of one launch of the persistent FP32 kernel (call_stream_kernel) */
+struct StreamQueue {
+    int64_t t_begin, t_end;       /* the segment's tiles */
+    unsigned long long* next;     /* tiles handed out so far (zero before the launch) */
+    int32_t* leftover;            /* tiles left to the binned kernels */
+    int* n_leftover;              /* their count (zero before the launch) */
 };
 
 struct CallArgs {

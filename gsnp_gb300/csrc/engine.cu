@@ -36,7 +36,9 @@
 namespace gsnp {
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
-                            int32_t* d_bin_tiles, cudaStream_t stream);
+                            int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list = nullptr);
+cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int ctas, cudaStream_t stream);
+int stream_ctas_per_sm(int slots, int L);
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
@@ -394,6 +396,12 @@ struct gsnp_context {
     int64_t* d_tile_rng = nullptr;  /* [n_tiles][2] */
     uint32_t* d_deep = nullptr;     /* record columns of the deep bins' CTAs */
     int64_t deep_cap = 0;           /* words */
+    /* the persistent FP32 kernel: its counters (tiles handed out, leftover
+     * count), the leftover tiles, its record slots and grid */
+    unsigned long long* d_stream_ctl = nullptr;
+    int32_t* d_leftover = nullptr;
+    int stream_slots = 0, stream_ctas = 0, stream_ctas_L = -1;
+    bool stream_path = true;
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
@@ -541,6 +549,7 @@ constexpr size_t kMapBins = 0;       /* int[2 * kNumBins] */
 constexpr size_t kMapDcount = 64;    /* unsigned long long[2] */
 constexpr size_t kMapError = 96;     /* int */
 constexpr size_t kMapGerror = 100;   /* int */
+constexpr size_t kMapLeftover = 104; /* int */
 constexpr size_t kMapStats = 128;    /* unsigned long long[kNumStats] */
 constexpr size_t kMapWindows = 256;  /* the call's window tables */
 static_assert(sizeof(int) * 2 * kNumBins <= kMapDcount, "bin counts overlap the deferred counts");
@@ -578,7 +587,7 @@ void free_all(gsnp_context* c) {
                     c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_win_host_src, c->d_emit,
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-                    c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep};
+                    c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep, c->d_stream_ctl, c->d_leftover};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -677,7 +686,17 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         CK(dev_alloc(&c->d_bin_tiles, (size_t)n_tiles * 2 * kNumBins), "cudaMalloc bins");
         CK(dev_alloc(&c->d_warp_rng, (size_t)n_tiles * 2), "cudaMalloc ranges");
         CK(dev_alloc(&c->d_tile_rng, (size_t)n_tiles * 2), "cudaMalloc ranges");
+        CK(dev_alloc(&c->d_leftover, (size_t)n_tiles), "cudaMalloc leftover tiles");
         c->tiles_cap = n_tiles;
+    }
+    if (!c->d_stream_ctl) CK(dev_alloc(&c->d_stream_ctl, 2), "cudaMalloc stream counters");
+    if (c->stream_ctas_L != c->params.read_length || c->stream_slots == 0) {
+        /* the persistent kernel's grid: every resident CTA of the GPU */
+        if (c->stream_slots == 0) c->stream_slots = 48;
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
+        c->stream_ctas = sms * stream_ctas_per_sm(c->stream_slots, c->params.read_length);
+        c->stream_ctas_L = c->params.read_length;
     }
     if (c->dsite_cap == 0) {
         /* deferred sites: about 0.1% of a 30x genome; grown on demand */
@@ -788,16 +807,43 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         }
         CallArgs a = make_args(c);
         a.n_reads = c->n_gathered;
-        int k = begin(kKindClassify, 0, g.t1 - g.t0);
+        /* In the FP32 form the persistent kernel calls the segment's tiles;
+         * the binned kernels take only the tiles it leaves (the FP64 windows'
+         * and those with a site deeper than its record slots). */
+        const bool use_stream = c->stream_path && c->params.precision == 1;
+        int64_t n_left = 0;
+        auto run_stream = [&](const CallArgs& as) -> int {
+            CK(cudaMemsetAsync(c->d_stream_ctl, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
+            const StreamQueue q{g.t0, g.t1, c->d_stream_ctl, c->d_leftover, reinterpret_cast<int*>(c->d_stream_ctl + 1)};
+            const int ks = begin(kKindStream, c->stream_slots, g.t1 - g.t0);
+            CK(launch_stream(as, q, c->stream_slots, c->stream_ctas, c->stream), "persistent calling kernel");
+            end(ks);
+            return GSNP_OK;
+        };
         CK(launch_tile_bounds(a, g.dlo, g.dhi, g.next_pos, c->stream), "tile bounds kernel");
         for (int pass = 0; pass < (any_external ? 2 : 1); ++pass) {
-            if (pass == 1) k = begin(kKindClassify, 0, g.t1 - g.t0);
-            CK(launch_classify(a, pass, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
+            const bool stream_pass = use_stream && pass == 0;
+            if (stream_pass) {
+                CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+                const int rc = run_stream(a);
+                if (rc != GSNP_OK) return rc;
+                CK(to_map(c, c->d_stream_ctl + 1, kMapLeftover, sizeof(int)), "leftover count");
+                CK(cudaStreamSynchronize(c->stream), "persistent calling kernel");
+                int nl = 0;
+                memcpy(&nl, c->h_map + kMapLeftover, sizeof(int));
+                n_left = nl;
+            }
+            const int k = begin(kKindClassify, 0, use_stream ? n_left : g.t1 - g.t0);
+            if (use_stream)
+                CK(launch_classify(a, pass, 0, n_left, c->d_bin_count, c->d_bin_tiles, c->stream, c->d_leftover),
+                   "classify kernel");
+            else
+                CK(launch_classify(a, pass, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
             end(k);
             CK(to_map(c, c->d_bin_count, kMapBins, sizeof(c->h_bin_count)), "bin counts");
             CK(cudaStreamSynchronize(c->stream), "classify");
             memcpy(c->h_bin_count, c->h_map + kMapBins, sizeof(c->h_bin_count));
-            bool any_fast = false;
+            bool any_fast = stream_pass;
             for (int b = 0; b < kNumBins; ++b) any_fast |= c->h_bin_count[kNumBins + b] > 0;
             {
                 const int rc = launch_bins(a, kKindFP64, 0);
@@ -808,7 +854,14 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
                 CallArgs af = make_args(c);
                 af.n_reads = c->n_gathered;
                 const int first = c->n_launches;
-                CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+                if (!(stream_pass && attempt == 0))
+                    CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+                if (stream_pass && attempt > 0) {
+                    /* the pool was too small: the persistent kernel's
+                     * deferrals are appended again too */
+                    const int rc = run_stream(af);
+                    if (rc != GSNP_OK) return rc;
+                }
                 {
                     const int rc = launch_bins(af, kKindFast, kNumBins);
                     if (rc != GSNP_OK) return rc;
@@ -819,10 +872,10 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
                 const int64_t ns = (int64_t)c->h_dcount[0], nw = (int64_t)c->h_dcount[1];
                 if (ns <= c->dsite_cap && nw <= c->dpool_cap) {
                     if (ns > 0) {
-                        k = begin(kKindDeferred, 0, (ns + kTile - 1) / kTile);
-                        if (k >= 0) c->launches[k].sites = ns;
+                        const int kd = begin(kKindDeferred, 0, (ns + kTile - 1) / kTile);
+                        if (kd >= 0) c->launches[kd].sites = ns;
                         CK(launch_deferred(af, ns, c->stream), "deferred calling kernel");
-                        end(k);
+                        end(kd);
                     }
                     break;
                 }
@@ -1161,6 +1214,10 @@ int gsnp_context_create(int device, gsnp_context** out) {
         return GSNP_ERR_CUDA;
     }
     c->own_stream = true;
+    /* GSNP_CALL_PATH=binned: the FP32 form through the depth-binned kernels
+     * only; GSNP_STREAM_SLOTS: record slots of the persistent kernel (48, 64) */
+    if (const char* e = getenv("GSNP_CALL_PATH")) c->stream_path = strcmp(e, "binned") != 0;
+    if (const char* e = getenv("GSNP_STREAM_SLOTS")) c->stream_slots = atoi(e) > 48 ? 64 : 48;
     *out = c;
     return GSNP_OK;
 }

@@ -133,3 +133,27 @@ def test_deep_sites_pcr_dependency(pcr, tmp_path, oracle_bin, native_lib):
         if got != ref["cns"]:
             i, x, y = first_diff(got, ref["cns"])
             pytest.fail(f"-p {pcr}, precision {prec}: first differing row {i}:\n gpu   : {x!r}\n oracle: {y!r}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,scale", [("c1", 0.02), ("c2", 0.02), ("c4", 0.0101)])
+def test_persistent_and_binned_paths_agree(name, scale, native_lib, monkeypatch):
+    """The FP32 form's persistent kernel (tiles in genome order, leftover
+    tiles to the binned kernels) gives the same site calls, byte for byte, as
+    the depth-binned kernels alone, with 48 and with 64 record slots."""
+    w = synth.make_workload(name, scale=scale)
+    flags = [f for f in w.cli_flags("dbsnp") if f != "-C"]
+    calls = {}
+    for path, slots in (("binned", "48"), ("persistent", "48"), ("persistent", "64")):
+        monkeypatch.setenv("GSNP_CALL_PATH", path)
+        monkeypatch.setenv("GSNP_STREAM_SLOTS", slots)
+        c, _, _ = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
+        try:
+            calls[(path, slots)] = c.fetch()
+            kinds = {li["kind"] for li in c.last_launches()}
+        finally:
+            c.close()
+        assert (4 in kinds) == (path == "persistent")
+    base = calls[("binned", "48")].tobytes()
+    for key, v in calls.items():
+        assert v.tobytes() == base, f"{name}: {key} differs from the binned path"
