@@ -41,6 +41,7 @@
 
 #include "calling.cuh"
 #include "site_math.cuh"
+#include "tma.cuh"
 
 namespace gsnp {
 
@@ -83,6 +84,62 @@ __device__ __forceinline__ int lower_bound_s(const int32_t* a, int n, int64_t v)
     return lo;
 }
 
+/* Running pileup of one site: per-base counters packed - count_uni 4 x 8
+ * bits (at most 255 unique bases), q_sum and count_all 4 x 16 bits (a site
+ * deeper than 65535 is a capacity error) - and its record column. */
+struct PileupAcc {
+    uint32_t cu4 = 0;
+    uint64_t qs4 = 0, ca4 = 0;
+    uint32_t depth = 0, repeat = 0;
+    int dep_uni = 0, num = 0;
+    bool overflow = false;
+
+    /* one covering read's base (kernel/update_kernel.cu:278-325): bq is its
+     * base | quality << 8 at the site, lh its (len << 16) | hit */
+    template <int SLOTS>
+    __device__ __forceinline__ void take(uint32_t bq, uint32_t lh, int coord, int minus, signed char qmin,
+                                         uint32_t* recs) {
+        const int rlen = (int)(lh >> 16);
+        const uint32_t hit = lh & 0xffffu;
+        const signed char base = (signed char)(bq & 0xff);
+        const signed char qual = (signed char)(bq >> 8);
+        depth += 1;
+        repeat += hit;
+        if (base == 'N' || qual < qmin || dep_uni >= 0xFF) return;
+        const int sh = ((base >> 1) & 3) * 16;
+        if (hit == 1) {
+            dep_uni += 1;
+            const int q = qual - qmin;
+            const uint32_t coord_val = minus ? (uint32_t)(rlen - 1 - coord) : (uint32_t)coord;
+            const uint32_t w = make_record(base, q, coord_val, (uint32_t)minus);
+            if (num < SLOTS) {
+                recs[num * kTile] = w;
+                num += 1;
+            } else {
+                overflow = true;
+            }
+            cu4 += 1u << (sh >> 1);
+            qs4 += (uint64_t)(uint32_t)q << sh;
+        }
+        ca4 += 1ull << sh;
+    }
+
+    __device__ __forceinline__ PackedPileup finish(const CallArgs& a, bool* report_overflow) const {
+        if (report_overflow) *report_overflow = overflow;
+        else if (overflow) atomicExch(a.error, 2);
+        if (depth > 0xffff) atomicExch(a.error, 1);
+        PackedPileup pk;
+        pk.cu4 = cu4;
+        pk.qs4 = qs4;
+        pk.ca4 = ca4;
+        pk.depth = depth;
+        pk.repeat = repeat;
+        pk.dep_uni = (uint16_t)dep_uni;
+        pk.num = (uint16_t)num;
+        return pk;
+    }
+};
+
 /* Pileup of one warp's 32 consecutive sites (kernel/update_kernel.cu:260-325).
  * Reads [r_lo, r_hi) are those starting in [w0 - L + 1, w0 + 31]; their
  * positions, lengths and strands are loaded 32 at a time and broadcast, and
@@ -97,14 +154,7 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
     const int lane = threadIdx.x & 31;
     const int L = a.L;
     const signed char qmin = (signed char)a.qmin;
-    /* per-base counters packed: count_uni 4 x 8 bits (at most 255 unique
-     * bases), q_sum and count_all 4 x 16 bits (a site deeper than 65535 is a
-     * capacity error) */
-    uint32_t cu4 = 0;
-    uint64_t qs4 = 0, ca4 = 0;
-    uint32_t depth = 0, repeat = 0;
-    int dep_uni = 0, num = 0;
-    bool overflow = false;
+    PileupAcc acc;
     for (int64_t rb = r_lo; rb < r_hi; rb += 32) {
         const int64_t r = rb + lane;
         int32_t mpos = 0;
@@ -134,47 +184,44 @@ __device__ __forceinline__ PackedPileup warp_pileup(const CallArgs& a, int64_t r
                 bqv[u] = covv[u] ? (uint32_t)__ldg(rows + k * L + coordv[u]) : 0u;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (!covv[u]) continue;
-                const int coord = coordv[u], minus = minusv[u];
-                const int rlen = (int)(lhv[u] >> 16);
-                const uint32_t hit = lhv[u] & 0xffffu;
-                const signed char base = (signed char)(bqv[u] & 0xff);
-                const signed char qual = (signed char)(bqv[u] >> 8);
-                depth += 1;
-                repeat += hit;
-                if (base == 'N' || qual < qmin || dep_uni >= 0xFF) continue;
-                const int sh = ((base >> 1) & 3) * 16;
-                if (hit == 1) {
-                    dep_uni += 1;
-                    const int q = qual - qmin;
-                    const uint32_t coord_val = minus ? (uint32_t)(rlen - 1 - coord) : (uint32_t)coord;
-                    const uint32_t w = make_record(base, q, coord_val, (uint32_t)minus);
-                    if (num < SLOTS) {
-                        recs[num * kTile] = w;
-                        num += 1;
-                    } else {
-                        overflow = true;
-                    }
-                    cu4 += 1u << (sh >> 1);
-                    qs4 += (uint64_t)(uint32_t)q << sh;
-                }
-                ca4 += 1ull << sh;
-            }
+            for (int u = 0; u < 4; ++u)
+                if (covv[u]) acc.take<SLOTS>(bqv[u], lhv[u], coordv[u], minusv[u], qmin, recs);
         }
     }
-    if (report_overflow) *report_overflow = overflow;
-    else if (overflow) atomicExch(a.error, 2);
-    if (depth > 0xffff) atomicExch(a.error, 1);
-    PackedPileup pk;
-    pk.cu4 = cu4;
-    pk.qs4 = qs4;
-    pk.ca4 = ca4;
-    pk.depth = depth;
-    pk.repeat = repeat;
-    pk.dep_uni = (uint16_t)dep_uni;
-    pk.num = (uint16_t)num;
-    return pk;
+    return acc.finish(a, report_overflow);
+}
+
+/* The reads of a tile staged in shared memory by the persistent kernel: per
+ * read its start, (len << 16) | hit with the strand in bit 31, and the byte
+ * offset in `rows` that column 0 of its row would have; the bulk copy of the
+ * read holds the columns that cover the tile. */
+struct StagedReads {
+    const int32_t* pos;
+    const uint32_t* lhs;
+    const int32_t* rbase;
+    const uint8_t* rows;
+    int n;
+};
+
+/* warp_pileup over staged reads: the same records and counts, read from
+ * shared memory (broadcast loads of the per-read values, one 16-bit load
+ * per covering read and lane). */
+template <int SLOTS>
+__device__ __forceinline__ PackedPileup warp_pileup_staged(const CallArgs& a, const StagedReads& sr, int64_t site,
+                                                          bool active, uint32_t* recs, bool* report_overflow) {
+    const signed char qmin = (signed char)a.qmin;
+    PileupAcc acc;
+    for (int k = 0; k < sr.n; ++k) {
+        const int32_t start = sr.pos[k];
+        const uint32_t lhs = sr.lhs[k];
+        const int coord = (int)(site - start);
+        const uint32_t lh = lhs & 0x7fffffffu;
+        if (active && coord >= 0 && coord < (int)(lh >> 16)) {
+            const uint32_t bq = *reinterpret_cast<const uint16_t*>(sr.rows + sr.rbase[k] + 2 * coord);
+            acc.take<SLOTS>(bq, lh, coord, (int)(lhs >> 31), qmin, recs);
+        }
+    }
+    return acc.finish(a, report_overflow);
 }
 
 /* dbSNP row of each flagged site of a tile: the rows before the tile plus the
@@ -476,21 +523,25 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
  * dependency walk, the compensated sums, the FP32 posterior, and the append
  * of the site to the deferred pool when its call is not proven.  Every lane
  * of the warp calls it (the appends are warp-aggregated). */
-template <int SLOTS>
+template <int SLOTS, bool FUSED = false>
 __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool active, uint8_t ori, uint8_t wflags,
                                           int32_t snp_row, const SitePileup& p, uint32_t* recs, uint32_t* seen) {
     const int lane = threadIdx.x & 31;
     uint8_t dflags = 0;
     if (active) {
         if (wflags & kWinKeepCounts) store_counts(a, site, p);
+        Kahan10 k;
+        k.init();
+        if (FUSED) {
+            /* walk and sums in one pass; the column keeps its records */
+            walk_sum32<kPcrBits(SLOTS, true)>(a, recs, seen, kTile, p.num, k);
+        } else {
         /* adjusted quality of each record, written over its occurrence byte */
         walk_records<true, kPcrBits(SLOTS, true)>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
             recs[i * kTile] = (recs[i * kTile] & ~0xffu) | (uint32_t)qa;
         });
         /* FP32 sums, four records per compensated step (the grouping of
          * likelihood_fp32) */
-        Kahan10 k;
-        k.init();
         for (int i = 0; i < p.num; i += 4) {
             float x[10], y[10];
             uint32_t w = recs[i * kTile];
@@ -515,6 +566,7 @@ __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool 
                 for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
             }
             k.add(x);
+        }
         }
         SiteCall call;
         if ((site & 4095) == 0 && a.stats) dflags = kCallSampled;
@@ -564,7 +616,10 @@ __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool 
     for (int i = 0; i < 3; ++i) d.pad[i] = 0;
     a.dsites[slot] = d;
     uint32_t* dst = a.dpool + off;
-    for (int i = 0; i < p.num; ++i) dst[i] = (recs[i * kTile] & ~0xffu) | 1u;
+    if (FUSED)
+        for (int i = 0; i < p.num; ++i) dst[i] = recs[i * kTile];
+    else
+        for (int i = 0; i < p.num; ++i) dst[i] = (recs[i * kTile] & ~0xffu) | 1u;
 }
 
 /* Sites whose call is not proven in FP32 (and every 4096th site, sampled for
@@ -602,6 +657,9 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
 /* the persistent FP32 calling kernel                                        */
 /* ------------------------------------------------------------------------ */
 
+/* The persistent kernel walks and sums each column in one pass (walk_sum32). */
+constexpr bool kStreamFused = true;
+
 /* Column sort for a tile whose deepest column holds tile_max records
  * (warp-uniform): the chunk network past the first 32 records is sized for
  * the tile, not for the kernel's slot capacity. */
@@ -613,6 +671,17 @@ __device__ __forceinline__ void sort_column_upto(uint32_t* recs, int num, int ti
     else sort_column<SLOTS>(recs, num);
 }
 
+/* Reads of a tile staged in shared memory by the persistent kernel, and the
+ * bytes of each read's row window (32 columns of 16-bit base|quality plus up
+ * to 14 bytes before them, to start the copy on a 16-byte boundary).  A tile
+ * with more reads than this (deep pileups) reads its rows from global memory
+ * instead. */
+constexpr int kStageReads = 56;
+constexpr int kStageSlot = 80;
+constexpr uint64_t kStageWaitNs = 1000000000ull;   /* bound on one wait for a tile's bulk copies */
+constexpr int kStageHeader = 16 + kStageReads * 12;
+static_assert(kStageHeader % 16 == 0 && kStageSlot % 16 == 0, "staging buffers are 16-byte aligned");
+
 /* One launch over the FP32 windows' tiles of a segment: each warp takes
  * kStreamChunk consecutive tiles at a time from a counter, so the tiles in
  * flight are neighbours and the read rows they share are fetched from DRAM
@@ -620,49 +689,154 @@ __device__ __forceinline__ void sort_column_upto(uint32_t* recs, int num, int ti
  * whatever the segment's length.  A tile whose window needs the FP64 form
  * (its likelihood is kept for, or taken from, another window), or one with a
  * site of more than SLOTS records, is appended to the leftover list for the
- * binned kernels instead. */
-template <int SLOTS>
+ * binned kernels instead.
+ *
+ * STAGED: as soon as a tile's pileup is done, the warp stages the next
+ * tile's reads in shared memory - their start, length and strand with plain
+ * loads, and each covering read's 32-column row window with one bulk copy
+ * (cp.async.bulk) completing on the warp's mbarrier - so that the copies run
+ * while the current tile is sorted, walked and summed, and the next pileup
+ * reads only shared memory.  A wait for the copies that does not complete
+ * within kStageWaitNs sets error code 5 and ends the warp. */
+template <int SLOTS, bool STAGED>
 __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(CallArgs a, StreamQueue q) {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);
+    uint8_t* base = smem;
+    uint64_t* bar = nullptr;
+    int32_t* s_pos = nullptr;
+    uint32_t* s_lhs = nullptr;
+    int32_t* s_rbase = nullptr;
+    uint8_t* s_rows = nullptr;
+    if (STAGED) {
+        bar = reinterpret_cast<uint64_t*>(base);
+        s_pos = reinterpret_cast<int32_t*>(base + 16);
+        s_lhs = reinterpret_cast<uint32_t*>(s_pos + kStageReads);
+        s_rbase = reinterpret_cast<int32_t*>(s_lhs + kStageReads);
+        s_rows = base + kStageHeader;
+        base = s_rows + kStageReads * kStageSlot;
+    }
+    uint32_t* recs_all = reinterpret_cast<uint32_t*>(base);
     uint32_t* seen_all = recs_all + SLOTS * kTile;
     const int t = threadIdx.x;
     uint32_t* recs = recs_all + t;
     uint32_t* seen = seen_all + t;
     const int64_t n = q.t_end - q.t_begin;
-    for (;;) {
-        unsigned long long first = 0;
-        if (t == 0) first = atomicAdd(q.next, (unsigned long long)kStreamChunk);
-        first = __shfl_sync(kFull, first, 0);
-        if ((int64_t)first >= n) break;
-        const int64_t last = min((int64_t)first + kStreamChunk, n);
-        for (int64_t k = (int64_t)first; k < last; ++k) {
-            const int64_t tile = q.t_begin + k;
-            const int64_t s0 = tile * kTile;
-            const int win = (int)(s0 / kWin);
-            const uint8_t wflags = a.win_flags[win];
-            if (wflags & (kWinKeepLik | kWinExternalLik)) {
-                if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
-                continue;
+
+    /* tiles in order: kStreamChunk at a time from the counter; -1 at the end */
+    int64_t chunk_next = 0, chunk_end = 0;
+    auto next_tile = [&]() -> int64_t {
+        if (chunk_next >= chunk_end) {
+            unsigned long long first = 0;
+            if (t == 0) first = atomicAdd(q.next, (unsigned long long)kStreamChunk);
+            first = __shfl_sync(kFull, first, 0);
+            chunk_next = (int64_t)first;
+            chunk_end = min(chunk_next + (int64_t)kStreamChunk, n);
+            if (chunk_next >= n) {
+                chunk_end = 0;
+                return -1;
             }
-            const int64_t r_lo = a.tile_rng[tile * 2];
-            const int64_t r_hi = a.tile_rng[tile * 2 + 1];
-            const int64_t site = s0 + t;
-            const bool active = site < a.chr_len;
-            const uint8_t ori = active ? __ldg(a.ori + site) : 0;
-            const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
-            bool overflow = false;
-            const SitePileup p = warp_pileup<SLOTS>(a, r_lo, r_hi, site, active, recs, &overflow).unpack();
-            if (__any_sync(kFull, overflow)) {
-                if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
-                continue;
+        }
+        return q.t_begin + chunk_next++;
+    };
+    auto fp64_window = [&](int64_t tile) {
+        return (a.win_flags[(int)(tile * kTile / kWin)] & (kWinKeepLik | kWinExternalLik)) != 0;
+    };
+    /* stage the reads of `tile` (see above); their count, or -1 when the
+     * tile is not staged.  Every lane calls it, after its last read of the
+     * buffers. */
+    auto stage = [&](int64_t tile) -> int {
+        if (!STAGED || tile < 0 || fp64_window(tile)) return -1;
+        const int64_t r_lo = a.tile_rng[tile * 2], r_hi = a.tile_rng[tile * 2 + 1];
+        const int64_t nr = r_hi - r_lo;
+        if (nr > kStageReads) return -1;
+        const int64_t s0 = tile * kTile;
+        uint32_t bytes[2] = {0u, 0u}, total = 0;
+        const uint8_t* src[2] = {nullptr, nullptr};
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int k = t + 32 * j;
+            if (k >= nr) continue;
+            const int64_t r = r_lo + k;
+            const int32_t pos = __ldg(a.pos + r);
+            const uint32_t lh = (uint32_t)__ldg(a.lenhit + r);
+            const uint32_t minus = __ldg(a.strand + r) != '+';
+            const int len = (int)(lh >> 16);
+            const int c_lo = max(0, (int)(s0 - pos));
+            const int c_hi = min(len, (int)(s0 + kTile - pos));
+            const int64_t e_lo = (r * a.L + c_lo) * 2;   /* byte offset of column c_lo in the rows */
+            const int m = (int)(e_lo & 15);
+            if (c_hi > c_lo) {
+                bytes[j] = (uint32_t)((m + 2 * (c_hi - c_lo) + 15) & ~15);
+                src[j] = reinterpret_cast<const uint8_t*>(a.bq) + (e_lo - m);
             }
+            s_pos[k] = pos;
+            s_lhs[k] = lh | (minus << 31);
+            s_rbase[k] = k * kStageSlot + m - 2 * c_lo;
+            total += bytes[j];
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(kFull, total, off);
+        /* this lane's reads of the rows are done before the copies overwrite them */
+        fence_proxy_async_smem();
+        if (t == 0) mbar_arrive_expect_tx(bar, total);
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            if (bytes[j]) bulk_copy_g2s(s_rows + (t + 32 * j) * kStageSlot, src[j], bytes[j], bar);
+        return (int)nr;
+    };
+
+    uint32_t phase = 0;
+    if (STAGED) {
+        if (t == 0) mbar_init(bar, 1);
+        __syncwarp();
+    }
+    int64_t tile = next_tile();
+    int staged_n = stage(tile);
+    while (tile >= 0) {
+        const int64_t s0 = tile * kTile;
+        const int win = (int)(s0 / kWin);
+        const uint8_t wflags = a.win_flags[win];
+        const int64_t nxt = next_tile();
+        if (wflags & (kWinKeepLik | kWinExternalLik)) {
+            if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
+            tile = nxt;
+            staged_n = stage(tile);
+            continue;
+        }
+        const int64_t site = s0 + t;
+        const bool active = site < a.chr_len;
+        const uint8_t ori = active ? __ldg(a.ori + site) : 0;
+        const int32_t snp_row = tile_snp_row(a, tile, (ori & 8) != 0);
+        bool overflow = false;
+        SitePileup p;
+        if (STAGED && staged_n >= 0) {
+            if (!mbar_wait_bounded(bar, phase, kStageWaitNs)) {
+                if (t == 0) atomicExch(a.error, 5);
+                (void)mbar_wait_bounded(bar, phase, kStageWaitNs);
+                return;
+            }
+            phase ^= 1u;
+            const StagedReads sr{s_pos, s_lhs, s_rbase, s_rows, staged_n};
+            p = warp_pileup_staged<SLOTS>(a, sr, site, active, recs, &overflow).unpack();
+        } else {
+            p = warp_pileup<SLOTS>(a, a.tile_rng[tile * 2], a.tile_rng[tile * 2 + 1], site, active, recs, &overflow)
+                    .unpack();
+        }
+        /* the staging buffers are free: stage the next tile now, so that its
+         * copies run while this one is sorted, walked and summed */
+        const int staged_next = stage(nxt);
+        if (__any_sync(kFull, overflow)) {
+            if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
+        } else {
             int tile_max = active ? p.num : 0;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) tile_max = max(tile_max, __shfl_xor_sync(kFull, tile_max, off));
             if (active) sort_column_upto<SLOTS>(recs, p.num, tile_max);
-            fast_site<SLOTS>(a, site, active, ori, wflags, snp_row, p, recs, seen);
+            fast_site<SLOTS, kStreamFused>(a, site, active, ori, wflags, snp_row, p, recs, seen);
         }
+        tile = nxt;
+        staged_n = staged_next;
     }
 }
 
@@ -749,29 +923,46 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_
     return cudaGetLastError();
 }
 
-size_t stream_smem_bytes(int slots, int L) { return call_smem_bytes(slots, L, true); }
+size_t stream_smem_bytes(int slots, int L, bool staged) {
+    return call_smem_bytes(slots, L, true) + (staged ? (size_t)kStageHeader + (size_t)kStageReads * kStageSlot : 0);
+}
 
-template <int SLOTS>
-static cudaError_t launch_stream_one(const CallArgs& a, const StreamQueue& q, int ctas, cudaStream_t stream) {
-    const int smem = (int)stream_smem_bytes(SLOTS, a.L);
-    cudaError_t e = cudaFuncSetAttribute(call_stream_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+template <int SLOTS, bool STAGED>
+static cudaError_t stream_attr(int L, int* ctas_per_sm, int carveout = 0) {
+    const int smem = (int)stream_smem_bytes(SLOTS, L, STAGED);
+    cudaError_t e =
+        cudaFuncSetAttribute(call_stream_kernel<SLOTS, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess && carveout > 0 &&
+        cudaFuncSetAttribute(call_stream_kernel<SLOTS, STAGED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             carveout) != cudaSuccess)
+        (void)cudaGetLastError();
+    if (e == cudaSuccess && ctas_per_sm)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, call_stream_kernel<SLOTS, STAGED>, kTile, smem);
+    return e;
+}
+
+template <int SLOTS, bool STAGED>
+static cudaError_t launch_stream_one(const CallArgs& a, const StreamQueue& q, int ctas, int carveout,
+                                     cudaStream_t stream) {
+    cudaError_t e = stream_attr<SLOTS, STAGED>(a.L, nullptr);
     if (e != cudaSuccess) return e;
-    call_stream_kernel<SLOTS><<<ctas, kTile, smem, stream>>>(a, q);
+    /* a preferred shared-memory carveout (percent; 0 leaves the default) is a
+     * hint: a refusal only costs speed, and its error is cleared */
+    if (carveout > 0 &&
+        cudaFuncSetAttribute(call_stream_kernel<SLOTS, STAGED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             carveout) != cudaSuccess)
+        (void)cudaGetLastError();
+    call_stream_kernel<SLOTS, STAGED><<<ctas, kTile, stream_smem_bytes(SLOTS, a.L, STAGED), stream>>>(a, q);
     return cudaGetLastError();
 }
 
-/* resident CTAs of the persistent kernel of `slots` record slots on one SM */
-int stream_ctas_per_sm(int slots, int L) {
+/* resident CTAs on one SM of the persistent kernel with `slots` record
+ * slots (48 or 64), staged or not */
+int stream_ctas_per_sm(int slots, int L, bool staged, int carveout) {
     int n = 0;
-    const int smem = (int)stream_smem_bytes(slots, L);
     cudaError_t e;
-    if (slots <= 48) {
-        e = cudaFuncSetAttribute(call_stream_kernel<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, call_stream_kernel<48>, kTile, smem);
-    } else {
-        e = cudaFuncSetAttribute(call_stream_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, call_stream_kernel<64>, kTile, smem);
-    }
+    if (slots <= 48) e = staged ? stream_attr<48, true>(L, &n, carveout) : stream_attr<48, false>(L, &n, carveout);
+    else e = staged ? stream_attr<64, true>(L, &n, carveout) : stream_attr<64, false>(L, &n, carveout);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         return 1;
@@ -781,9 +972,14 @@ int stream_ctas_per_sm(int slots, int L) {
 
 /* The persistent FP32 kernel over q's tiles with `ctas` CTAs; slots is 48 or
  * 64.  q.next and q.n_leftover must be zero. */
-cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int ctas, cudaStream_t stream) {
+cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, bool staged, int ctas, int carveout,
+                          cudaStream_t stream) {
     if (q.t_end <= q.t_begin) return cudaSuccess;
-    return slots <= 48 ? launch_stream_one<48>(a, q, ctas, stream) : launch_stream_one<64>(a, q, ctas, stream);
+    if (slots <= 48)
+        return staged ? launch_stream_one<48, true>(a, q, ctas, carveout, stream)
+                      : launch_stream_one<48, false>(a, q, ctas, carveout, stream);
+    return staged ? launch_stream_one<64, true>(a, q, ctas, carveout, stream)
+                  : launch_stream_one<64, false>(a, q, ctas, carveout, stream);
 }
 
 template <int SLOTS>

@@ -37,8 +37,9 @@ namespace gsnp {
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
                             int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list = nullptr);
-cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int ctas, cudaStream_t stream);
-int stream_ctas_per_sm(int slots, int L);
+cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, bool staged, int ctas, int carveout,
+                          cudaStream_t stream);
+int stream_ctas_per_sm(int slots, int L, bool staged, int carveout);
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
@@ -400,8 +401,8 @@ struct gsnp_context {
      * count), the leftover tiles, its record slots and grid */
     unsigned long long* d_stream_ctl = nullptr;
     int32_t* d_leftover = nullptr;
-    int stream_slots = 0, stream_ctas = 0, stream_ctas_L = -1;
-    bool stream_path = true;
+    int stream_slots = 0, stream_ctas = 0, stream_ctas_L = -1, stream_carveout = 0;
+    bool stream_path = true, stream_staged = true;
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
@@ -695,7 +696,8 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         if (c->stream_slots == 0) c->stream_slots = 48;
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
-        c->stream_ctas = sms * stream_ctas_per_sm(c->stream_slots, c->params.read_length);
+        c->stream_ctas =
+            sms * stream_ctas_per_sm(c->stream_slots, c->params.read_length, c->stream_staged, c->stream_carveout);
         c->stream_ctas_L = c->params.read_length;
     }
     if (c->dsite_cap == 0) {
@@ -816,7 +818,8 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             CK(cudaMemsetAsync(c->d_stream_ctl, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
             const StreamQueue q{g.t0, g.t1, c->d_stream_ctl, c->d_leftover, reinterpret_cast<int*>(c->d_stream_ctl + 1)};
             const int ks = begin(kKindStream, c->stream_slots, g.t1 - g.t0);
-            CK(launch_stream(as, q, c->stream_slots, c->stream_ctas, c->stream), "persistent calling kernel");
+            CK(launch_stream(as, q, c->stream_slots, c->stream_staged, c->stream_ctas, c->stream_carveout, c->stream),
+               "persistent calling kernel");
             end(ks);
             return GSNP_OK;
         };
@@ -903,6 +906,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
     memcpy(c->stats, c->h_map + kMapStats, sizeof(c->stats));
     for (int k = 0; k < c->n_launches; ++k) cudaEventElapsedTime(&c->launches[k].ms, c->ev[2 * k], c->ev[2 * k + 1]);
     if (err == 1) return fail(c, GSNP_ERR_CAPACITY, "a site is covered by more than 65535 alignments");
+    if (err == 5) return fail(c, GSNP_ERR_STATE, "a staging bulk copy of the calling kernel did not complete");
     if (err) return fail(c, GSNP_ERR_STATE, "record slots of a tile overflowed its depth bin");
     c->stats[0] = (uint64_t)c->chr_len;
     c->called = true;
@@ -1082,7 +1086,9 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(dev_alloc(&c->d_lenhit, (size_t)nd), "cudaMalloc reads");
         CK(dev_alloc(&c->d_len, (size_t)nd), "cudaMalloc reads");
         CK(dev_alloc(&c->d_strand, (size_t)nd), "cudaMalloc reads");
-        CK(dev_alloc(&c->d_bq, (size_t)nd * L + 8), "cudaMalloc reads");
+        /* 64 elements of slack: the staging bulk copies of the persistent
+         * kernel round a row window up to 16 bytes past the last row */
+        CK(dev_alloc(&c->d_bq, (size_t)nd * L + 64), "cudaMalloc reads");
         c->cap_dep = nd;
     }
     c->n_dep = nd;
@@ -1215,9 +1221,13 @@ int gsnp_context_create(int device, gsnp_context** out) {
     }
     c->own_stream = true;
     /* GSNP_CALL_PATH=binned: the FP32 form through the depth-binned kernels
-     * only; GSNP_STREAM_SLOTS: record slots of the persistent kernel (48, 64) */
+     * only; GSNP_STREAM_SLOTS: record slots of the persistent kernel (48, 64);
+     * GSNP_STREAM_STAGED=0: its reads from global memory, not staged;
+     * GSNP_STREAM_CARVEOUT: its preferred shared-memory carveout, percent */
     if (const char* e = getenv("GSNP_CALL_PATH")) c->stream_path = strcmp(e, "binned") != 0;
     if (const char* e = getenv("GSNP_STREAM_SLOTS")) c->stream_slots = atoi(e) > 48 ? 64 : 48;
+    if (const char* e = getenv("GSNP_STREAM_STAGED")) c->stream_staged = atoi(e) != 0;
+    if (const char* e = getenv("GSNP_STREAM_CARVEOUT")) c->stream_carveout = std::max(0, std::min(100, atoi(e)));
     *out = c;
     return GSNP_OK;
 }
