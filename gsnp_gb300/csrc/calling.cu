@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
  * dependency walk, the compensated sums, the FP32 posterior, and the append
  * of the site to the deferred pool when its call is not proven.  Every lane
  * of the warp calls it (the appends are warp-aggregated). */
-template <int SLOTS, bool FUSED = false>
+template <int SLOTS>
 __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool active, uint8_t ori, uint8_t wflags,
                                           int32_t snp_row, const SitePileup& p, uint32_t* recs, uint32_t* seen) {
     const int lane = threadIdx.x & 31;
@@ -532,10 +532,6 @@ __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool 
         if (wflags & kWinKeepCounts) store_counts(a, site, p);
         Kahan10 k;
         k.init();
-        if (FUSED) {
-            /* walk and sums in one pass; the column keeps its records */
-            walk_sum32<kPcrBits(SLOTS, true)>(a, recs, seen, kTile, p.num, k);
-        } else {
         /* adjusted quality of each record, written over its occurrence byte */
         walk_records<true, kPcrBits(SLOTS, true)>(a, recs, seen, kTile, p.num, [&](int i, int qa, int, int) {
             recs[i * kTile] = (recs[i * kTile] & ~0xffu) | (uint32_t)qa;
@@ -566,7 +562,6 @@ __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool 
                 for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
             }
             k.add(x);
-        }
         }
         SiteCall call;
         if ((site & 4095) == 0 && a.stats) dflags = kCallSampled;
@@ -616,10 +611,7 @@ __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool 
     for (int i = 0; i < 3; ++i) d.pad[i] = 0;
     a.dsites[slot] = d;
     uint32_t* dst = a.dpool + off;
-    if (FUSED)
-        for (int i = 0; i < p.num; ++i) dst[i] = recs[i * kTile];
-    else
-        for (int i = 0; i < p.num; ++i) dst[i] = (recs[i * kTile] & ~0xffu) | 1u;
+    for (int i = 0; i < p.num; ++i) dst[i] = (recs[i * kTile] & ~0xffu) | 1u;
 }
 
 /* Sites whose call is not proven in FP32 (and every 4096th site, sampled for
@@ -657,20 +649,6 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
 /* the persistent FP32 calling kernel                                        */
 /* ------------------------------------------------------------------------ */
 
-/* The persistent kernel walks and sums each column in one pass (walk_sum32). */
-constexpr bool kStreamFused = true;
-
-/* Column sort for a tile whose deepest column holds tile_max records
- * (warp-uniform): the chunk network past the first 32 records is sized for
- * the tile, not for the kernel's slot capacity. */
-template <int SLOTS>
-__device__ __forceinline__ void sort_column_upto(uint32_t* recs, int num, int tile_max) {
-    if (tile_max <= 32) sort_column<32>(recs, num);
-    else if (tile_max <= 40) sort_column<40>(recs, num);
-    else if (tile_max <= 48 || SLOTS <= 48) sort_column<(SLOTS < 48 ? SLOTS : 48)>(recs, num);
-    else sort_column<SLOTS>(recs, num);
-}
-
 /* Reads of a tile staged in shared memory by the persistent kernel, and the
  * bytes of each read's row window (32 columns of 16-bit base|quality plus up
  * to 14 bytes before them, to start the copy on a 16-byte boundary).  A tile
@@ -680,6 +658,10 @@ constexpr int kStageReads = 56;
 constexpr int kStageSlot = 80;
 constexpr uint64_t kStageWaitNs = 1000000000ull;   /* bound on one wait for a tile's bulk copies */
 constexpr int kStageHeader = 16 + kStageReads * 12;
+/* how the persistent kernel fetches a tile's reads */
+constexpr int kStreamPlain = 0;      /* loads from global memory (through L1/L2) */
+constexpr int kStreamPrefetch = 1;   /* the same, after a bulk prefetch of the rows into L2 */
+constexpr int kStreamStaged = 2;     /* bulk copies into shared memory, one tile ahead */
 static_assert(kStageHeader % 16 == 0 && kStageSlot % 16 == 0, "staging buffers are 16-byte aligned");
 
 /* One launch over the FP32 windows' tiles of a segment: each warp takes
@@ -691,15 +673,19 @@ static_assert(kStageHeader % 16 == 0 && kStageSlot % 16 == 0, "staging buffers a
  * site of more than SLOTS records, is appended to the leftover list for the
  * binned kernels instead.
  *
- * STAGED: as soon as a tile's pileup is done, the warp stages the next
- * tile's reads in shared memory - their start, length and strand with plain
+ * MODE kStreamPrefetch: as soon as a warp takes a tile, it asks the
+ * bulk-copy unit to prefetch the next tile's read rows into L2
+ * (cp.async.bulk.prefetch), which costs no shared memory.
+ * MODE kStreamStaged: as soon as a tile's pileup is done, the warp stages the
+ * next tile's reads in shared memory - their start, length and strand with plain
  * loads, and each covering read's 32-column row window with one bulk copy
  * (cp.async.bulk) completing on the warp's mbarrier - so that the copies run
  * while the current tile is sorted, walked and summed, and the next pileup
  * reads only shared memory.  A wait for the copies that does not complete
  * within kStageWaitNs sets error code 5 and ends the warp. */
-template <int SLOTS, bool STAGED>
+template <int SLOTS, int MODE>
 __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(CallArgs a, StreamQueue q) {
+    constexpr bool STAGED = MODE == kStreamStaged;
     extern __shared__ __align__(16) uint8_t smem[];
     uint8_t* base = smem;
     uint64_t* bar = nullptr;
@@ -786,6 +772,18 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(Call
         return (int)nr;
     };
 
+    /* the read rows of `tile` into L2 (the rows of a tile's reads are one
+     * contiguous block; the bulk unit wants 16-byte bounds, and the row
+     * array has slack past its end for the rounding) */
+    auto prefetch_l2 = [&](int64_t tile) {
+        if (MODE != kStreamPrefetch || tile < 0 || t != 0) return;
+        const int64_t r_lo = a.tile_rng[tile * 2], r_hi = a.tile_rng[tile * 2 + 1];
+        if (r_hi <= r_lo) return;
+        const uintptr_t lo = reinterpret_cast<uintptr_t>(a.bq + r_lo * a.L) & ~(uintptr_t)15;
+        const uintptr_t hi = (reinterpret_cast<uintptr_t>(a.bq + r_hi * a.L) + 15) & ~(uintptr_t)15;
+        bulk_prefetch_l2(reinterpret_cast<const void*>(lo), (uint32_t)(hi - lo));
+    };
+
     uint32_t phase = 0;
     if (STAGED) {
         if (t == 0) mbar_init(bar, 1);
@@ -798,6 +796,7 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(Call
         const int win = (int)(s0 / kWin);
         const uint8_t wflags = a.win_flags[win];
         const int64_t nxt = next_tile();
+        prefetch_l2(nxt);
         if (wflags & (kWinKeepLik | kWinExternalLik)) {
             if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
             tile = nxt;
@@ -829,11 +828,10 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(Call
         if (__any_sync(kFull, overflow)) {
             if (t == 0) q.leftover[atomicAdd(q.n_leftover, 1)] = (int32_t)tile;
         } else {
-            int tile_max = active ? p.num : 0;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) tile_max = max(tile_max, __shfl_xor_sync(kFull, tile_max, off));
-            if (active) sort_column_upto<SLOTS>(recs, p.num, tile_max);
-            fast_site<SLOTS, kStreamFused>(a, site, active, ori, wflags, snp_row, p, recs, seen);
+            /* one sort network for every tile: specialised networks per
+             * tile depth made the kernel's code larger and it ran slower */
+            if (active) sort_column<SLOTS>(recs, p.num);
+            fast_site<SLOTS>(a, site, active, ori, wflags, snp_row, p, recs, seen);
         }
         tile = nxt;
         staged_n = staged_next;
@@ -923,46 +921,56 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_
     return cudaGetLastError();
 }
 
-size_t stream_smem_bytes(int slots, int L, bool staged) {
-    return call_smem_bytes(slots, L, true) + (staged ? (size_t)kStageHeader + (size_t)kStageReads * kStageSlot : 0);
+size_t stream_smem_bytes(int slots, int L, int mode) {
+    return call_smem_bytes(slots, L, true) +
+           (mode == kStreamStaged ? (size_t)kStageHeader + (size_t)kStageReads * kStageSlot : 0);
 }
 
-template <int SLOTS, bool STAGED>
+template <int SLOTS, int MODE>
 static cudaError_t stream_attr(int L, int* ctas_per_sm, int carveout = 0) {
-    const int smem = (int)stream_smem_bytes(SLOTS, L, STAGED);
+    const int smem = (int)stream_smem_bytes(SLOTS, L, MODE);
     cudaError_t e =
-        cudaFuncSetAttribute(call_stream_kernel<SLOTS, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(call_stream_kernel<SLOTS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    /* a preferred shared-memory carveout (percent; 0 leaves the default) is a
+     * hint: a refusal only costs speed, and its error is cleared */
     if (e == cudaSuccess && carveout > 0 &&
-        cudaFuncSetAttribute(call_stream_kernel<SLOTS, STAGED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        cudaFuncSetAttribute(call_stream_kernel<SLOTS, MODE>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              carveout) != cudaSuccess)
         (void)cudaGetLastError();
     if (e == cudaSuccess && ctas_per_sm)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, call_stream_kernel<SLOTS, STAGED>, kTile, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, call_stream_kernel<SLOTS, MODE>, kTile, smem);
     return e;
 }
 
-template <int SLOTS, bool STAGED>
+template <int SLOTS, int MODE>
 static cudaError_t launch_stream_one(const CallArgs& a, const StreamQueue& q, int ctas, int carveout,
                                      cudaStream_t stream) {
-    cudaError_t e = stream_attr<SLOTS, STAGED>(a.L, nullptr);
+    cudaError_t e = stream_attr<SLOTS, MODE>(a.L, nullptr, carveout);
     if (e != cudaSuccess) return e;
-    /* a preferred shared-memory carveout (percent; 0 leaves the default) is a
-     * hint: a refusal only costs speed, and its error is cleared */
-    if (carveout > 0 &&
-        cudaFuncSetAttribute(call_stream_kernel<SLOTS, STAGED>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             carveout) != cudaSuccess)
-        (void)cudaGetLastError();
-    call_stream_kernel<SLOTS, STAGED><<<ctas, kTile, stream_smem_bytes(SLOTS, a.L, STAGED), stream>>>(a, q);
+    call_stream_kernel<SLOTS, MODE><<<ctas, kTile, stream_smem_bytes(SLOTS, a.L, MODE), stream>>>(a, q);
     return cudaGetLastError();
 }
 
+template <int SLOTS>
+static cudaError_t stream_dispatch(int mode, const CallArgs* a, const StreamQueue* q, int ctas, int carveout,
+                                   cudaStream_t stream, int L, int* ctas_per_sm) {
+    if (!a) {
+        return mode == kStreamStaged     ? stream_attr<SLOTS, kStreamStaged>(L, ctas_per_sm, carveout)
+               : mode == kStreamPrefetch ? stream_attr<SLOTS, kStreamPrefetch>(L, ctas_per_sm, carveout)
+                                         : stream_attr<SLOTS, kStreamPlain>(L, ctas_per_sm, carveout);
+    }
+    return mode == kStreamStaged     ? launch_stream_one<SLOTS, kStreamStaged>(*a, *q, ctas, carveout, stream)
+           : mode == kStreamPrefetch ? launch_stream_one<SLOTS, kStreamPrefetch>(*a, *q, ctas, carveout, stream)
+                                     : launch_stream_one<SLOTS, kStreamPlain>(*a, *q, ctas, carveout, stream);
+}
+
 /* resident CTAs on one SM of the persistent kernel with `slots` record
- * slots (48 or 64), staged or not */
-int stream_ctas_per_sm(int slots, int L, bool staged, int carveout) {
+ * slots (48 or 64) and read mode `mode` (0 plain, 1 L2 prefetch, 2 staged
+ * in shared memory) */
+int stream_ctas_per_sm(int slots, int L, int mode, int carveout) {
     int n = 0;
-    cudaError_t e;
-    if (slots <= 48) e = staged ? stream_attr<48, true>(L, &n, carveout) : stream_attr<48, false>(L, &n, carveout);
-    else e = staged ? stream_attr<64, true>(L, &n, carveout) : stream_attr<64, false>(L, &n, carveout);
+    const cudaError_t e = slots <= 48 ? stream_dispatch<48>(mode, nullptr, nullptr, 0, carveout, nullptr, L, &n)
+                                      : stream_dispatch<64>(mode, nullptr, nullptr, 0, carveout, nullptr, L, &n);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         return 1;
@@ -972,14 +980,11 @@ int stream_ctas_per_sm(int slots, int L, bool staged, int carveout) {
 
 /* The persistent FP32 kernel over q's tiles with `ctas` CTAs; slots is 48 or
  * 64.  q.next and q.n_leftover must be zero. */
-cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, bool staged, int ctas, int carveout,
+cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int mode, int ctas, int carveout,
                           cudaStream_t stream) {
     if (q.t_end <= q.t_begin) return cudaSuccess;
-    if (slots <= 48)
-        return staged ? launch_stream_one<48, true>(a, q, ctas, carveout, stream)
-                      : launch_stream_one<48, false>(a, q, ctas, carveout, stream);
-    return staged ? launch_stream_one<64, true>(a, q, ctas, carveout, stream)
-                  : launch_stream_one<64, false>(a, q, ctas, carveout, stream);
+    return slots <= 48 ? stream_dispatch<48>(mode, &a, &q, ctas, carveout, stream, a.L, nullptr)
+                       : stream_dispatch<64>(mode, &a, &q, ctas, carveout, stream, a.L, nullptr);
 }
 
 template <int SLOTS>

@@ -37,9 +37,9 @@ namespace gsnp {
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
                             int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list = nullptr);
-cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, bool staged, int ctas, int carveout,
+cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int mode, int ctas, int carveout,
                           cudaStream_t stream);
-int stream_ctas_per_sm(int slots, int L, bool staged, int carveout);
+int stream_ctas_per_sm(int slots, int L, int mode, int carveout);
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
@@ -402,7 +402,8 @@ struct gsnp_context {
     unsigned long long* d_stream_ctl = nullptr;
     int32_t* d_leftover = nullptr;
     int stream_slots = 0, stream_ctas = 0, stream_ctas_L = -1, stream_carveout = 0;
-    bool stream_path = true, stream_staged = true;
+    bool stream_path = true;
+    int stream_mode = 0;            /* 0 plain loads, 1 L2 bulk prefetch, 2 staged in shared memory */
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
@@ -418,7 +419,13 @@ struct gsnp_context {
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
     /* the call's copy streams: uploads in chunks, downloads per segment */
     static const int kUploadChunks = 16;
+    static const int kMaxUpStreams = 4;
     cudaStream_t up_stream = nullptr, down_stream = nullptr, gather_stream = nullptr;
+    /* the upload's pieces go round-robin over n_up copy streams (up_stream is
+     * the first), so that several copy engines can share the host link */
+    cudaStream_t up_extra[kMaxUpStreams - 1] = {};
+    int n_up = 1;
+    cudaStream_t up(int k) const { return k % n_up == 0 ? up_stream : up_extra[k % n_up - 1]; }
     std::vector<cudaEvent_t> ev_gather;   /* per segment: its reads are gathered */
     cudaEvent_t ev_index = nullptr;       /* the deposited index list is built */
     /* the depth bins of one pass run side by side, so that one bin's last
@@ -697,7 +704,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         int sms = 0;
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
         c->stream_ctas =
-            sms * stream_ctas_per_sm(c->stream_slots, c->params.read_length, c->stream_staged, c->stream_carveout);
+            sms * stream_ctas_per_sm(c->stream_slots, c->params.read_length, c->stream_mode, c->stream_carveout);
         c->stream_ctas_L = c->params.read_length;
     }
     if (c->dsite_cap == 0) {
@@ -818,7 +825,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             CK(cudaMemsetAsync(c->d_stream_ctl, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
             const StreamQueue q{g.t0, g.t1, c->d_stream_ctl, c->d_leftover, reinterpret_cast<int*>(c->d_stream_ctl + 1)};
             const int ks = begin(kKindStream, c->stream_slots, g.t1 - g.t0);
-            CK(launch_stream(as, q, c->stream_slots, c->stream_staged, c->stream_ctas, c->stream_carveout, c->stream),
+            CK(launch_stream(as, q, c->stream_slots, c->stream_mode, c->stream_ctas, c->stream_carveout, c->stream),
                "persistent calling kernel");
             end(ks);
             return GSNP_OK;
@@ -977,6 +984,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     const int64_t n = r->n;
     if (!c->up_stream) {
         CK(cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (int i = 0; i + 1 < c->n_up; ++i)
+            CK(cudaStreamCreateWithFlags(&c->up_extra[i], cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaStreamCreateWithFlags(&c->down_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaStreamCreateWithFlags(&c->gather_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaEventCreateWithFlags(&c->ev_index, cudaEventDisableTiming), "cudaEventCreate");
@@ -1010,22 +1019,33 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(cudaMemcpyAsync(c->d_raw_strand, r->strand, n, cudaMemcpyHostToDevice, c->up_stream), "upload");
     }
     CK(cudaEventRecord(c->ev_small, c->up_stream), "event");
+    if (c->n_up > 1) {
+        /* the other copy streams start after the small arrays' copies */
+        for (int i = 0; i + 1 < c->n_up; ++i) CK(cudaStreamWaitEvent(c->up_extra[i], c->ev_small, 0), "wait");
+    }
     for (int k = 0; k < gsnp_context::kUploadChunks; ++k) {
         const int64_t b = std::min(n, k * chunk_rows), e = std::min(n, (k + 1) * chunk_rows);
+        cudaStream_t us = c->up(k);
         if (e > b) {
             const size_t off = (size_t)b * r->pitch, bytes = (size_t)(e - b) * r->pitch;
-            CK(cudaMemcpyAsync(c->d_raw_seq + off, r->seq + off, bytes, cudaMemcpyHostToDevice, c->up_stream),
-               "upload seq");
-            CK(cudaMemcpyAsync(c->d_raw_qual + off, r->qual + off, bytes, cudaMemcpyHostToDevice, c->up_stream),
-               "upload qual");
+            CK(cudaMemcpyAsync(c->d_raw_seq + off, r->seq + off, bytes, cudaMemcpyHostToDevice, us), "upload seq");
+            CK(cudaMemcpyAsync(c->d_raw_qual + off, r->qual + off, bytes, cudaMemcpyHostToDevice, us), "upload qual");
         }
-        CK(cudaEventRecord(c->ev_chunk[k], c->up_stream), "event");
+        CK(cudaEventRecord(c->ev_chunk[k], us), "event");
         if (k == 0 || k == gsnp_context::kUploadChunks / 2 - 1 || k == gsnp_context::kUploadChunks - 1)
-            tl.rec("uploaded piece " + std::to_string(k), c->up_stream);
+            tl.rec("uploaded piece " + std::to_string(k), us);
     }
     timer.mark("uploads issued");
+    auto sync_up = [&]() {
+        cudaError_t e = cudaStreamSynchronize(c->up_stream);
+        for (int i = 0; i + 1 < c->n_up; ++i) {
+            const cudaError_t e2 = cudaStreamSynchronize(c->up_extra[i]);
+            if (e == cudaSuccess) e = e2;
+        }
+        return e;
+    };
     auto drain = [&]() {
-        cudaStreamSynchronize(c->up_stream);
+        sync_up();
         if (c->gather_stream) cudaStreamSynchronize(c->gather_stream);
         for (cudaStream_t b : c->bin_stream)
             if (b) cudaStreamSynchronize(b);
@@ -1126,13 +1146,16 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     const bool vec4 = L % 4 == 0 && r->pitch % 4 == 0 && L <= r->pitch;
     const int per_row = vec4 ? L / 4 : L;
     const int rows_per_block = std::max(1, 256 / per_row);
-    int64_t gathered_seg = -1;
+    int64_t gathered_seg = -1, waited_chunk = -1;
     auto gather_through = [&](int64_t target) -> int {
         while (gathered_seg < target) {
             const Segment& g = segs[(size_t)++gathered_seg];
             if (g.dhi > g.dlo) {
                 const int64_t chunk = std::min<int64_t>((g.raw_hi - 1) / chunk_rows, gsnp_context::kUploadChunks - 1);
-                CK(cudaStreamWaitEvent(c->gather_stream, c->ev_chunk[chunk], 0), "wait");
+                /* every piece up to the one holding the segment's last row
+                 * (the pieces of several copy streams finish in any order) */
+                for (; waited_chunk < chunk; ++waited_chunk)
+                    CK(cudaStreamWaitEvent(c->gather_stream, c->ev_chunk[waited_chunk + 1], 0), "wait");
                 const int64_t rows = g.dhi - g.dlo;
                 const int64_t per_block = (int64_t)rows_per_block * kGatherRows;
                 const unsigned blocks = (unsigned)((rows + per_block - 1) / per_block);
@@ -1177,7 +1200,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         return GSNP_OK;
     };
     int rc2 = run_calling(c, segs, before, after);
-    cudaError_t e_up = cudaStreamSynchronize(c->up_stream), e_down = cudaStreamSynchronize(c->down_stream);
+    cudaError_t e_up = sync_up(), e_down = cudaStreamSynchronize(c->down_stream);
     const cudaError_t e_gather = cudaStreamSynchronize(c->gather_stream);
     tl.rec("end", c->down_stream);
     cudaStreamSynchronize(c->down_stream);
@@ -1222,12 +1245,16 @@ int gsnp_context_create(int device, gsnp_context** out) {
     c->own_stream = true;
     /* GSNP_CALL_PATH=binned: the FP32 form through the depth-binned kernels
      * only; GSNP_STREAM_SLOTS: record slots of the persistent kernel (48, 64);
-     * GSNP_STREAM_STAGED=0: its reads from global memory, not staged;
+     * GSNP_STREAM_MODE: how it fetches reads (0 loads, 1 L2 bulk prefetch,
+     * 2 bulk copies into shared memory);
      * GSNP_STREAM_CARVEOUT: its preferred shared-memory carveout, percent */
     if (const char* e = getenv("GSNP_CALL_PATH")) c->stream_path = strcmp(e, "binned") != 0;
     if (const char* e = getenv("GSNP_STREAM_SLOTS")) c->stream_slots = atoi(e) > 48 ? 64 : 48;
-    if (const char* e = getenv("GSNP_STREAM_STAGED")) c->stream_staged = atoi(e) != 0;
+    if (const char* e = getenv("GSNP_STREAM_MODE")) c->stream_mode = std::max(0, std::min(2, atoi(e)));
     if (const char* e = getenv("GSNP_STREAM_CARVEOUT")) c->stream_carveout = std::max(0, std::min(100, atoi(e)));
+    /* GSNP_UPLOAD_STREAMS: copy streams of the alignment upload (1 to 4) */
+    if (const char* e = getenv("GSNP_UPLOAD_STREAMS"))
+        c->n_up = std::max(1, std::min((int)gsnp_context::kMaxUpStreams, atoi(e)));
     *out = c;
     return GSNP_OK;
 }
@@ -1241,6 +1268,8 @@ void gsnp_context_destroy(gsnp_context* c) {
         if (c->bin_stream[i]) cudaStreamSynchronize(c->bin_stream[i]);
     if (c->gather_stream) cudaStreamSynchronize(c->gather_stream);
     if (c->up_stream) cudaStreamSynchronize(c->up_stream);
+    for (cudaStream_t u : c->up_extra)
+        if (u) cudaStreamSynchronize(u);
     if (c->down_stream) cudaStreamSynchronize(c->down_stream);
     free_all(c);
     if (c->h_text) cudaFreeHost(c->h_text);
@@ -1269,6 +1298,8 @@ void gsnp_context_destroy(gsnp_context* c) {
         cudaStreamSynchronize(c->up_stream);
         cudaStreamDestroy(c->up_stream);
     }
+    for (cudaStream_t u : c->up_extra)
+        if (u) cudaStreamDestroy(u);
     if (c->down_stream) {
         cudaStreamSynchronize(c->down_stream);
         cudaStreamDestroy(c->down_stream);

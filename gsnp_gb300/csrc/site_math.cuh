@@ -135,15 +135,6 @@ struct Kahan10 {
     }
 };
 
-/* the 10 FP32 table terms of row r = (qa * L + coord) * 4 + o */
-__device__ __forceinline__ void lik32_row_at(const CallArgs& a, int r, float* x) {
-    const float4* row = reinterpret_cast<const float4*>(a.lik32 + (size_t)r * 12);
-    const float4 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2);
-    x[0] = x0.x; x[1] = x0.y; x[2] = x0.z; x[3] = x0.w;
-    x[4] = x1.x; x[5] = x1.y; x[6] = x1.z; x[7] = x1.w;
-    x[8] = x2.x; x[9] = x2.y;
-}
-
 __device__ __forceinline__ void lik32_row(const CallArgs& a, int qa, int coord, int o, float* x) {
     const float4* row = reinterpret_cast<const float4*>(a.lik32 + ((size_t)(qa * a.L + coord) * 4 + o) * 12);
     const float4 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2);
@@ -194,82 +185,6 @@ __device__ __forceinline__ void likelihood_fp32(const CallArgs& a, const uint32_
         const int g = genotype_of(i);
         tl[g] = (double)k.s[i];
         eps[g] = isinf(tl[g]) ? 0.0 : fabs(tl[g]) * kk;
-    }
-}
-
-/* The dependency walk (walk_records) and the FP32 sums of the fast kernel
- * in one pass over a sorted column of unit-occurrence records: each record's
- * adjusted quality is found as the walk reaches it and the table rows of four
- * records are loaded together, then added as likelihood_fp32 adds them:
- * ((x0 + x1) + (x2 + x3)), Kahan-summed group by group.  The column is only
- * read.  Same values as walk_records followed by those sums. */
-template <int BITS>
-__device__ __forceinline__ void walk_sum32(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int stride,
-                                           int num, Kahan10& k) {
-    static_assert(BITS == 1 || BITS == 2 || BITS == 4, "1, 2 or 4 bits per key");
-    constexpr int kPer = 32 / BITS;
-    constexpr uint32_t kMax = (1u << BITS) - 1u;
-    const int L = a.L;
-    const int nw = pcr_words(L, BITS);
-    const bool sat_exact = BITS == 4 && a.tmax <= 16;
-    int gdc = -1, last_o = -1, gstart = 0;
-    /* row offset (in 12-float rows) of record i: one walk step */
-    auto step = [&](int i) -> int {
-        const uint32_t w = recs[i * stride];
-        const int o = rec_base(w);
-        const int coord = rec_coord(w);
-        const int key = rec_strand(w) * L + coord;
-        if (o != last_o) {
-            for (int j = 0; j < nw; ++j) seen[j * stride] = 0u;
-            gstart = i;
-            gdc = -1;
-            last_o = o;
-        }
-        uint32_t* cw = seen + (key / kPer) * stride;
-        const int sh = (key % kPer) * BITS;
-        const uint32_t word = *cw;
-        const uint32_t cnt = (word >> sh) & kMax;
-        int tmp = (int)cnt;
-        if (cnt == kMax) {
-            if (!sat_exact) {
-                tmp = 0;
-                for (int j = gstart; j < i; ++j)
-                    if (((recs[j * stride] ^ w) & 0x1ff00u) == 0) tmp += 1;
-            }
-        } else {
-            *cw = (word & ~(kMax << sh)) | ((cnt + 1u) << sh);
-        }
-        if (tmp == 0) gdc += 1;
-        tmp += 1;
-        const int qa = (tmp < a.tmax && gdc < a.gmax)
-                           ? (int)GSNP_LDG(a.qadj + ((size_t)tmp * a.gmax + gdc) * 65 + rec_q(w))
-                           : 1;
-        return (qa * L + coord) * 4 + o;
-    };
-    for (int i = 0; i < num; i += 4) {
-        const int r0 = step(i);
-        const int r1 = i + 1 < num ? step(i + 1) : -1;
-        const int r2 = i + 2 < num ? step(i + 2) : -1;
-        const int r3 = i + 3 < num ? step(i + 3) : -1;
-        float x[10], y[10];
-        lik32_row_at(a, r0, x);
-        if (r1 >= 0) {
-            lik32_row_at(a, r1, y);
-#pragma unroll
-            for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
-        }
-        if (r2 >= 0) {
-            float z[10];
-            lik32_row_at(a, r2, y);
-            if (r3 >= 0) {
-                lik32_row_at(a, r3, z);
-#pragma unroll
-                for (int v = 0; v < 10; ++v) y[v] = __fadd_rn(y[v], z[v]);
-            }
-#pragma unroll
-            for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
-        }
-        k.add(x);
     }
 }
 

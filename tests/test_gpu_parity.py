@@ -140,20 +140,24 @@ def test_deep_sites_pcr_dependency(pcr, tmp_path, oracle_bin, native_lib):
 def test_persistent_and_binned_paths_agree(name, scale, native_lib, monkeypatch):
     """The FP32 form's persistent kernel (tiles in genome order, leftover
     tiles to the binned kernels) gives the same site calls, byte for byte, as
-    the depth-binned kernels alone, with 48 and with 64 record slots."""
+    the depth-binned kernels alone: with 48 and 64 record slots, and with its
+    reads loaded from global memory, prefetched into L2 by the bulk-copy unit,
+    or staged in shared memory by bulk copies."""
     w = synth.make_workload(name, scale=scale)
     flags = [f for f in w.cli_flags("dbsnp") if f != "-C"]
     calls = {}
-    for path, slots in (("binned", "48"), ("persistent", "48"), ("persistent", "64")):
+    for path, slots, mode in (("binned", "48", "0"), ("persistent", "48", "0"), ("persistent", "64", "0"),
+                              ("persistent", "48", "1"), ("persistent", "48", "2"), ("persistent", "64", "2")):
         monkeypatch.setenv("GSNP_CALL_PATH", path)
         monkeypatch.setenv("GSNP_STREAM_SLOTS", slots)
+        monkeypatch.setenv("GSNP_STREAM_MODE", mode)
         c, _, _ = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
         try:
-            calls[(path, slots)] = c.fetch()
+            calls[(path, slots, mode)] = c.fetch()
             kinds = {li["kind"] for li in c.last_launches()}
         finally:
             c.close()
         assert (4 in kinds) == (path == "persistent")
-    base = calls[("binned", "48")].tobytes()
+    base = calls[("binned", "48", "0")].tobytes()
     for key, v in calls.items():
         assert v.tobytes() == base, f"{name}: {key} differs from the binned path"

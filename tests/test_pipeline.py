@@ -55,3 +55,27 @@ def test_call_into_equals_call_and_fetch(segs, native_lib, monkeypatch):
         c.close()
     assert got.tobytes() == want.tobytes()
     assert again.tobytes() == want.tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("up_streams,segs", [(2, 5), (4, 9)])
+def test_upload_over_several_copy_streams(up_streams, segs, native_lib, monkeypatch):
+    """The upload's pieces spread over several copy streams finish in any
+    order; every segment's gather waits for all the pieces it reads, and the
+    calls equal those of a one-stream, one-segment call."""
+    w = synth.make_workload("c2", scale=0.02)
+    flags = [f for f in w.cli_flags() if f != "-C"]
+    c, reads, pm = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
+    try:
+        want = c.fetch(0, w.genome_len).copy()
+    finally:
+        c.close()
+    monkeypatch.setenv("GSNP_UPLOAD_STREAMS", str(up_streams))
+    monkeypatch.setenv("GSNP_SEGMENTS", str(segs))
+    c, reads, pm = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
+    try:
+        got = np.zeros(w.genome_len, dtype=api.SITE_DTYPE)
+        c.call_into(reads, got.ctypes.data)
+    finally:
+        c.close()
+    assert got.tobytes() == want.tobytes()
