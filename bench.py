@@ -67,6 +67,8 @@ def parse_args():
                     help="synthetic workload shape (the headline is c1, the 30x configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch settings (no autotuner)")
+    ap.add_argument("--tune-windows", type=int, default=32, help="windows of 262,144 sites the autotuner samples")
     return ap.parse_args()
 
 
@@ -299,6 +301,16 @@ def main():
     caller.set_stream(stream.cuda_stream)
     caller.call(reads)                       # uploads the alignments, first pass
     sites = w.genome_len
+    # the launch autotuner on a sample of the resident workload (untimed): the
+    # chosen settings are those of every timed pass below
+    tuning = None
+    if not args.no_tune:
+        t1 = time.time()
+        report = caller.tune(sample_windows=args.tune_windows)
+        tuning = {"options": dict(ln.split() for ln in report.splitlines() if ln and not ln.startswith("#")
+                                  and len(ln.split()) == 2 and not ln.split()[1].endswith("ms")),
+                  "summary": next((ln[2:] for ln in report.splitlines() if ln.startswith("# ")), ""),
+                  "seconds": round(time.time() - t1, 2)}
 
     def barrier():
         if dist is not None:
@@ -312,21 +324,29 @@ def main():
         return float(t.item())
 
     def time_form(prec):
-        """Warm up, then time exactly args.steps device-resident calling passes."""
+        """Per-kernel times from passes launched one kernel at a time (each
+        timed by events, untimed region), then, after the warm-up, exactly
+        args.steps device-resident calling passes replayed as a CUDA graph."""
         caller.load_tables(api.params_from_flags(flags, prec), pm, prior, rank_tab)
-        for _ in range(args.warmup):
-            caller.recall_resident()
-        n_launch = len(caller.last_launches())
-        barrier()
-        torch.cuda.synchronize()
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        caller.set_option("graphs", 0)
         kernel_ms = {}
-        start.record(stream)
-        for _ in range(args.steps):
+        for i in range(3):
             caller.recall_resident()
+            if i == 0:
+                continue
             for li in caller.last_launches():
                 key = (li["kind"], li["slots"])
                 kernel_ms.setdefault(key, []).append((li["ms"], li["sites"], li["tiles"]))
+        n_launch = len(caller.last_launches())
+        caller.set_option("graphs", 1)
+        for _ in range(args.warmup):
+            caller.recall_resident()
+        barrier()
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            caller.recall_resident()
         end.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -441,7 +461,8 @@ def main():
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
     bsite = site_bytes(w)
-    names = {1: "call_tiles_kernel", 2: "call_fast_kernel", 3: "deferred_sites_kernel", 4: "call_stream_kernel"}
+    names = {1: "call_tiles_kernel", 2: "call_fast_kernel", 3: "deferred_sites_kernel", 4: "call_stream_kernel",
+             5: "graph"}
     dom_key = max((k for k in kernel_ms if k[0] in (1, 2, 4)), key=lambda k: sum(x[0] for x in kernel_ms[k]))
     dom = kernel_ms[dom_key]
     dom_ms = statistics.mean(x[0] for x in dom)
@@ -494,6 +515,7 @@ def main():
                                      if (args.workload,) + dom_key in NCU_BYTES_PER_SITE else None),
                          "kernel": "%s<%d>" % (names[dom_key[0]], dom_key[1]), "sites_per_launch": dom_sites,
                          "bytes_per_site": bsite, "peak_source": peak_kind},
+            "tuning": tuning,
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),
             "stats": stats,

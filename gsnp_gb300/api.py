@@ -89,6 +89,8 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_get_stats": (ctypes.c_int, [_P, _P, ctypes.c_int]),
         "gsnp_last_launches": (ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_int)]),
         "gsnp_transfer_bytes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+        "gsnp_set_option": (ctypes.c_int, [_P, ctypes.c_char_p, _I64]),
+        "gsnp_tune": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -191,6 +193,17 @@ class Caller:
         if rc != GSNP_OK:
             msg = self.lib.gsnp_context_error(self.ctx)
             raise RuntimeError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def set_option(self, name: str, value: int) -> None:
+        """A launch option of the context (gsnp_set_option)."""
+        self._check(self.lib.gsnp_set_option(self.ctx, name.encode(), int(value)), "gsnp_set_option")
+
+    def tune(self, sample_windows: int = 16) -> str:
+        """Run the launch autotuner on the resident reads of the last call
+        (gsnp_tune); returns its report."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self.lib.gsnp_tune(self.ctx, int(sample_windows), buf, len(buf)), "gsnp_tune")
+        return buf.value.decode()
 
     def set_stream(self, stream_ptr: int) -> None:
         self._check(self.lib.gsnp_set_stream(self.ctx, _P(stream_ptr)), "gsnp_set_stream")

@@ -276,8 +276,6 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
 /* tile classification                                                       */
 /* ------------------------------------------------------------------------ */
 
-__constant__ int c_slots[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
-
 /* Read range of every tile, [lower_bound(s0 - L + 1), lower_bound(s0 + kTile)),
  * in one pass over the sorted starts: read r is the lower bound of every
  * boundary b with pos[r - 1] < b <= pos[r].  Threads r_begin .. r_end; the
@@ -363,16 +361,22 @@ static_assert(kClassifyThreads % kTile == 0, "a classify CTA holds whole tiles")
 __global__ void __launch_bounds__(kClassifyThreads) classify_tiles_kernel(CallArgs a, int pass, int64_t t_begin,
                                                                           int64_t t_end, int* bin_count,
                                                                           int32_t* bin_tiles,
-                                                                          const int32_t* __restrict__ list) {
+                                                                          const int32_t* __restrict__ list,
+                                                                          const int* __restrict__ d_count) {
     __shared__ int32_t spos[kClassifyTiles][kClassifyStage];
     __shared__ int smax[kClassifyThreads / 32];
     __shared__ int sbin_count[2 * kNumBins], sbin_base[2 * kNumBins];
     const int lt = threadIdx.x / kTile, tt = threadIdx.x % kTile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    /* the tiles [t_begin, t_end), or with a list the tiles list[t_begin, t_end) */
-    const int64_t idx = t_begin + (int64_t)blockIdx.x * kClassifyTiles + lt;
+    /* the tiles [t_begin, t_end), or with a list the tiles list[t_begin,
+     * t_end); with d_count, t_end is t_begin + *d_count.  The CTAs take
+     * kClassifyTiles tiles at a time, every gridDim.x-th group. */
+    const int64_t end = d_count ? t_begin + *d_count : t_end;
+    for (int64_t gbase = t_begin + (int64_t)blockIdx.x * kClassifyTiles; gbase < end;
+         gbase += (int64_t)gridDim.x * kClassifyTiles) {
+    const int64_t idx = gbase + lt;
     if (threadIdx.x < 2 * kNumBins) sbin_count[threadIdx.x] = 0;
-    bool part = idx < t_end;
+    bool part = idx < end;
     const int64_t tile = list ? (part ? (int64_t)list[idx] : 0) : idx;
     const int64_t s0 = tile * kTile;
     uint8_t wflags = 0;
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(kClassifyThreads) classify_tiles_kernel(CallAr
         const int m = smax[lt];
         const bool fast = a.precision == 1 && !(wflags & (kWinKeepLik | kWinExternalLik));
         int bin = 0;
-        while (bin < kNumBins - 1 && m > c_slots[bin]) ++bin;
+        while (bin < kNumBins - 1 && m > a.bin_limit[bin]) ++bin;
         my_bin = bin + (fast ? kNumBins : 0);
         my_rank = atomicAdd(&sbin_count[my_bin], 1);
     }
@@ -419,6 +423,8 @@ __global__ void __launch_bounds__(kClassifyThreads) classify_tiles_kernel(CallAr
     }
     __syncthreads();
     if (my_bin >= 0) bin_tiles[(int64_t)my_bin * a.n_tiles + sbin_base[my_bin] + my_rank] = (int32_t)tile;
+    __syncthreads();
+    }
 }
 
 /* log10 genotype priors of every dbSNP row (kernel/posterior_kernel.cu:575-633,
@@ -464,14 +470,10 @@ cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, c
 /* the FP64 calling kernel                                                   */
 /* ------------------------------------------------------------------------ */
 
+/* One tile of the FP64 kernel; every lane of the warp calls it. */
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);                   /* [SLOTS][kTile] */
-    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;    /* [nw][kTile] */
-
+__device__ __forceinline__ void fp64_tile(const CallArgs& a, int64_t tile, uint32_t* recs_all, uint32_t* seen_all) {
     const int t = threadIdx.x;
-    const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
     const int win = (int)(s0 / kWin);
     const uint8_t wflags = a.win_flags[win];
@@ -513,6 +515,27 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
     SiteCall call;
     site_posterior(a, ori, p, tl, nullptr, lp, recs, kTile, nq, &call);
     a.out[site] = call;
+}
+
+/* The tiles of one depth bin: tiles[blockIdx.x] with count == nullptr (one
+ * CTA per tile), else the first *count tiles of the list, each CTA taking
+ * every gridDim.x-th (a grid sized to the resident CTAs, whatever the count
+ * the device holds). */
+template <int SLOTS>
+__global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles,
+                                                                           const int* __restrict__ count) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);                   /* [SLOTS][kTile] */
+    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;    /* [nw][kTile] */
+    if (!count) {
+        fp64_tile<SLOTS>(a, tiles[blockIdx.x], recs_all, seen_all);
+        return;
+    }
+    const int n = *count;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        fp64_tile<SLOTS>(a, tiles[i], recs_all, seen_all);
+        __syncwarp();
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -620,14 +643,8 @@ __device__ __forceinline__ void fast_site(const CallArgs& a, int64_t site, bool 
  * keep counting past the capacities so that the host can size the pool and
  * run the pass again. */
 template <int SLOTS>
-__global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    constexpr bool kGlobal = kGlobalRecs(SLOTS, true);
-    uint32_t* recs_all = kGlobal ? a.deep_recs + (size_t)blockIdx.x * SLOTS * kTile : reinterpret_cast<uint32_t*>(smem);
-    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + (kGlobal ? 0 : SLOTS * kTile);
-
+__device__ __forceinline__ void fast_tile(const CallArgs& a, int64_t tile, uint32_t* recs_all, uint32_t* seen_all) {
     const int t = threadIdx.x;
-    const int64_t tile = tiles[blockIdx.x];
     const int64_t s0 = tile * kTile;
     const int win = (int)(s0 / kWin);
     const uint8_t wflags = a.win_flags[win];
@@ -643,6 +660,26 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
     if (active) sort_column<SLOTS>(recs, p.num);
 
     fast_site<SLOTS>(a, site, active, ori, wflags, snp_row, p, recs, seen);
+}
+
+/* The tiles of one depth bin, as call_tiles_kernel takes them.  The deep
+ * bins' record columns are the CTA's slice of a.deep_recs. */
+template <int SLOTS>
+__global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles,
+                                                                          const int* __restrict__ count) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    constexpr bool kGlobal = kGlobalRecs(SLOTS, true);
+    uint32_t* recs_all = kGlobal ? a.deep_recs + (size_t)blockIdx.x * SLOTS * kTile : reinterpret_cast<uint32_t*>(smem);
+    uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + (kGlobal ? 0 : SLOTS * kTile);
+    if (!count) {
+        fast_tile<SLOTS>(a, tiles[blockIdx.x], recs_all, seen_all);
+        return;
+    }
+    const int n = *count;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        fast_tile<SLOTS>(a, tiles[i], recs_all, seen_all);
+        __syncwarp();
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -835,6 +872,7 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(Call
         }
         tile = nxt;
         staged_n = staged_next;
+        __syncwarp();
     }
 }
 
@@ -843,9 +881,17 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(Call
  * bound checks, then the FP64 sums where those fail.  Sampled sites also get
  * the FP64 sums for the accuracy figure, and when the fast kernel had decided
  * them its call is compared with this one. */
-__global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void deferred_site(const CallArgs& a, int64_t i);
+
+/* n sites, or with d_n the count the fast kernels requested (a.dcount[0]),
+ * at most the pool's capacity, each thread taking every (grid)-th site */
+__global__ void __launch_bounds__(32) deferred_sites_kernel(CallArgs a, int64_t n, const unsigned long long* d_n) {
+    if (d_n) n = (int64_t)min(*d_n, (unsigned long long)a.dsite_cap);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        deferred_site(a, i);
+}
+
+__device__ __forceinline__ void deferred_site(const CallArgs& a, int64_t i) {
     const DeferredSite d = a.dsites[i];
     const int64_t site = d.site;
     const uint32_t* recs = a.dpool + d.rec_off;
@@ -910,14 +956,19 @@ size_t call_smem_bytes(int slots, int L, bool fast) {
     return (kGlobalRecs(slots, fast) ? 0 : (size_t)slots * kTile * 4) + nw * kTile * 4;
 }
 
+/* Classify tiles [t_begin, t_end) (with a list, list[t_begin, t_end); with
+ * d_count, list[0, *d_count) read on the device, by a fixed grid of `grid`
+ * CTAs) into the depth bins. */
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
-                            int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list) {
+                            int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list, const int* d_count,
+                            int grid) {
     cudaError_t e = cudaMemsetAsync(d_bin_count, 0, sizeof(int) * 2 * kNumBins, stream);
     if (e != cudaSuccess) return e;
-    const unsigned blocks = (unsigned)((t_end - t_begin + kClassifyTiles - 1) / kClassifyTiles);
+    const unsigned blocks =
+        d_count ? (unsigned)grid : (unsigned)((t_end - t_begin + kClassifyTiles - 1) / kClassifyTiles);
     if (blocks == 0) return cudaSuccess;
     classify_tiles_kernel<<<blocks, kClassifyThreads, 0, stream>>>(a, pass, t_begin, t_end, d_bin_count, d_bin_tiles,
-                                                                   list);
+                                                                   list, d_count);
     return cudaGetLastError();
 }
 
@@ -987,53 +1038,81 @@ cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, in
                        : stream_dispatch<64>(mode, &a, &q, ctas, carveout, stream, a.L, nullptr);
 }
 
+/* set the bin kernel's shared-memory size and carveout (percent; 0 leaves the
+ * default); with ctas_per_sm, its resident CTAs on one SM */
 template <int SLOTS>
-static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles, int count, cudaStream_t stream) {
+static cudaError_t bin_attr(int kind, int L, int carveout, int* ctas_per_sm) {
+    const int smem = (int)call_smem_bytes(SLOTS, L, kind == kKindFast);
+    const void* fn = kind == kKindFast ? reinterpret_cast<const void*>(call_fast_kernel<SLOTS>)
+                                       : reinterpret_cast<const void*>(call_tiles_kernel<SLOTS>);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    /* the carveout is a hint: a refusal only costs speed, and its error is
+     * cleared so that it is not taken for the launch's */
+    if (carveout > 0 && cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carveout) != cudaSuccess)
+        (void)cudaGetLastError();
+    if (ctas_per_sm) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, kTile, smem);
+    return cudaSuccess;
+}
+
+template <int SLOTS>
+static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles, const BinLaunch& bl,
+                              cudaStream_t stream) {
+    cudaError_t e = bin_attr<SLOTS>(kind, a.L, bl.carveout, nullptr);
+    if (e != cudaSuccess) return e;
     const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
-    cudaError_t e;
-    if (kind == kKindFast) {
-        e = cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        /* The 40-slot bin runs faster with 72% of the SM's shared memory
-         * carved out (about 21 resident CTAs) than with the carveout that
-         * fits the most CTAs: the L1 left beside 29 CTAs holds too little of
-         * the likelihood table, whose loads are the longest stall (c1 at 25%
-         * scale: 2.02 -> 1.90 ms).  The other bins ran as fast or slower
-         * with 58-86%.  The carveout is a hint: a refusal only costs speed,
-         * and its error is cleared so that it is not taken for the
-         * launch's. */
-        if (SLOTS == 40 &&
-            cudaFuncSetAttribute(call_fast_kernel<SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 72) !=
-                cudaSuccess)
-            (void)cudaGetLastError();
-        call_fast_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
-    } else {
-        e = cudaFuncSetAttribute(call_tiles_kernel<SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        call_tiles_kernel<SLOTS><<<count, kTile, smem, stream>>>(a, tiles);
-    }
+    const unsigned grid = (unsigned)(bl.d_count ? bl.grid : bl.count);
+    if (grid == 0) return cudaSuccess;
+    if (kind == kKindFast) call_fast_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count);
+    else call_tiles_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count);
     return cudaGetLastError();
 }
 
-/* Launch the FP64 or the fast calling kernel over the `count` tiles of depth
- * bin `bin`. */
-cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream) {
+/* Launch the FP64 or the fast calling kernel over the tiles of depth bin
+ * `bin` (see BinLaunch). */
+cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, const BinLaunch& bl,
+                       cudaStream_t stream) {
     switch (bin) {
-        case 0: return launch_one<32>(a, kind, tiles, count, stream);
-        case 1: return launch_one<40>(a, kind, tiles, count, stream);
-        case 2: return launch_one<48>(a, kind, tiles, count, stream);
-        case 3: return launch_one<64>(a, kind, tiles, count, stream);
-        case 4: return launch_one<96>(a, kind, tiles, count, stream);
-        case 5: return launch_one<128>(a, kind, tiles, count, stream);
-        default: return launch_one<256>(a, kind, tiles, count, stream);
+        case 0: return launch_one<32>(a, kind, tiles, bl, stream);
+        case 1: return launch_one<40>(a, kind, tiles, bl, stream);
+        case 2: return launch_one<48>(a, kind, tiles, bl, stream);
+        case 3: return launch_one<64>(a, kind, tiles, bl, stream);
+        case 4: return launch_one<96>(a, kind, tiles, bl, stream);
+        case 5: return launch_one<128>(a, kind, tiles, bl, stream);
+        default: return launch_one<256>(a, kind, tiles, bl, stream);
     }
 }
 
-cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream) {
-    if (n <= 0) return cudaSuccess;
+/* resident CTAs on one SM of bin `bin` of kernel `kind` at a carveout */
+int bin_ctas_per_sm(int kind, int bin, int L, int carveout) {
+    int n = 0;
+    cudaError_t e;
+    switch (bin) {
+        case 0: e = bin_attr<32>(kind, L, carveout, &n); break;
+        case 1: e = bin_attr<40>(kind, L, carveout, &n); break;
+        case 2: e = bin_attr<48>(kind, L, carveout, &n); break;
+        case 3: e = bin_attr<64>(kind, L, carveout, &n); break;
+        case 4: e = bin_attr<96>(kind, L, carveout, &n); break;
+        case 5: e = bin_attr<128>(kind, L, carveout, &n); break;
+        default: e = bin_attr<256>(kind, L, carveout, &n); break;
+    }
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
+/* The FP64 pass over n deferred sites, or with d_n over the count the fast
+ * kernels requested (read on the device) with a fixed grid of `grid` CTAs. */
+cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream, const unsigned long long* d_n,
+                            int grid) {
+    if (!d_n && n <= 0) return cudaSuccess;
     /* one warp per CTA: the deferred sites are few and each is a long serial
      * computation, so they are spread over as many SMs as possible */
-    deferred_sites_kernel<<<(unsigned)((n + 31) / 32), 32, 0, stream>>>(a, n);
+    const unsigned blocks = d_n ? (unsigned)grid : (unsigned)((n + 31) / 32);
+    if (blocks == 0) return cudaSuccess;
+    deferred_sites_kernel<<<blocks, 32, 0, stream>>>(a, n, d_n);
     return cudaGetLastError();
 }
 

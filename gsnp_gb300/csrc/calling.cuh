@@ -29,6 +29,7 @@ enum CallKind : int {
     kKindFast = 2,      /* FP32 likelihood and posterior, hard sites deferred */
     kKindDeferred = 3,  /* FP64 pass over the sites the fast kernel deferred */
     kKindStream = 4,    /* the persistent FP32 kernel over a segment's tiles */
+    kKindGraph = 5,     /* a whole pass replayed as a CUDA graph */
 };
 
 /* A site the fast kernel left to the FP64 pass: its pileup counts and the
@@ -56,6 +57,16 @@ enum WindowFlags : uint8_t {
 
 /* tiles a warp of the persistent FP32 kernel takes per counter increment */
 constexpr int kStreamChunk = 2;
+
+/* One launch of a depth bin's kernel: `count` tiles, one CTA each; or, with
+ * d_count, the count the device holds, taken by `grid` CTAs in turn.  The
+ * preferred shared-memory carveout in percent (0: the default). */
+struct BinLaunch {
+    int count;
+    const int* d_count;
+    int grid;
+    int carveout;
+};
 
 /* work queue of one launch of the persistent FP32 kernel (call_stream_kernel) */
 struct StreamQueue {
@@ -104,6 +115,7 @@ struct CallArgs {
     int64_t n_tiles;
     int64_t* tile_rng;           /* [n_tiles][2]: reads starting in [s0 - L + 1, s0 + kTile) of each tile */
     int64_t* warp_rng;           /* [n_tiles][2]: reads that can cover each tile's sites */
+    int bin_limit[kNumBins];     /* deepest column each depth bin takes (at most its record slots) */
     uint32_t* deep_recs;         /* record columns of the deep bins' CTAs, [CTA][SLOTS][kTile] */
     /* the call of a site without records or counts, by site code (16 entries;
      * empty_valid[code] = 0 where it is not a fixed homozygous call) */

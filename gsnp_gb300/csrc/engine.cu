@@ -36,20 +36,30 @@
 namespace gsnp {
 
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
-                            int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list = nullptr);
+                            int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list = nullptr,
+                            const int* d_count = nullptr, int grid = 0);
 cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, int mode, int ctas, int carveout,
                           cudaStream_t stream);
 int stream_ctas_per_sm(int slots, int L, int mode, int carveout);
-cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, int count, cudaStream_t stream);
+cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, const BinLaunch& bl,
+                       cudaStream_t stream);
+int bin_ctas_per_sm(int kind, int bin, int L, int carveout);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
-cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream);
+cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream,
+                            const unsigned long long* d_n = nullptr, int grid = 0);
 cudaError_t launch_tile_bounds(const CallArgs& a, int64_t r_begin, int64_t r_end, int64_t next_pos,
                                cudaStream_t stream);
 cudaError_t launch_empty_calls(const CallArgs& a, SiteCall* calls, uint8_t* valid, cudaStream_t stream);
 int bin_slots(int bin);
+inline int kSlotsOf(int bin) { return bin_slots(bin); }
 int64_t bin_global_words(int kind, int bin, int64_t count);
 
 /* ---- device helpers ---- */
+
+/* dmax[i] = max(dmax[i], v[i]) for i < 2 (one thread each) */
+__global__ void track_max_kernel(const unsigned long long* __restrict__ v, unsigned long long* __restrict__ dmax) {
+    if (threadIdx.x < 2) dmax[threadIdx.x] = max(dmax[threadIdx.x], v[threadIdx.x]);
+}
 
 /* bytes between device memory and mapped host memory (small control data) */
 __global__ void copy_bytes_kernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, size_t n) {
@@ -404,6 +414,19 @@ struct gsnp_context {
     int stream_slots = 0, stream_ctas = 0, stream_ctas_L = -1, stream_carveout = 0;
     bool stream_path = true;
     int stream_mode = 0;            /* 0 plain loads, 1 L2 bulk prefetch, 2 staged in shared memory */
+    /* Device-driven calling: the bins' kernels, the classification of the
+     * persistent kernel's leftover tiles and the deferred pass read their
+     * counts on the device, with grids sized to the resident CTAs, so that a
+     * call queues all its work without waiting on the host; the resident
+     * recall replays it as a captured CUDA graph. */
+    bool device_driven = true, use_graphs = true;
+    int bin_limit[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
+    int bin_carveout[2][kNumBins] = {{0, 0, 0, 0, 0, 0, 0}, {0, 72, 0, 0, 0, 0, 0}};
+    int bin_grid[2][kNumBins] = {};
+    int grid_L = -1, deferred_grid = 0, classify_grid = 0, sms = 0;
+    unsigned long long* d_dmax = nullptr;   /* [2] largest deferred request of the call's segments */
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_key = 0;
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
@@ -595,7 +618,8 @@ void free_all(gsnp_context* c) {
                     c->d_dpool, c->d_dcount, c->d_warp_rng, c->d_win_host_src, c->d_emit,
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
-                    c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep, c->d_stream_ctl, c->d_leftover};
+                    c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep, c->d_stream_ctl, c->d_leftover,
+                    c->d_dmax};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -637,6 +661,7 @@ CallArgs make_args(gsnp_context* c) {
     a.althom_unval = c->params.althom_unval;
     /* the FP32 error bound needs every table term <= 0 */
     a.precision = c->tables.all_nonpositive ? c->params.precision : GSNP_PRECISION_FP64;
+    for (int b = 0; b < kNumBins; ++b) a.bin_limit[b] = c->bin_limit[b];
     a.win_flags = c->d_win_flags;
     a.win_lik_src = c->d_win_lik_src;
     a.n_tiles = (c->chr_len + kTile - 1) / kTile;
@@ -671,8 +696,9 @@ struct Segment {
  * segment (the call gathers the reads there; it must leave the reads of
  * segment s + 1 on the device too, which the tile ranges and the next-site
  * lookups of segment s reach), after(s) once its calls are queued. */
-int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
-                const std::function<int(size_t)>& after) {
+/* Allocations and one-time work of a calling pass, done before any of its
+ * work is queued (and outside a graph capture). */
+int prepare_calling(gsnp_context* c) {
     const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
     {
         const int rc = ensure_map(c, kMapWindows);
@@ -716,6 +742,83 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
     }
     if (!c->ev[0])
         for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i) CK(cudaEventCreate(&c->ev[i]), "cudaEventCreate");
+    if (!c->ev_fork) {
+        CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        for (int i = 0; i < gsnp_context::kBinStreams; ++i) {
+            CK(cudaStreamCreateWithFlags(&c->bin_stream[i], cudaStreamNonBlocking), "cudaStreamCreate");
+            CK(cudaEventCreateWithFlags(&c->ev_join[i], cudaEventDisableTiming), "cudaEventCreate");
+        }
+    }
+    if (c->device_driven) {
+        if (!c->d_dmax) CK(dev_alloc(&c->d_dmax, 2), "cudaMalloc");
+        if (c->grid_L != c->params.read_length) {
+            /* grids of the device-driven launches: the resident CTAs */
+            CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
+            for (int kind = 0; kind < 2; ++kind)
+                for (int b = 0; b < kNumBins; ++b)
+                    c->bin_grid[kind][b] = c->sms * bin_ctas_per_sm(kind == 0 ? kKindFP64 : kKindFast, b,
+                                                                   c->params.read_length, c->bin_carveout[kind][b]);
+            c->deferred_grid = c->sms * 32;
+            c->classify_grid = c->sms * 4;
+            c->grid_L = c->params.read_length;
+        }
+        /* record columns of the deepest fast bin: one slice per resident CTA */
+        const int64_t words = bin_global_words(kKindFast, kNumBins - 1, c->bin_grid[1][kNumBins - 1]);
+        if (words > c->deep_cap) {
+            CK(dev_alloc(&c->d_deep, (size_t)words), "cudaMalloc deep scratch");
+            c->deep_cap = words;
+        }
+    }
+    return GSNP_OK;
+}
+
+/* The result checks of a device-driven pass, once its work is queued: the
+ * error word, the statistics and the largest deferred-site request, through
+ * the mapped control area. */
+constexpr int kRedoDeferred = -100;   /* the deferred pool was too small: it was grown, call again */
+
+int finish_device(gsnp_context* c) {
+    CK(to_map(c, c->d_error, kMapError, sizeof(int)), "error flag");
+    CK(to_map(c, c->d_stats, kMapStats, sizeof(c->stats)), "stats");
+    CK(to_map(c, c->d_dmax, kMapDcount, sizeof(c->h_dcount)), "deferred counts");
+    CK(cudaStreamSynchronize(c->stream), "calling");
+    int err = 0;
+    memcpy(&err, c->h_map + kMapError, sizeof(int));
+    memcpy(c->stats, c->h_map + kMapStats, sizeof(c->stats));
+    memcpy(c->h_dcount, c->h_map + kMapDcount, sizeof(c->h_dcount));
+    for (int k = 0; k < c->n_launches; ++k) cudaEventElapsedTime(&c->launches[k].ms, c->ev[2 * k], c->ev[2 * k + 1]);
+    if (err == 1) return fail(c, GSNP_ERR_CAPACITY, "a site is covered by more than 65535 alignments");
+    if (err == 5) return fail(c, GSNP_ERR_STATE, "a staging bulk copy of the calling kernel did not complete");
+    if (err) return fail(c, GSNP_ERR_STATE, "record slots of a tile overflowed its depth bin");
+    const int64_t ns = (int64_t)c->h_dcount[0], nw = (int64_t)c->h_dcount[1];
+    if (ns > c->dsite_cap || nw > c->dpool_cap) {
+        c->dsite_cap = std::max(c->dsite_cap, ns + ns / 8 + 1024);
+        c->dpool_cap = std::max(c->dpool_cap, nw + nw / 8 + 65536);
+        CK(dev_alloc(&c->d_dsites, (size_t)c->dsite_cap), "cudaMalloc deferred");
+        CK(dev_alloc(&c->d_dpool, (size_t)c->dpool_cap), "cudaMalloc deferred");
+        return kRedoDeferred;
+    }
+    c->stats[0] = (uint64_t)c->chr_len;
+    c->called = true;
+    return GSNP_OK;
+}
+
+/* device-driven queueing of a calling pass (defined below) */
+int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
+                   const std::function<int(size_t)>& after, bool record);
+
+int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
+                const std::function<int(size_t)>& after) {
+    const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    {
+        const int rc = prepare_calling(c);
+        if (rc != GSNP_OK) return rc;
+    }
+    if (c->device_driven) {
+        const int rc = enqueue_device(c, segs, before, after, true);
+        if (rc != GSNP_OK) return rc;
+        return finish_device(c);
+    }
     CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
     CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * kNumStats, c->stream), "memset");
     const CallArgs a = make_args(c);
@@ -745,13 +848,6 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
     auto end_on = [&](int k, cudaStream_t st) {
         if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], st);
     };
-    if (!c->ev_fork) {
-        CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
-        for (int i = 0; i < gsnp_context::kBinStreams; ++i) {
-            CK(cudaStreamCreateWithFlags(&c->bin_stream[i], cudaStreamNonBlocking), "cudaStreamCreate");
-            CK(cudaEventCreateWithFlags(&c->ev_join[i], cudaEventDisableTiming), "cudaEventCreate");
-        }
-    }
     /* the non-empty bins of kind in decreasing tile count.  In a call of
      * several segments, whose bins are small launches, they run side by side
      * on the bin streams (the context's stream waits for all of them); a
@@ -784,7 +880,8 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
                 const int b = order[j];
                 const int nb = c->h_bin_count[base + b];
                 const int k = begin(kind, bin_slots(b), nb);
-                CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, c->stream),
+                const BinLaunch bl{nb, nullptr, 0, c->bin_carveout[kind == kKindFast][b]};
+                CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, bl, c->stream),
                    "calling kernel");
                 end(k);
             }
@@ -798,7 +895,8 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             cudaStream_t st = c->bin_stream[j % ns];
             const int nb = c->h_bin_count[base + b];
             const int k = begin_on(kind, bin_slots(b), nb, st);
-            CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, nb, st),
+            const BinLaunch bl{nb, nullptr, 0, c->bin_carveout[kind == kKindFast][b]};
+            CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, bl, st),
                "calling kernel");
             end_on(k, st);
         }
@@ -920,6 +1018,123 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
     return GSNP_OK;
 }
 
+
+/* One pass queued with its launch sizes read on the device (see the
+ * device_driven field of the context): per segment the tile ranges, in the
+ * FP32 form the persistent kernel and the classification of the tiles it
+ * leaves, the depth bins' kernels (each a grid of its resident CTAs taking the
+ * bin's tiles in turn), the deferred pass, and, when the segment has windows
+ * that take their likelihood from another window, the second pass of those.
+ * Nothing here waits on the host.  record: launch records with events
+ * (false while a graph is captured). */
+int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
+                   const std::function<int(size_t)>& after, bool record) {
+    const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
+    CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * kNumStats, c->stream), "memset");
+    CK(cudaMemsetAsync(c->d_dmax, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
+    c->n_launches = 0;
+    auto begin = [&](int kind, int sl, int64_t tiles) -> int {
+        if (!record || c->n_launches >= gsnp_context::kMaxLaunches) return -1;
+        const int k = c->n_launches++;
+        c->launches[k].kind = kind;
+        c->launches[k].slots = sl;
+        c->launches[k].tiles = tiles;
+        c->launches[k].sites = std::min<int64_t>(tiles * kTile, c->chr_len);
+        c->launches[k].ms = 0.f;
+        cudaEventRecord(c->ev[2 * k], c->stream);
+        return k;
+    };
+    auto end = [&](int k) {
+        if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], c->stream);
+    };
+    const bool fast = make_args(c).precision == 1;
+    const bool use_stream = c->stream_path && fast;
+    int* d_left = reinterpret_cast<int*>(c->d_stream_ctl + 1);
+    for (size_t si = 0; si < segs.size(); ++si) {
+        const Segment& g = segs[si];
+        if (before) {
+            const int rc = before(si);
+            if (rc != GSNP_OK) return rc;
+        }
+        /* which passes the segment's windows need (the host replay knows) */
+        bool keep_lik = false, external = false;
+        const int64_t w0 = g.t0 * kTile / kWin, w1 = std::min<int64_t>(c->plan.n_windows, (g.t1 * kTile + kWin - 1) / kWin);
+        for (int64_t w = w0; w < w1; ++w) {
+            keep_lik |= (c->plan.flags[w] & kWinKeepLik) != 0;
+            external |= (c->plan.flags[w] & kWinExternalLik) != 0;
+        }
+        CallArgs a = make_args(c);
+        a.n_reads = c->n_gathered;
+        a.deep_recs = c->d_deep;
+        int k = begin(kKindClassify, 0, g.t1 - g.t0);
+        CK(launch_tile_bounds(a, g.dlo, g.dhi, g.next_pos, c->stream), "tile bounds kernel");
+        CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+        auto bins = [&](int kind, int pass) -> int {
+            const int ki = kind == kKindFast ? 1 : 0;
+            for (int b = 0; b < kNumBins; ++b) {
+                /* after the persistent kernel, the fast bins get only tiles
+                 * deeper than its record slots */
+                if (kind == kKindFast && use_stream && kSlotsOf(b) <= c->stream_slots) continue;
+                const BinLaunch bl{0, c->d_bin_count + ki * kNumBins + b, c->bin_grid[ki][b], c->bin_carveout[ki][b]};
+                const int kb = begin(kind, kSlotsOf(b), 0);
+                CK(launch_bin(a, kind, b, c->d_bin_tiles + (int64_t)(ki * kNumBins + b) * n_tiles, bl, c->stream),
+                   "calling kernel");
+                end(kb);
+            }
+            (void)pass;
+            return GSNP_OK;
+        };
+        /* pass 0 */
+        if (use_stream) {
+            CK(cudaMemsetAsync(c->d_stream_ctl, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
+            end(k);
+            const StreamQueue q{g.t0, g.t1, c->d_stream_ctl, c->d_leftover, d_left};
+            const int ks = begin(kKindStream, c->stream_slots, g.t1 - g.t0);
+            CK(launch_stream(a, q, c->stream_slots, c->stream_mode, c->stream_ctas, c->stream_carveout, c->stream),
+               "persistent calling kernel");
+            end(ks);
+            k = begin(kKindClassify, 0, 0);
+            CK(launch_classify(a, 0, 0, 0, c->d_bin_count, c->d_bin_tiles, c->stream, c->d_leftover, d_left,
+                               c->classify_grid),
+               "classify kernel");
+        } else {
+            CK(launch_classify(a, 0, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
+        }
+        end(k);
+        if (!fast || keep_lik) {
+            const int rc = bins(kKindFP64, 0);
+            if (rc != GSNP_OK) return rc;
+        }
+        if (fast) {
+            const int rc = bins(kKindFast, 0);
+            if (rc != GSNP_OK) return rc;
+            const int kd = begin(kKindDeferred, 0, 0);
+            CK(launch_deferred(a, 0, c->stream, c->d_dcount, c->deferred_grid), "deferred calling kernel");
+            end(kd);
+            track_max_kernel<<<1, 2, 0, c->stream>>>(c->d_dcount, c->d_dmax);
+            CK(cudaGetLastError(), "deferred counts");
+        }
+        /* pass 1: the windows whose likelihood another window kept */
+        if (external) {
+            const int kc = begin(kKindClassify, 0, 0);
+            if (use_stream)
+                CK(launch_classify(a, 1, 0, 0, c->d_bin_count, c->d_bin_tiles, c->stream, c->d_leftover, d_left,
+                                   c->classify_grid),
+                   "classify kernel");
+            else
+                CK(launch_classify(a, 1, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
+            end(kc);
+            const int rc = bins(kKindFP64, 1);
+            if (rc != GSNP_OK) return rc;
+        }
+        if (after) {
+            const int rc = after(si);
+            if (rc != GSNP_OK) return rc;
+        }
+    }
+    return GSNP_OK;
+}
 
 /* the whole chromosome as one segment (the deposited reads are resident) */
 Segment whole_segment(const gsnp_context* c) {
@@ -1200,6 +1415,22 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         return GSNP_OK;
     };
     int rc2 = run_calling(c, segs, before, after);
+    if (rc2 == kRedoDeferred) {
+        /* the deferred pool was too small for the device-driven pass and has
+         * been grown: every read is on the device now, so the pass runs
+         * again over the whole chromosome, and the calls are downloaded
+         * again */
+        sync_up();
+        cudaStreamSynchronize(c->down_stream);
+        cudaStreamSynchronize(c->gather_stream);
+        rc2 = run_calling(c, {whole_segment(c)}, nullptr, nullptr);
+        if (rc2 == GSNP_OK && out) {
+            CK(cudaMemcpyAsync(out, c->d_out, (size_t)c->chr_len * sizeof(SiteCall), cudaMemcpyDeviceToHost,
+                               c->stream),
+               "download");
+            CK(cudaStreamSynchronize(c->stream), "download");
+        }
+    }
     cudaError_t e_up = sync_up(), e_down = cudaStreamSynchronize(c->down_stream);
     const cudaError_t e_gather = cudaStreamSynchronize(c->gather_stream);
     tl.rec("end", c->down_stream);
@@ -1226,6 +1457,40 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
 
 extern "C" {
 
+int gsnp_set_option(gsnp_context* c, const char* name, int64_t value) {
+    if (!c || !name) return GSNP_ERR_ARG;
+    const std::string n(name);
+    auto clamp = [](int64_t v, int lo, int hi) { return (int)std::max<int64_t>(lo, std::min<int64_t>(hi, v)); };
+    if (n == "persistent") c->stream_path = value != 0;
+    else if (n == "persistent_slots") c->stream_slots = value > 48 ? 64 : 48;
+    else if (n == "persistent_mode") c->stream_mode = clamp(value, 0, 2);
+    else if (n == "persistent_carveout") c->stream_carveout = clamp(value, 0, 100);
+    else if (n == "device_driven") c->device_driven = value != 0;
+    else if (n == "graphs") c->use_graphs = value != 0;
+    else if (n == "upload_streams") c->n_up = c->up_stream ? c->n_up : clamp(value, 1, gsnp_context::kMaxUpStreams);
+    else if (n.rfind("fast_carveout_", 0) == 0 || n.rfind("fp64_carveout_", 0) == 0 || n.rfind("bin_limit_", 0) == 0) {
+        const bool lim = n[0] == 'b';
+        const int slots = atoi(n.c_str() + (lim ? 10 : 14));
+        int b = 0;
+        while (b < kNumBins && bin_slots(b) != slots) ++b;
+        if (b == kNumBins) return fail(c, GSNP_ERR_ARG, "no depth bin of " + std::to_string(slots) + " slots");
+        if (lim) {
+            /* a bin takes columns up to its limit: at most its slots, above
+             * the previous bin's limit (the deepest bin takes the rest) */
+            if (b == kNumBins - 1) return GSNP_OK;
+            c->bin_limit[b] = clamp(value, b ? c->bin_limit[b - 1] : 1, slots);
+        } else {
+            c->bin_carveout[n[1] == 'a' ? 1 : 0][b] = clamp(value, 0, 100);
+        }
+    } else {
+        return fail(c, GSNP_ERR_ARG, "unknown option " + n);
+    }
+    /* grids and graphs follow the new settings */
+    c->grid_L = -1;
+    c->stream_ctas_L = -1;
+    return GSNP_OK;
+}
+
 int gsnp_context_create(int device, gsnp_context** out) {
     if (!out) return GSNP_ERR_ARG;
     *out = nullptr;
@@ -1243,18 +1508,32 @@ int gsnp_context_create(int device, gsnp_context** out) {
         return GSNP_ERR_CUDA;
     }
     c->own_stream = true;
-    /* GSNP_CALL_PATH=binned: the FP32 form through the depth-binned kernels
-     * only; GSNP_STREAM_SLOTS: record slots of the persistent kernel (48, 64);
-     * GSNP_STREAM_MODE: how it fetches reads (0 loads, 1 L2 bulk prefetch,
-     * 2 bulk copies into shared memory);
-     * GSNP_STREAM_CARVEOUT: its preferred shared-memory carveout, percent */
-    if (const char* e = getenv("GSNP_CALL_PATH")) c->stream_path = strcmp(e, "binned") != 0;
-    if (const char* e = getenv("GSNP_STREAM_SLOTS")) c->stream_slots = atoi(e) > 48 ? 64 : 48;
-    if (const char* e = getenv("GSNP_STREAM_MODE")) c->stream_mode = std::max(0, std::min(2, atoi(e)));
-    if (const char* e = getenv("GSNP_STREAM_CARVEOUT")) c->stream_carveout = std::max(0, std::min(100, atoi(e)));
-    /* GSNP_UPLOAD_STREAMS: copy streams of the alignment upload (1 to 4) */
-    if (const char* e = getenv("GSNP_UPLOAD_STREAMS"))
-        c->n_up = std::max(1, std::min((int)gsnp_context::kMaxUpStreams, atoi(e)));
+    /* options from the environment: GSNP_OPTIONS="name=value,..." (see
+     * gsnp_set_option), then GSNP_TUNE_FILE if it names a file of
+     * "name value" lines (written by gsnp_tune) */
+    auto apply_env = [&](const char* spec) {
+        std::string item;
+        for (const char* p = spec;; ++p) {
+            if (*p == ',' || *p == 0) {
+                const size_t eq = item.find('=');
+                if (eq != std::string::npos)
+                    (void)gsnp_set_option(c, item.substr(0, eq).c_str(), atoll(item.c_str() + eq + 1));
+                item.clear();
+                if (*p == 0) break;
+            } else {
+                item += *p;
+            }
+        }
+    };
+    if (const char* e = getenv("GSNP_TUNE_FILE")) {
+        if (FILE* f = fopen(e, "r")) {
+            char name[64];
+            long long v = 0;
+            while (fscanf(f, "%63s %lld", name, &v) == 2) (void)gsnp_set_option(c, name, v);
+            fclose(f);
+        }
+    }
+    if (const char* e = getenv("GSNP_OPTIONS")) apply_env(e);
     *out = c;
     return GSNP_OK;
 }
@@ -1289,6 +1568,7 @@ void gsnp_context_destroy(gsnp_context* c) {
         }
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     for (cudaEvent_t e : c->ev_gather) cudaEventDestroy(e);
     if (c->gather_stream) {
         cudaStreamSynchronize(c->gather_stream);
@@ -1467,10 +1747,244 @@ int gsnp_rank_table(double* out) {
     return GSNP_OK;
 }
 
+namespace gsnp {
+
+/* everything a captured pass depends on: its arguments (pointers, sizes,
+ * parameters), the segment and the launch configuration */
+uint64_t graph_key_of(gsnp_context* c, const Segment& g) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+        const uint8_t* b = static_cast<const uint8_t*>(p);
+        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    const CallArgs a = make_args(c);
+    mix(&a, sizeof a);
+    mix(&g, sizeof g);
+    const int cfg[] = {c->stream_path, c->stream_slots, c->stream_mode, c->stream_carveout, c->stream_ctas,
+                       c->deferred_grid, c->classify_grid};
+    mix(cfg, sizeof cfg);
+    mix(c->bin_grid, sizeof c->bin_grid);
+    mix(c->bin_carveout, sizeof c->bin_carveout);
+    mix(&c->n_gathered, sizeof c->n_gathered);
+    const void* ptrs[] = {c->d_deep, c->d_leftover, c->d_stream_ctl, c->d_dmax, c->d_bin_tiles, c->d_bin_count};
+    mix(ptrs, sizeof ptrs);
+    return h;
+}
+
+/* The resident recall as a CUDA graph: the device-driven pass over the whole
+ * chromosome is captured once and replayed while nothing it depends on
+ * changes. */
+int recall_graph(gsnp_context* c) {
+    {
+        const int rc = prepare_calling(c);
+        if (rc != GSNP_OK) return rc;
+    }
+    const std::vector<Segment> segs{whole_segment(c)};
+    const uint64_t key = graph_key_of(c, segs[0]);
+    if (!c->graph_exec || key != c->graph_key) {
+        if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        const int rc = enqueue_device(c, segs, nullptr, nullptr, false);
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (rc != GSNP_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        CK(e, "graph capture");
+        const cudaError_t ei = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(ei, "graph instantiate");
+        c->graph_key = key;
+    }
+    c->n_launches = 1;
+    c->launches[0].kind = kKindGraph;
+    c->launches[0].slots = 0;
+    c->launches[0].tiles = segs[0].t1 - segs[0].t0;
+    c->launches[0].sites = c->chr_len;
+    c->launches[0].ms = 0.f;
+    cudaEventRecord(c->ev[0], c->stream);
+    CK(cudaGraphLaunch(c->graph_exec, c->stream), "graph launch");
+    cudaEventRecord(c->ev[1], c->stream);
+    return finish_device(c);
+}
+
+}  // namespace gsnp
+
+namespace gsnp {
+
+/* one tuning measurement: the calling pass over segment g, best of `reps`,
+ * device time between events on the context's stream */
+float time_pass(gsnp_context* c, const Segment& g, int reps, int* rc) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < reps && *rc == GSNP_OK; ++r) {
+        cudaEventRecord(e0, c->stream);
+        *rc = run_calling(c, {g}, nullptr, nullptr);
+        if (*rc == kRedoDeferred) *rc = run_calling(c, {g}, nullptr, nullptr);
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
+}  // namespace gsnp
+
+int gsnp_tune(gsnp_context* c, int sample_windows, char* report, size_t report_cap) {
+    if (!c) return GSNP_ERR_ARG;
+    if (!c->called || !c->have_tables || c->n_gathered < c->n_dep)
+        return fail(c, GSNP_ERR_STATE, "tuning samples the resident reads of a finished call");
+    cudaSetDevice(c->device);
+    const WindowPlan& P = c->plan;
+    const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    const int64_t w0 = P.n_windows / 3, w1 = std::min<int64_t>(P.n_windows, w0 + std::max(1, sample_windows));
+    /* tile ranges of every read (cheap), calling of the sample's tiles only */
+    const Segment g{std::min(n_tiles, w0 * (kWin / kTile)), std::min(n_tiles, w1 * (kWin / kTile)), 0, c->n_dep, 0,
+                    kNoRead};
+    std::string rep;
+    char line[160];
+    int rc = GSNP_OK;
+    const bool fast = make_args(c).precision == 1;
+    const int kind = fast ? 1 : 0;
+    const char* prefix = fast ? "fast_carveout_" : "fp64_carveout_";
+    const bool saved_graphs = c->use_graphs;
+    c->device_driven = true;
+    (void)time_pass(c, g, 1, &rc);   /* warm-up: grids, scratch, tables in cache */
+
+    /* 1. the binned kernels: each bin's carveout, measured per launch */
+    c->stream_path = false;
+    static const int kCarveouts[] = {0, 58, 72, 86};
+    float bin_best[kNumBins];
+    int bin_choice[kNumBins];
+    for (int b = 0; b < kNumBins; ++b) {
+        bin_best[b] = 1e30f;
+        bin_choice[b] = c->bin_carveout[kind][b];
+    }
+    for (int cv : kCarveouts) {
+        for (int b = 0; b < kNumBins; ++b) c->bin_carveout[kind][b] = cv;
+        c->grid_L = -1;
+        float bin_ms[kNumBins] = {};
+        for (int r = 0; r < 2 && rc == GSNP_OK; ++r) {
+            rc = run_calling(c, {g}, nullptr, nullptr);
+            if (rc == kRedoDeferred) rc = run_calling(c, {g}, nullptr, nullptr);
+            float this_ms[kNumBins] = {};
+            for (int k = 0; k < c->n_launches; ++k)
+                if (c->launches[k].kind == (fast ? kKindFast : kKindFP64))
+                    for (int b = 0; b < kNumBins; ++b)
+                        if (bin_slots(b) == c->launches[k].slots) this_ms[b] += c->launches[k].ms;
+            for (int b = 0; b < kNumBins; ++b) bin_ms[b] = r == 0 ? this_ms[b] : std::min(bin_ms[b], this_ms[b]);
+        }
+        for (int b = 0; b < kNumBins; ++b)
+            if (bin_ms[b] < bin_best[b]) {
+                bin_best[b] = bin_ms[b];
+                bin_choice[b] = cv;
+            }
+        snprintf(line, sizeof line, "binned carveout %d:", cv);
+        rep += line;
+        for (int b = 0; b < kNumBins; ++b) {
+            snprintf(line, sizeof line, " %d:%.3f", bin_slots(b), bin_ms[b]);
+            rep += line;
+        }
+        rep += " ms\n";
+    }
+    for (int b = 0; b < kNumBins; ++b) c->bin_carveout[kind][b] = bin_choice[b];
+    c->grid_L = -1;
+
+    /* 2. the depth bins' limits of the two shallowest bins */
+    static const int kLimits[][2] = {{32, 40}, {30, 40}, {28, 40}, {32, 36}, {30, 38}};
+    float best_binned = 1e30f;
+    int best_lim = 0;
+    const int saved0 = c->bin_limit[0], saved1 = c->bin_limit[1];
+    for (int i = 0; i < (int)(sizeof kLimits / sizeof kLimits[0]) && rc == GSNP_OK; ++i) {
+        c->bin_limit[0] = kLimits[i][0];
+        c->bin_limit[1] = kLimits[i][1];
+        const float ms = time_pass(c, g, 2, &rc);
+        snprintf(line, sizeof line, "binned limits %d/%d: %.3f ms\n", kLimits[i][0], kLimits[i][1], ms);
+        rep += line;
+        if (ms < best_binned) {
+            best_binned = ms;
+            best_lim = i;
+        }
+    }
+    c->bin_limit[0] = rc == GSNP_OK ? kLimits[best_lim][0] : saved0;
+    c->bin_limit[1] = rc == GSNP_OK ? kLimits[best_lim][1] : saved1;
+
+    /* 3. the persistent kernel (FP32 form): slots, carveout, read mode */
+    float best_pers = 1e30f;
+    int best_slots = 48, best_cv = 0, best_mode = 0;
+    if (fast) {
+        c->stream_path = true;
+        for (int slots : {48, 64})
+            for (int cv : {0, 72, 86})
+                for (int mode : {0, 1}) {
+                    if (rc != GSNP_OK) break;
+                    c->stream_slots = slots;
+                    c->stream_carveout = cv;
+                    c->stream_mode = mode;
+                    c->stream_ctas_L = -1;
+                    const float ms = time_pass(c, g, 2, &rc);
+                    snprintf(line, sizeof line, "persistent slots %d carveout %d mode %d: %.3f ms\n", slots, cv, mode,
+                             ms);
+                    rep += line;
+                    if (ms < best_pers) {
+                        best_pers = ms;
+                        best_slots = slots;
+                        best_cv = cv;
+                        best_mode = mode;
+                    }
+                }
+        c->stream_slots = best_slots;
+        c->stream_carveout = best_cv;
+        c->stream_mode = best_mode;
+        c->stream_ctas_L = -1;
+    }
+    c->stream_path = fast && best_pers < best_binned;
+    c->use_graphs = saved_graphs;
+    if (rc != GSNP_OK) return rc;
+
+    /* the choice, as option lines (gsnp_set_option names) */
+    std::string opts;
+    snprintf(line, sizeof line, "persistent %d\npersistent_slots %d\npersistent_carveout %d\npersistent_mode %d\n",
+             c->stream_path ? 1 : 0, c->stream_slots, c->stream_carveout, c->stream_mode);
+    opts += line;
+    for (int b = 0; b < kNumBins; ++b) {
+        snprintf(line, sizeof line, "%s%d %d\n", prefix, bin_slots(b), c->bin_carveout[kind][b]);
+        opts += line;
+    }
+    snprintf(line, sizeof line, "bin_limit_32 %d\nbin_limit_40 %d\n", c->bin_limit[0], c->bin_limit[1]);
+    opts += line;
+    snprintf(line, sizeof line, "sample: windows %lld-%lld (%lld tiles); best binned %.3f ms, best persistent %.3f ms\n",
+             (long long)w0, (long long)w1, (long long)(g.t1 - g.t0), best_binned, fast ? best_pers : 0.f);
+    rep = opts + "# " + line + rep;
+    if (const char* path = getenv("GSNP_TUNE_FILE")) {
+        if (FILE* f = fopen(path, "w")) {
+            fputs(opts.c_str(), f);
+            fclose(f);
+        }
+    }
+    if (report && report_cap > 0) {
+        const size_t n = std::min(report_cap - 1, rep.size());
+        memcpy(report, rep.data(), n);
+        report[n] = 0;
+    }
+    return GSNP_OK;
+}
+
 int gsnp_recall_resident(gsnp_context* c) {
     if (!c || !c->have_tables || c->plan.n_windows == 0) return fail(c, GSNP_ERR_STATE, "nothing resident");
     cudaSetDevice(c->device);
-    return run_calling(c, {whole_segment(c)}, nullptr, nullptr);
+    int rc = c->device_driven && c->use_graphs ? recall_graph(c) : run_calling(c, {whole_segment(c)}, nullptr, nullptr);
+    /* the deferred pool was grown to what the pass asked for: run it again */
+    if (rc == kRedoDeferred) rc = run_calling(c, {whole_segment(c)}, nullptr, nullptr);
+    return rc;
 }
 
 int gsnp_fetch_sites(gsnp_context* c, int64_t first, int64_t count, gsnp_site_call* out) {

@@ -148,6 +148,47 @@ int gsnp_call_chromosome_into(gsnp_context* ctx, const gsnp_reads* reads, gsnp_s
  * (no host transfer); used to time the kernels alone. */
 int gsnp_recall_resident(gsnp_context* ctx);
 
+/* No counterpart in the reference (its launch configuration is fixed at
+ * build time).  Set a launch option of the context; the next calling pass
+ * uses it.  Names and values:
+ *   persistent            FP32 form: 1 the persistent region-ordered kernel
+ *                         with the binned kernels for the tiles it leaves,
+ *                         0 the depth-binned kernels only
+ *   persistent_slots      48 or 64 record slots of the persistent kernel
+ *   persistent_mode       0 read loads, 1 after a bulk L2 prefetch of the
+ *                         next tile's rows, 2 rows staged in shared memory by
+ *                         bulk copies
+ *   persistent_carveout   preferred shared-memory carveout, percent (0: the
+ *                         default)
+ *   fast_carveout_<S>, fp64_carveout_<S>   the same for the S-slot bin of the
+ *                         FP32 / FP64 binned kernel (S = 32 40 48 64 96 128 256)
+ *   bin_limit_<S>         deepest column the S-slot bin takes (at most S)
+ *   device_driven         1: launch sizes read on the device, no host wait
+ *                         inside a pass; 0: the host reads each bin's count
+ *   graphs                1: gsnp_recall_resident replays a CUDA graph
+ *   upload_streams        copy streams of the upload (1-4; before the first
+ *                         call only)
+ * GSNP_ERR_ARG for an unknown name or bin.  The environment variable
+ * GSNP_OPTIONS="name=value,..." sets options when a context is created, after
+ * the "name value" lines of the file GSNP_TUNE_FILE names (gsnp_tune). */
+int gsnp_set_option(gsnp_context* ctx, const char* name, int64_t value);
+
+/* No counterpart in the reference.  The launch autotuner: times the calling
+ * pass of the resident reads of the last call over a sample of
+ * `sample_windows` windows (from a third of the way along the chromosome)
+ * with candidate launch settings, and keeps the fastest:
+ *   - each binned kernel's shared-memory carveout (0, 58, 72, 86%), per bin;
+ *   - the column-depth limits of the two shallowest bins;
+ *   - for the FP32 form, the persistent kernel's record slots (48, 64),
+ *     carveout (0, 72, 86%) and read mode (loads, L2 prefetch), and whether
+ *     it or the binned kernels alone call the FP32 windows.
+ * The chosen settings are written to `report` as "name value" lines (the
+ * gsnp_set_option names), followed by the measurements as "#"-led and plain
+ * lines; when GSNP_TUNE_FILE is set the option lines are written to that file,
+ * which contexts created later load.  The sample's calls are recomputed with
+ * the same results.  GSNP_ERR_STATE before a finished call. */
+int gsnp_tune(gsnp_context* ctx, int sample_windows, char* report, size_t report_cap);
+
 /* Copy calls for sites [first, first + count) to host memory. */
 int gsnp_fetch_sites(gsnp_context* ctx, int64_t first, int64_t count, gsnp_site_call* out);
 

@@ -147,17 +147,49 @@ def test_persistent_and_binned_paths_agree(name, scale, native_lib, monkeypatch)
     flags = [f for f in w.cli_flags("dbsnp") if f != "-C"]
     calls = {}
     for path, slots, mode in (("binned", "48", "0"), ("persistent", "48", "0"), ("persistent", "64", "0"),
-                              ("persistent", "48", "1"), ("persistent", "48", "2"), ("persistent", "64", "2")):
-        monkeypatch.setenv("GSNP_CALL_PATH", path)
-        monkeypatch.setenv("GSNP_STREAM_SLOTS", slots)
-        monkeypatch.setenv("GSNP_STREAM_MODE", mode)
+                              ("persistent", "48", "1"), ("persistent", "48", "2"), ("persistent", "64", "2"),
+                              ("binned-host", "48", "0"), ("persistent-host", "64", "1")):
+        monkeypatch.setenv("GSNP_OPTIONS", "persistent=%d,persistent_slots=%s,persistent_mode=%s,device_driven=%d" % (
+            path.startswith("persistent"), slots, mode, not path.endswith("-host")))
         c, _, _ = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
         try:
             calls[(path, slots, mode)] = c.fetch()
             kinds = {li["kind"] for li in c.last_launches()}
         finally:
             c.close()
-        assert (4 in kinds) == (path == "persistent")
+        assert (4 in kinds) == path.startswith("persistent")
     base = calls[("binned", "48", "0")].tobytes()
     for key, v in calls.items():
         assert v.tobytes() == base, f"{name}: {key} differs from the binned path"
+
+
+
+@pytest.mark.gpu
+def test_graph_replay_and_tuning_keep_the_calls(tmp_path, native_lib, monkeypatch):
+    """The resident recall replayed as a CUDA graph, the autotuner's sample
+    passes and its chosen settings, and a new context loading them from the
+    tuning file, all give the calls of the first pass."""
+    tune_file = str(tmp_path / "tune.txt")
+    monkeypatch.setenv("GSNP_TUNE_FILE", tune_file)
+    w = synth.make_workload("c1", scale=0.05)
+    flags = [f for f in w.cli_flags("dbsnp") if f != "-C"]
+    c, reads, pm = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
+    try:
+        want = c.fetch().tobytes()
+        for _ in range(3):
+            c.recall_resident()
+            assert [li["kind"] for li in c.last_launches()] == [5]
+        assert c.fetch().tobytes() == want
+        report = c.tune(sample_windows=4)
+        assert "persistent " in report and "fast_carveout_40 " in report
+        c.recall_resident()
+        assert c.fetch().tobytes() == want
+    finally:
+        c.close()
+    lines = open(tune_file).read().split("\n")
+    assert any(x.startswith("persistent ") for x in lines)
+    c, reads, pm = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
+    try:
+        assert c.fetch().tobytes() == want
+    finally:
+        c.close()

@@ -70,7 +70,7 @@ def test_upload_over_several_copy_streams(up_streams, segs, native_lib, monkeypa
         want = c.fetch(0, w.genome_len).copy()
     finally:
         c.close()
-    monkeypatch.setenv("GSNP_UPLOAD_STREAMS", str(up_streams))
+    monkeypatch.setenv("GSNP_OPTIONS", "upload_streams=%d" % up_streams)
     monkeypatch.setenv("GSNP_SEGMENTS", str(segs))
     c, reads, pm = api.run_workload(w, flags, precision=api.PRECISION_FP32_FIXUP)
     try:
