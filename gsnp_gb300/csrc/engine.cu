@@ -426,6 +426,7 @@ struct gsnp_context {
     int grid_L = -1, deferred_grid = 0, classify_grid = 0, sms = 0;
     unsigned long long* d_dmax = nullptr;   /* [2] largest deferred request of the call's segments */
     cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t capture_stream = nullptr;
     uint64_t graph_key = 0;
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
@@ -1569,6 +1570,7 @@ void gsnp_context_destroy(gsnp_context* c) {
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
     for (cudaEvent_t e : c->ev_gather) cudaEventDestroy(e);
     if (c->gather_stream) {
         cudaStreamSynchronize(c->gather_stream);
@@ -1783,11 +1785,23 @@ int recall_graph(gsnp_context* c) {
     const uint64_t key = graph_key_of(c, segs[0]);
     if (!c->graph_exec || key != c->graph_key) {
         if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
         c->graph_exec = nullptr;
         cudaGraph_t graph = nullptr;
-        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        /* captured on a stream of its own: the caller's stream may be the
+         * legacy default stream, which cannot be captured */
+        if (!c->capture_stream)
+            CK(cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        const cudaStream_t user = c->stream;
+        c->stream = c->capture_stream;
+        cudaError_t eb = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+        if (eb != cudaSuccess) {
+            c->stream = user;
+            CK(eb, "graph capture");
+        }
         const int rc = enqueue_device(c, segs, nullptr, nullptr, false);
         const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        c->stream = user;
         if (rc != GSNP_OK) {
             if (graph) cudaGraphDestroy(graph);
             return rc;

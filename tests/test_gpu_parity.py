@@ -180,6 +180,10 @@ def test_graph_replay_and_tuning_keep_the_calls(tmp_path, native_lib, monkeypatc
             c.recall_resident()
             assert [li["kind"] for li in c.last_launches()] == [5]
         assert c.fetch().tobytes() == want
+        c.set_stream(0)   # the legacy default stream: captured on the library's own stream, replayed here
+        for _ in range(2):
+            c.recall_resident()
+        assert c.fetch().tobytes() == want
         report = c.tune(sample_windows=4)
         assert "persistent " in report and "fast_carveout_40 " in report
         c.recall_resident()
