@@ -972,6 +972,12 @@ cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_
     return cudaGetLastError();
 }
 
+/* Launchers set their kernel's shared-memory size and carveout before each
+ * launch, except while this thread captures a graph: the attributes were set
+ * when the grids were sized, before the capture. */
+thread_local bool g_launch_attributes = true;
+void set_launch_attributes(bool on) { g_launch_attributes = on; }
+
 size_t stream_smem_bytes(int slots, int L, int mode) {
     return call_smem_bytes(slots, L, true) +
            (mode == kStreamStaged ? (size_t)kStageHeader + (size_t)kStageReads * kStageSlot : 0);
@@ -996,7 +1002,7 @@ static cudaError_t stream_attr(int L, int* ctas_per_sm, int carveout = 0) {
 template <int SLOTS, int MODE>
 static cudaError_t launch_stream_one(const CallArgs& a, const StreamQueue& q, int ctas, int carveout,
                                      cudaStream_t stream) {
-    cudaError_t e = stream_attr<SLOTS, MODE>(a.L, nullptr, carveout);
+    cudaError_t e = g_launch_attributes ? stream_attr<SLOTS, MODE>(a.L, nullptr, carveout) : cudaSuccess;
     if (e != cudaSuccess) return e;
     call_stream_kernel<SLOTS, MODE><<<ctas, kTile, stream_smem_bytes(SLOTS, a.L, MODE), stream>>>(a, q);
     return cudaGetLastError();
@@ -1058,7 +1064,7 @@ static cudaError_t bin_attr(int kind, int L, int carveout, int* ctas_per_sm) {
 template <int SLOTS>
 static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles, const BinLaunch& bl,
                               cudaStream_t stream) {
-    cudaError_t e = bin_attr<SLOTS>(kind, a.L, bl.carveout, nullptr);
+    cudaError_t e = g_launch_attributes ? bin_attr<SLOTS>(kind, a.L, bl.carveout, nullptr) : cudaSuccess;
     if (e != cudaSuccess) return e;
     const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
     const unsigned grid = (unsigned)(bl.d_count ? bl.grid : bl.count);

@@ -36,6 +36,7 @@
 
 #include "dict.h"
 #include "rows.h"
+#include "columns_gpu.h"
 
 namespace gsnp {
 
@@ -412,6 +413,33 @@ private:
         f_.put(f_.f1517, snp.data(), 4 * snp.size());
     }
 };
+
+}  // namespace
+
+bool encode_window_host(int64_t len, int mode, const uint8_t* codes_w, const SiteCall* calls_w,
+                        const SiteCounts* counts_w, const DictCodec& dict, std::string* parts, std::string* err) {
+    /* make_row indexes the shown window's counts at hs * kWin + j: the
+     * window's counts sit after a window of padding */
+    std::vector<SiteCounts> shown;
+    if (mode == 1) {
+        shown.resize((size_t)(kWin + len));
+        std::copy(counts_w, counts_w + len, shown.begin() + kWin);
+    }
+    std::vector<CnsRow> rows((size_t)len);
+    for (int64_t j = 0; j < len; ++j)
+        rows[(size_t)j] = make_row(mode == 1 ? 1 : mode, 0, j, codes_w, calls_w, shown.empty() ? nullptr : shown.data());
+    Files f;
+    Writer wr(dict, f);
+    if (!wr.window(rows, err)) return false;
+    parts[0].swap(f.f346);
+    parts[1].swap(f.frle);
+    parts[2].swap(f.f10);
+    parts[3].swap(f.f111213);
+    parts[4].swap(f.f1517);
+    return true;
+}
+
+namespace {
 
 FILE* open_file(const std::string& path, const char* mode, std::string* err) {
     FILE* f = fopen(path.c_str(), mode);

@@ -1,0 +1,927 @@
+/*
+ * columns_gpu.cu - the -C compressed output encoded on the GPU.
+ *
+ * The five binary files of the -C output (cpp/compress.h:86-1312; the byte
+ * layouts are those of columns.cpp, which is pinned to the reference's files)
+ * are encoded window by window from the calls resident on the device: one CTA
+ * of 1024 threads per window, each thread owning 256 consecutive rows.  A
+ * window's rows are those the host writer builds (rows.h make_row: the site's
+ * call with the count columns of the window the reference's host arrays held),
+ * and each file's block is written in place into a per-window slice of a
+ * batch buffer:
+ *   .3_4_6            2-bit reference bases, N ids, genotype and best-base
+ *                     differences (ids by block-wide scans, in row order);
+ *   .5_7_8_9_14_16    six columns run-length encoded (run starts counted per
+ *                     thread, scanned, written in order), run values and run
+ *                     lengths each dictionary coded;
+ *   .10               2-bit second bases, N ids;
+ *   .11_12_13         the common / extra sparse lists, three dictionaries;
+ *   .15_17            sparse rank-sum values and dbSNP ids.
+ * Dictionaries (cuda_dictCompression's contract: the distinct values
+ * ascending, each value's index packed MSB-first) of integer columns go
+ * through a presence bitmap over the value range in shared memory and a scan
+ * of its word counts, which gives every value its index with no sort; those
+ * of doubles through a shared-memory hash set of their bit patterns (both
+ * zeros one key), sorted by a bitonic network.  The bits per index come from
+ * a table the host fills with the reference's own formula.
+ *
+ * A window whose block would not fit its slice, or whose double column has
+ * more distinct values than the hash set holds, is flagged; the host encodes
+ * that window itself.  The host then writes the blocks in window order.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "columns.h"
+#include "columns_gpu.h"
+#include "dict.h"
+#include "rows.h"
+
+namespace gsnp {
+namespace {
+
+constexpr int kEncThreads = 1024;
+constexpr int kEncPer = kWin / kEncThreads;           /* rows per thread */
+constexpr int kBitmapBits = kWin + 64;                /* value span of an integer dictionary */
+constexpr int kBitmapWords = kBitmapBits / 32;
+constexpr int kHashCap = 4096;                        /* slots of the double hash set */
+constexpr int kHashMax = kHashCap / 2;                /* distinct doubles a column may have */
+constexpr unsigned long long kEmptyKey = ~0ull;       /* a NaN pattern, never a value */
+
+/* per-window slice of each file's batch buffer: the worst case of every file
+ * but the run-length one (15, 4.25, 40 and 16 bytes per row at most), whose
+ * worst case a window of a few thousand runs is far from */
+constexpr size_t kCapHost[5] = {4u << 20, 12u << 20, 1300u << 10, 11u << 20, 5u << 20};
+
+enum : int { kF346 = 0, kFRle = 1, kF10 = 2, kF111213 = 3, kF1517 = 4 };
+
+__constant__ char c_abbv[17] = {'A', 'M', 'W', 'R', 'M', 'C', 'Y', 'S', 'W', 'Y', 'T', 'K', 'R', 'S', 'K', 'G', 'N'};
+__constant__ char c_actgn[8] = {'A', 'C', 'T', 'G', 'N', 'N', 'N', 'N'};
+
+struct EncArgs {
+    int64_t w0;                      /* first window of the batch */
+    const int64_t* call_len;         /* per window */
+    const int32_t* host_src;         /* per window */
+    const uint8_t* codes;
+    const SiteCall* calls;
+    const SiteCounts* counts;
+    const uint8_t* bits;             /* bits per dictionary index of a dictionary of d values */
+    uint8_t* out[5];                 /* [batch][cap[f]] */
+    uint64_t cap[5];
+    uint64_t* len;                   /* [batch][5] bytes used */
+    int* fallback;                   /* [batch] */
+    /* scratch, [batch][kWin] each */
+    uint64_t* s_val;                 /* run values (integer or double bits), sparse values */
+    uint32_t* s_aux;                 /* run starts, then run lengths */
+    uint64_t* s_dict;                /* dictionary values */
+};
+
+__device__ __forceinline__ void put8(uint8_t* p, uint8_t v) { *p = v; }
+__device__ __forceinline__ void put32(uint8_t* p, uint32_t v) {
+    p[0] = (uint8_t)v;
+    p[1] = (uint8_t)(v >> 8);
+    p[2] = (uint8_t)(v >> 16);
+    p[3] = (uint8_t)(v >> 24);
+}
+__device__ __forceinline__ void put64(uint8_t* p, uint64_t v) {
+    put32(p, (uint32_t)v);
+    put32(p + 4, (uint32_t)(v >> 32));
+}
+
+/* exclusive prefix of v over the CTA's threads in order; *total the sum */
+__device__ int64_t block_scan(int64_t v, int64_t* total) {
+    __shared__ int64_t ws[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int64_t s = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        ws[lane] = s;
+    }
+    __syncthreads();
+    const int64_t before = (warp ? ws[warp - 1] : 0) + x - v;
+    *total = ws[31];
+    __syncthreads();
+    return before;
+}
+
+__device__ int64_t block_min(int64_t v) {
+    __shared__ int64_t ws[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) ws[warp] = v;
+    __syncthreads();
+    int64_t r = ws[0];
+    for (int i = 1; i < 32; ++i) r = min(r, ws[i]);
+    __syncthreads();
+    return r;
+}
+
+__device__ int64_t block_max(int64_t v) { return -block_min(-v); }
+
+struct Enc {
+    const EncArgs& e;
+    int b;            /* window in the batch */
+    int64_t w;        /* window */
+    int n;            /* rows */
+    int hs;
+    int r0, r1;       /* this thread's rows */
+    bool bad;         /* CTA-uniform: the window falls back to the host */
+
+    __device__ CnsRow row(int j) const { return make_row(hs, w, j, e.codes, e.calls, e.counts); }
+    __device__ uint8_t* out(int f) const { return e.out[f] + (size_t)b * e.cap[f]; }
+    __device__ uint64_t* sval() const { return e.s_val + (size_t)b * kWin; }
+    __device__ uint32_t* saux() const { return e.s_aux + (size_t)b * kWin; }
+    __device__ uint64_t* sdict() const { return e.s_dict + (size_t)b * kWin; }
+    __device__ bool fits(int f, uint64_t bytes) {
+        if (bytes > e.cap[f]) bad = true;
+        return !bad;
+    }
+};
+
+/* ---- dictionaries ---------------------------------------------------- */
+
+/* Integer dictionary of the m values vals[0, m) (non-negative, span at most
+ * kBitmapBits): the bitmap and its word prefix counts in shared memory.
+ * Returns the dictionary size, or -1 when the span is too wide. */
+struct IntDict {
+    uint32_t* bm;     /* [kBitmapWords] */
+    uint32_t* pre;    /* [kBitmapWords] */
+    int64_t lo;
+    int d;
+
+    template <class V>
+    __device__ int build(const V* vals, int m) {
+        int64_t mn = INT64_MAX, mx = INT64_MIN;
+        for (int i = threadIdx.x; i < m; i += kEncThreads) {
+            mn = min(mn, (int64_t)vals[i]);
+            mx = max(mx, (int64_t)vals[i]);
+        }
+        mn = block_min(mn);
+        mx = block_max(mx);
+        if (m == 0) {
+            d = 0;
+            return 0;
+        }
+        if (mx - mn >= kBitmapBits) return -1;
+        lo = mn;
+        for (int i = threadIdx.x; i < kBitmapWords; i += kEncThreads) bm[i] = 0u;
+        __syncthreads();
+        for (int i = threadIdx.x; i < m; i += kEncThreads) {
+            const int64_t v = (int64_t)vals[i] - lo;
+            atomicOr(&bm[v >> 5], 1u << (v & 31));
+        }
+        __syncthreads();
+        constexpr int kChunk = (kBitmapWords + kEncThreads - 1) / kEncThreads;
+        const int c0 = threadIdx.x * kChunk;
+        int cnt = 0;
+        for (int k = c0; k < c0 + kChunk && k < kBitmapWords; ++k) cnt += __popc(bm[k]);
+        int64_t total = 0;
+        int run = (int)block_scan(cnt, &total);
+        for (int k = c0; k < c0 + kChunk && k < kBitmapWords; ++k) {
+            pre[k] = (uint32_t)run;
+            run += __popc(bm[k]);
+        }
+        __syncthreads();
+        d = (int)total;
+        return d;
+    }
+    __device__ uint32_t index(int64_t v) const {
+        const int64_t x = v - lo;
+        return pre[x >> 5] + __popc(bm[x >> 5] & ((1u << (x & 31)) - 1u));
+    }
+    /* the values ascending as 4-byte integers at dst */
+    __device__ void put_values(uint8_t* dst) const {
+        for (int k = threadIdx.x; k < kBitmapWords; k += kEncThreads) {
+            uint32_t bits = bm[k];
+            uint32_t r = pre[k];
+            while (bits) {
+                const int i = __ffs(bits) - 1;
+                bits &= bits - 1;
+                put32(dst + 4 * (size_t)r++, (uint32_t)(lo + (int64_t)k * 32 + i));
+            }
+        }
+    }
+};
+
+__device__ __forceinline__ unsigned long long dkey(double v) {
+    if (v == 0.0) v = 0.0;   /* -0.0 and +0.0: one key */
+    return (unsigned long long)__double_as_longlong(v);
+}
+
+/* Double dictionary through a hash set in shared memory; -1 when there are
+ * more than kHashMax distinct values. */
+struct DblDict {
+    unsigned long long* tab;   /* [kHashCap]: keys, then the sorted values' bits */
+    int* counter;              /* shared */
+    int* negzero;              /* shared */
+    int d;
+
+    __device__ int build(const uint64_t* vals, int m) {
+        for (int i = threadIdx.x; i < kHashCap; i += kEncThreads) tab[i] = kEmptyKey;
+        if (threadIdx.x == 0) {
+            *counter = 0;
+            *negzero = 0;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < m; i += kEncThreads) {
+            const double v = __longlong_as_double((long long)vals[i]);
+            if (v == 0.0 && signbit(v)) atomicOr(negzero, 1);
+            const unsigned long long k = dkey(v);
+            uint32_t h = (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> 52) & (kHashCap - 1);
+            for (int probe = 0; probe < kHashCap; ++probe) {
+                const unsigned long long old = atomicCAS(&tab[h], kEmptyKey, k);
+                if (old == kEmptyKey) {
+                    atomicAdd(counter, 1);
+                    break;
+                }
+                if (old == k) break;
+                h = (h + 1) & (kHashCap - 1);
+            }
+        }
+        __syncthreads();
+        const int cnt = *counter;
+        if (cnt > kHashMax) return -1;
+        /* compact the keys to the front, then sort them by value */
+        __shared__ int pos;
+        if (threadIdx.x == 0) pos = 0;
+        __syncthreads();
+        unsigned long long mine[kHashCap / kEncThreads];
+        int nm = 0;
+        for (int i = threadIdx.x; i < kHashCap; i += kEncThreads)
+            if (tab[i] != kEmptyKey) mine[nm++] = tab[i];
+        __syncthreads();
+        for (int i = 0; i < nm; ++i) tab[atomicAdd(&pos, 1)] = mine[i];
+        __syncthreads();
+        int p2 = 1;
+        while (p2 < cnt) p2 <<= 1;
+        for (int i = cnt + threadIdx.x; i < p2; i += kEncThreads)
+            tab[i] = (unsigned long long)__double_as_longlong(INFINITY);
+        __syncthreads();
+        for (int k = 2; k <= p2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < p2; i += kEncThreads) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const double a = __longlong_as_double((long long)tab[i]);
+                        const double c = __longlong_as_double((long long)tab[l]);
+                        const bool up = (i & k) == 0;
+                        if ((a > c) == up) {
+                            const unsigned long long t = tab[i];
+                            tab[i] = tab[l];
+                            tab[l] = t;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        d = cnt;
+        return d;
+    }
+    /* lower_bound of the double whose bits are given, in the sorted values */
+    __device__ uint32_t index(uint64_t bits) const {
+        const double v = __longlong_as_double((long long)dkey(__longlong_as_double((long long)bits)));
+        int lo = 0, hi = d;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__longlong_as_double((long long)tab[mid]) < v) lo = mid + 1;
+            else hi = mid;
+        }
+        return (uint32_t)lo;
+    }
+    /* value bits of entry i, the zero entry -0.0 when any input was -0.0 */
+    __device__ uint64_t value(int i) const {
+        const double v = __longlong_as_double((long long)tab[i]);
+        if (v == 0.0 && *negzero) return (uint64_t)__double_as_longlong(-0.0);
+        return tab[i];
+    }
+};
+
+/* the m indices of vals packed MSB-first, floor(32 / bits) per word, into
+ * dst (4 bytes per word) when write; returns the word count */
+template <class D, class V>
+__device__ uint64_t pack(const D& dict, const uint8_t* bits_tab, const V* vals, int m, uint8_t* dst, bool write) {
+    if (m == 0) return 0;
+    const int bits = bits_tab[dict.d];
+    const int per = 32 / bits;
+    const int64_t nw = (m + per - 1) / per;
+    if (write)
+        for (int64_t k = threadIdx.x; k < nw; k += kEncThreads) {
+            const int first = (int)(k * per), last = min(m, first + per);
+            uint32_t word = 0;
+            for (int i = first; i < last; ++i) word = (word << bits) | dict.index(vals[i]);
+            put32(dst + 4 * k, word);
+        }
+    return (uint64_t)nw;
+}
+
+/* ---- files ------------------------------------------------------------- */
+
+/* 2-bit code of A C G T (compress_kernel.cu:25-58); any other letter is an
+ * A here, the callers having replaced N */
+__device__ __forceinline__ uint32_t code2(char c) { return c == 'C' ? 1u : c == 'G' ? 2u : c == 'T' ? 3u : 0u; }
+
+__device__ void file_346(Enc& x, bool all_n) {
+    uint8_t* o = x.out(kF346);
+    const uint64_t n = (uint64_t)x.n;
+    if (all_n) {
+        if (threadIdx.x == 0) {
+            const uint64_t param[7] = {1, 0, n, 0, 0, 0, 0};
+            for (int i = 0; i < 7; ++i) put64(o + 8 * i, param[i]);
+            x.e.len[x.b * 5 + kF346] = 56;
+        }
+        return;
+    }
+    auto abc = [&](int j, char* a, char* b, char* c) {
+        const CnsRow r = x.row(j);
+        *a = *b = *c = 'N';
+        if (r.called()) {
+            *a = c_actgn[r.ori & 7];
+            *b = c_abbv[r.type1];
+            *c = c_actgn[r.base1 & 7];
+        }
+    };
+    int c4 = 0, c6 = 0, cn = 0;
+    for (int j = x.r0; j < x.r1; ++j) {
+        char a, b, c;
+        abc(j, &a, &b, &c);
+        c4 += b != a;
+        c6 += c != a;
+        cn += a == 'N';
+    }
+    int64_t N4, N6, NN;
+    int64_t o4 = block_scan(c4, &N4), o6 = block_scan(c6, &N6), on = block_scan(cn, &NN);
+    const uint64_t nw = (n + 15) / 16;
+    const uint64_t total = 56 + 5 * N4 + 5 * N6 + 4 * NN + 4 * nw;
+    if (!x.fits(kF346, total)) return;
+    const uint64_t b_id4 = 56, b_v4 = b_id4 + 4 * N4, b_id6 = b_v4 + N4, b_v6 = b_id6 + 4 * N6, b_idn = b_v6 + N6,
+                   b_code = b_idn + 4 * NN;
+    for (int j = x.r0; j < x.r1; ++j) {
+        char a, b, c;
+        abc(j, &a, &b, &c);
+        if (b != a) {
+            put32(o + b_id4 + 4 * o4, (uint32_t)j);
+            put8(o + b_v4 + o4, (uint8_t)b);
+            ++o4;
+        }
+        if (c != a) {
+            put32(o + b_id6 + 4 * o6, (uint32_t)j);
+            put8(o + b_v6 + o6, (uint8_t)c);
+            ++o6;
+        }
+        if (a == 'N') {
+            put32(o + b_idn + 4 * on, (uint32_t)j);
+            ++on;
+        }
+    }
+    /* the 16 code words of this thread's rows */
+    for (int k = 0; k < kEncPer / 16; ++k) {
+        const int first = x.r0 + 16 * k;
+        if (first >= x.n) break;
+        const int last = min(x.n, first + 16);
+        uint32_t word = 0;
+        for (int j = first; j < last; ++j) {
+            char a, b, c;
+            abc(j, &a, &b, &c);
+            word = (word << 2) | code2(a);
+        }
+        put32(o + b_code + 4 * (uint64_t)(first / 16), word);
+    }
+    if (threadIdx.x == 0) {
+        const uint64_t param[7] = {0, (uint64_t)(5 * N4 + 5 * N6 + 4 * NN) + 4 * nw, n, nw, (uint64_t)NN,
+                                   (uint64_t)N4, (uint64_t)N6};
+        for (int i = 0; i < 7; ++i) put64(o + 8 * i, param[i]);
+        x.e.len[x.b * 5 + kF346] = total;
+    }
+}
+
+/* value of RLE column k of a row (columns 5 7 8 9 14 as integers, 16 as the
+ * bits of a double) */
+__device__ __forceinline__ uint64_t rle_value(const CnsRow& r, int k) {
+    const bool called = r.called();
+    switch (k) {
+        case 0: return (uint64_t)(called ? r.q_cns : 0);
+        case 1: return (uint64_t)(called ? r.avg1 : 0);
+        case 2: return (uint64_t)(called ? r.cu1 : 0);
+        case 3: return (uint64_t)(called ? r.ca1 : 0);
+        case 4: return (uint64_t)(called ? (int)r.depth : 0);
+        default: {
+            const double v = called ? (r.depth == 0 ? 255.0 : (double)r.repeat / r.depth) : 255.0;
+            return (uint64_t)__double_as_longlong(v);
+        }
+    }
+}
+
+__device__ void file_rle(Enc& x, bool all_n, IntDict& idict, DblDict& ddict) {
+    uint8_t* o = x.out(kFRle);
+    __shared__ uint64_t pos;
+    if (threadIdx.x == 0) {
+        put32(o, all_n ? 1u : 0u);
+        pos = 4;
+    }
+    __syncthreads();
+    if (all_n) {
+        if (threadIdx.x == 0) x.e.len[x.b * 5 + kFRle] = 4;
+        return;
+    }
+    uint64_t* rv = x.sval();    /* run values */
+    uint32_t* rs = x.saux();    /* run starts */
+    uint64_t* rl = x.sdict();   /* run lengths */
+    for (int k = 0; k < 6; ++k) {
+        /* run starts: a row whose value differs from the row before */
+        int cs = 0;
+        uint64_t prev = x.r0 > 0 && x.r0 < x.n ? rle_value(x.row(x.r0 - 1), k) : 0;
+        for (int j = x.r0; j < x.r1; ++j) {
+            const uint64_t v = rle_value(x.row(j), k);
+            cs += j == 0 || v != prev;
+            prev = v;
+        }
+        int64_t R;
+        int64_t orun = block_scan(cs, &R);
+        prev = x.r0 > 0 && x.r0 < x.n ? rle_value(x.row(x.r0 - 1), k) : 0;
+        for (int j = x.r0; j < x.r1; ++j) {
+            const uint64_t v = rle_value(x.row(j), k);
+            if (j == 0 || v != prev) {
+                rv[orun] = v;
+                rs[orun] = (uint32_t)j;
+                ++orun;
+            }
+            prev = v;
+        }
+        __syncthreads();
+        for (int64_t r = threadIdx.x; r < R; r += kEncThreads)
+            rl[r] = (uint64_t)((r + 1 < R ? (int64_t)rs[r + 1] : (int64_t)x.n) - (int64_t)rs[r]);
+        __syncthreads();
+        const int m = (int)R;
+        const bool dbl = k == 5;
+        const uint64_t val_bytes = dbl ? 8 : 4;
+        /* sizes: the lengths' dictionary, then the values' */
+        if (idict.build(rl, m) < 0) {
+            x.bad = true;
+            return;
+        }
+        const uint64_t ndl = (uint64_t)idict.d, nwl = pack(idict, x.e.bits, rl, m, (uint8_t*)nullptr, false);
+        uint64_t ndv, nwv;
+        if (dbl) {
+            if (ddict.build(rv, m) < 0) {
+                x.bad = true;
+                return;
+            }
+            ndv = (uint64_t)ddict.d;
+            nwv = pack(ddict, x.e.bits, rv, m, (uint8_t*)nullptr, false);
+        } else {
+            if (idict.build(rv, m) < 0) {
+                x.bad = true;
+                return;
+            }
+            ndv = (uint64_t)idict.d;
+            nwv = pack(idict, x.e.bits, rv, m, (uint8_t*)nullptr, false);
+        }
+        const uint64_t p0 = pos;
+        const uint64_t b_cval = p0 + 48, b_clen = b_cval + 4 * nwv, b_dval = b_clen + 4 * nwl,
+                       b_dlen = b_dval + val_bytes * ndv, end = b_dlen + 4 * ndl;
+        if (!x.fits(kFRle, end)) return;
+        /* the values' words and dictionary (the dictionary built last) */
+        if (dbl) {
+            pack(ddict, x.e.bits, rv, m, o + b_cval, true);
+            for (int i = threadIdx.x; i < ddict.d; i += kEncThreads) put64(o + b_dval + 8 * (size_t)i, ddict.value(i));
+        } else {
+            pack(idict, x.e.bits, rv, m, o + b_cval, true);
+            idict.put_values(o + b_dval);
+        }
+        __syncthreads();
+        /* the lengths' dictionary again, for its words and values */
+        idict.build(rl, m);
+        pack(idict, x.e.bits, rl, m, o + b_clen, true);
+        idict.put_values(o + b_dlen);
+        if (threadIdx.x == 0) {
+            const uint64_t param[6] = {(uint64_t)R, nwv, nwl, ndv, ndl, 4 * nwv + 4 * nwl + val_bytes * ndv + 4 * ndl};
+            for (int i = 0; i < 6; ++i) put64(o + p0 + 8 * i, param[i]);
+            pos = end;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) x.e.len[x.b * 5 + kFRle] = pos;
+}
+
+__device__ void file_10(Enc& x, bool all_n) {
+    uint8_t* o = x.out(kF10);
+    if (threadIdx.x == 0) put32(o, all_n ? 1u : 0u);
+    if (all_n) {
+        if (threadIdx.x == 0) x.e.len[x.b * 5 + kF10] = 4;
+        return;
+    }
+    auto letter = [&](int j) {
+        const CnsRow r = x.row(j);
+        return (r.called() && r.base2 < 4) ? c_actgn[r.base2] : 'N';
+    };
+    int cn = 0;
+    for (int j = x.r0; j < x.r1; ++j) cn += letter(j) == 'N';
+    int64_t NN;
+    int64_t on = block_scan(cn, &NN);
+    const uint64_t n = (uint64_t)x.n, nw = (n + 15) / 16;
+    const uint64_t b_code = 4 + 24, b_nid = b_code + 4 * nw, total = b_nid + 4 * NN;
+    if (!x.fits(kF10, total)) return;
+    for (int j = x.r0; j < x.r1; ++j)
+        if (letter(j) == 'N') put32(o + b_nid + 4 * on++, (uint32_t)j);
+    for (int k = 0; k < kEncPer / 16; ++k) {
+        const int first = x.r0 + 16 * k;
+        if (first >= x.n) break;
+        const int last = min(x.n, first + 16);
+        uint32_t word = 0;
+        for (int j = first; j < last; ++j) {
+            const char c = letter(j);
+            word = (word << 2) | code2(c == 'N' ? 'A' : c);
+        }
+        put32(o + b_code + 4 * (uint64_t)(first / 16), word);
+    }
+    if (threadIdx.x == 0) {
+        put64(o + 4, (uint64_t)NN);
+        put64(o + 12, nw);
+        put64(o + 20, n);
+        x.e.len[x.b * 5 + kF10] = total;
+    }
+}
+
+__device__ void file_111213(Enc& x, bool all_n, IntDict& idict) {
+    uint8_t* o = x.out(kF111213);
+    if (threadIdx.x == 0) put32(o, all_n ? 1u : 0u);
+    if (all_n) {
+        if (threadIdx.x == 0) x.e.len[x.b * 5 + kF111213] = 4;
+        return;
+    }
+    /* 0: common, 1: extra column 12, 2: extra column 13, -1: none */
+    auto cls = [&](int j, int* v11, int* v12, int* v13) {
+        const CnsRow r = x.row(j);
+        *v11 = *v12 = *v13 = 0;
+        if (r.called() && r.base2 < 4) {
+            *v11 = r.avg2;
+            *v12 = r.cu2;
+            *v13 = r.ca2;
+        }
+        if (*v11 != 0) return 0;
+        if (*v11 != *v12) return 1;
+        if (*v11 != *v13) return 2;
+        return -1;
+    };
+    int cc = 0, c12 = 0, c13 = 0;
+    for (int j = x.r0; j < x.r1; ++j) {
+        int a, b, c;
+        const int k = cls(j, &a, &b, &c);
+        cc += k == 0;
+        c12 += k == 1;
+        c13 += k == 2;
+    }
+    int64_t NC, N12, N13;
+    int64_t oc = block_scan(cc, &NC), o12 = block_scan(c12, &N12), o13 = block_scan(c13, &N13);
+    const uint64_t b_e12id = 4 + 32, b_e12 = b_e12id + 4 * N12, b_e13id = b_e12 + 4 * N12, b_e13 = b_e13id + 4 * N13,
+                   b_cid = b_e13 + 4 * N13, b_dicts = b_cid + 4 * NC;
+    if (!x.fits(kF111213, b_dicts)) return;
+    /* the common entries' three values */
+    uint64_t* v11 = x.sval();
+    uint32_t* v12 = x.saux();
+    uint64_t* v13 = x.sdict();
+    for (int j = x.r0; j < x.r1; ++j) {
+        int a, b, c;
+        const int k = cls(j, &a, &b, &c);
+        if (k == 0) {
+            put32(o + b_cid + 4 * oc, (uint32_t)j);
+            v11[oc] = (uint64_t)a;
+            v12[oc] = (uint32_t)b;
+            v13[oc] = (uint64_t)c;
+            ++oc;
+        } else if (k == 1) {
+            put32(o + b_e12id + 4 * o12, (uint32_t)j);
+            put32(o + b_e12 + 4 * o12, (uint32_t)b);
+            ++o12;
+        } else if (k == 2) {
+            put32(o + b_e13id + 4 * o13, (uint32_t)j);
+            put32(o + b_e13 + 4 * o13, (uint32_t)c);
+            ++o13;
+        }
+    }
+    __syncthreads();
+    uint64_t p = b_dicts;
+    for (int col = 0; col < 3; ++col) {
+        const int m = (int)NC;
+        int r = col == 0 ? idict.build(v11, m) : col == 1 ? idict.build(v12, m) : idict.build(v13, m);
+        if (r < 0) {
+            x.bad = true;
+            return;
+        }
+        const uint64_t nd = (uint64_t)idict.d;
+        const uint64_t nw = col == 0   ? pack(idict, x.e.bits, v11, m, (uint8_t*)nullptr, false)
+                            : col == 1 ? pack(idict, x.e.bits, v12, m, (uint8_t*)nullptr, false)
+                                       : pack(idict, x.e.bits, v13, m, (uint8_t*)nullptr, false);
+        if (!x.fits(kF111213, p + 16 + 4 * nw + 4 * nd)) return;
+        if (col == 0) pack(idict, x.e.bits, v11, m, o + p + 16, true);
+        else if (col == 1) pack(idict, x.e.bits, v12, m, o + p + 16, true);
+        else pack(idict, x.e.bits, v13, m, o + p + 16, true);
+        idict.put_values(o + p + 16 + 4 * nw);
+        if (threadIdx.x == 0) {
+            put64(o + p, nw);
+            put64(o + p + 8, nd);
+        }
+        p += 16 + 4 * nw + 4 * nd;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        put64(o + 4, (uint64_t)x.n);
+        put64(o + 12, (uint64_t)NC);
+        put64(o + 20, (uint64_t)N12);
+        put64(o + 28, (uint64_t)N13);
+        x.e.len[x.b * 5 + kF111213] = p;
+    }
+}
+
+__device__ void file_1517(Enc& x, bool all_n) {
+    uint8_t* o = x.out(kF1517);
+    if (threadIdx.x == 0) put32(o, all_n ? 1u : 0u);
+    if (all_n) {
+        if (threadIdx.x == 0) x.e.len[x.b * 5 + kF1517] = 4;
+        return;
+    }
+    int cr = 0, cs = 0;
+    for (int j = x.r0; j < x.r1; ++j) {
+        const CnsRow r = x.row(j);
+        if (!r.called()) continue;
+        cr += r.rank_sum != 1.0;
+        cs += (r.ori & 8) != 0;
+    }
+    int64_t NR, NS;
+    int64_t orr = block_scan(cr, &NR), os = block_scan(cs, &NS);
+    const uint64_t b_id = 8, b_val = b_id + 4 * NR, b_cnt2 = b_val + 8 * NR, b_snp = b_cnt2 + 4, total = b_snp + 4 * NS;
+    if (!x.fits(kF1517, total)) return;
+    for (int j = x.r0; j < x.r1; ++j) {
+        const CnsRow r = x.row(j);
+        if (!r.called()) continue;
+        if (r.rank_sum != 1.0) {
+            put32(o + b_id + 4 * orr, (uint32_t)j);
+            put64(o + b_val + 8 * orr, (uint64_t)__double_as_longlong(r.rank_sum));
+            ++orr;
+        }
+        if (r.ori & 8) put32(o + b_snp + 4 * os++, (uint32_t)j);
+    }
+    if (threadIdx.x == 0) {
+        put32(o + 4, (uint32_t)NR);
+        put32(o + b_cnt2, (uint32_t)NS);
+        x.e.len[x.b * 5 + kF1517] = total;
+    }
+}
+
+__global__ void __launch_bounds__(kEncThreads) encode_windows_kernel(EncArgs e) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int hash_counter, hash_negzero;
+    IntDict idict;
+    idict.bm = reinterpret_cast<uint32_t*>(smem);
+    idict.pre = idict.bm + kBitmapWords;
+    idict.d = 0;
+    idict.lo = 0;
+    DblDict ddict;
+    ddict.tab = reinterpret_cast<unsigned long long*>(smem + 2 * kBitmapWords * 4);
+    ddict.counter = &hash_counter;
+    ddict.negzero = &hash_negzero;
+    ddict.d = 0;
+
+    Enc x{e, (int)blockIdx.x, e.w0 + blockIdx.x, 0, 0, 0, 0, false};
+    x.n = (int)e.call_len[x.w];
+    x.hs = e.host_src[x.w];
+    x.r0 = min(x.n, (int)threadIdx.x * kEncPer);
+    x.r1 = min(x.n, x.r0 + kEncPer);
+    bool mine = true;
+    for (int j = x.r0; j < x.r1; ++j) mine = mine && x.row(j).nflag;
+    const bool all_n = __syncthreads_and(mine) != 0;
+    file_346(x, all_n);
+    __syncthreads();
+    if (!x.bad) file_rle(x, all_n, idict, ddict);
+    __syncthreads();
+    if (!x.bad) file_10(x, all_n);
+    __syncthreads();
+    if (!x.bad) file_111213(x, all_n, idict);
+    __syncthreads();
+    if (!x.bad) file_1517(x, all_n);
+    if (threadIdx.x == 0) e.fallback[x.b] = x.bad ? 1 : 0;
+}
+
+constexpr size_t kEncSmem = 2 * kBitmapWords * 4 + kHashCap * 8;
+
+#define CKE(x, what)                                                      \
+    do {                                                                  \
+        cudaError_t e_ = (x);                                             \
+        if (e_ != cudaSuccess) {                                          \
+            *err = std::string(what) + ": " + cudaGetErrorString(e_);     \
+            return 1;                                                     \
+        }                                                                 \
+    } while (0)
+
+}  // namespace
+
+int write_columns_gpu(const WindowPlan& plan, const uint8_t* d_codes, const SiteCall* d_calls,
+                      const SiteCounts* d_counts, const uint8_t* h_codes, const char* chr_name,
+                      const std::string& base, cudaStream_t stream, int threads, ColumnsGpuStats* st,
+                      std::string* err) {
+    const char* ext[5] = {".3_4_6", ".5_7_8_9_14_16", ".10", ".11_12_13", ".15_17"};
+    FILE* fb[5] = {};
+    for (int i = 0; i < 5; ++i) {
+        fb[i] = fopen((base + ext[i]).c_str(), "wb");
+        if (!fb[i]) {
+            *err = "cannot create " + base + ext[i];
+            for (FILE* f : fb)
+                if (f) fclose(f);
+            return 1;
+        }
+    }
+    FILE* f12 = fopen((base + ".1_2").c_str(), "w");
+    if (!f12) {
+        *err = "cannot create " + base + ".1_2";
+        for (FILE* f : fb) fclose(f);
+        return 1;
+    }
+    fprintf(f12, "%lu\n", (unsigned long)plan.n_windows);
+    for (int64_t w = 0; w < plan.n_windows; ++w)
+        fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1),
+                (unsigned long)plan.call_len[w]);
+    int rc = 0;
+    auto finish = [&]() {
+        for (FILE* f : fb)
+            if (fclose(f) != 0 && rc == 0) {
+                *err = "write failed";
+                rc = 1;
+            }
+        if (fclose(f12) != 0 && rc == 0) {
+            *err = "write failed";
+            rc = 1;
+        }
+        return rc;
+    };
+    const int64_t nwin = plan.n_windows;
+    if (nwin == 0) return finish();
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t batch = std::min<int64_t>(nwin, std::max(32, sms));
+    /* device buffers of one batch; the window tables; the bits table */
+    std::vector<uint8_t> bits(kWin + 2);
+    bits[0] = 1;
+    for (size_t d = 1; d < bits.size(); ++d) bits[d] = (uint8_t)dict_bits((unsigned long)d);
+    std::vector<int32_t> hs(plan.host_src.begin(), plan.host_src.end());
+    uint8_t* d_out[5] = {};
+    uint8_t* d_bits = nullptr;
+    int64_t* d_len_tab = nullptr;
+    int32_t* d_hs = nullptr;
+    uint64_t* d_len = nullptr;
+    int* d_fb = nullptr;
+    uint64_t *d_sval = nullptr, *d_sdict = nullptr;
+    uint32_t* d_saux = nullptr;
+    auto free_dev = [&]() {
+        for (uint8_t* p : d_out) cudaFree(p);
+        cudaFree(d_bits);
+        cudaFree(d_len_tab);
+        cudaFree(d_hs);
+        cudaFree(d_len);
+        cudaFree(d_fb);
+        cudaFree(d_sval);
+        cudaFree(d_sdict);
+        cudaFree(d_saux);
+    };
+    cudaError_t ce = cudaSuccess;
+    for (int f = 0; f < 5 && ce == cudaSuccess; ++f) ce = cudaMalloc((void**)&d_out[f], kCapHost[f] * (size_t)batch);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_bits, bits.size());
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_len_tab, sizeof(int64_t) * nwin);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_hs, sizeof(int32_t) * nwin);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_len, sizeof(uint64_t) * 5 * batch);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_fb, sizeof(int) * batch);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sval, sizeof(uint64_t) * kWin * batch);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sdict, sizeof(uint64_t) * kWin * batch);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_saux, sizeof(uint32_t) * kWin * batch);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d_len_tab, plan.call_len.data(), sizeof(int64_t) * nwin, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d_hs, hs.data(), sizeof(int32_t) * nwin, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess)
+        ce = cudaFuncSetAttribute(encode_windows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEncSmem);
+    if (ce != cudaSuccess) {
+        free_dev();
+        finish();
+        *err = std::string("-C encoder set-up: ") + cudaGetErrorString(ce);
+        return 1;
+    }
+    std::vector<uint64_t> h_len((size_t)(5 * batch));
+    std::vector<int> h_fb((size_t)batch);
+    std::vector<std::string> blocks(5);
+    std::vector<std::vector<char>> host_buf(5);
+    HostDictCodec dict;
+    for (int64_t w0 = 0; w0 < nwin && rc == 0; w0 += batch) {
+        const int64_t nb = std::min(batch, nwin - w0);
+        EncArgs e;
+        e.w0 = w0;
+        e.call_len = d_len_tab;
+        e.host_src = d_hs;
+        e.codes = d_codes;
+        e.calls = d_calls;
+        e.counts = d_counts;
+        e.bits = d_bits;
+        for (int f = 0; f < 5; ++f) {
+            e.out[f] = d_out[f];
+            e.cap[f] = kCapHost[f];
+        }
+        e.len = d_len;
+        e.fallback = d_fb;
+        e.s_val = d_sval;
+        e.s_aux = d_saux;
+        e.s_dict = d_sdict;
+        encode_windows_kernel<<<(unsigned)nb, kEncThreads, kEncSmem, stream>>>(e);
+        ce = cudaGetLastError();
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_len.data(), d_len, sizeof(uint64_t) * 5 * nb, cudaMemcpyDeviceToHost, stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_fb.data(), d_fb, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+        if (ce != cudaSuccess) {
+            *err = std::string("-C encoder: ") + cudaGetErrorString(ce);
+            rc = 1;
+            break;
+        }
+        /* the batch's blocks, window by window, into one host buffer per file */
+        size_t tot[5] = {};
+        for (int64_t b = 0; b < nb; ++b)
+            if (!h_fb[(size_t)b])
+                for (int f = 0; f < 5; ++f) tot[f] += h_len[(size_t)(5 * b + f)];
+        for (int f = 0; f < 5; ++f) host_buf[f].resize(tot[f]);
+        size_t off[5] = {};
+        for (int64_t b = 0; b < nb && ce == cudaSuccess; ++b) {
+            if (h_fb[(size_t)b]) continue;
+            for (int f = 0; f < 5 && ce == cudaSuccess; ++f) {
+                const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
+                if (bytes)
+                    ce = cudaMemcpyAsync(host_buf[f].data() + off[f], d_out[f] + (size_t)b * kCapHost[f], bytes,
+                                         cudaMemcpyDeviceToHost, stream);
+                off[f] += bytes;
+            }
+        }
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+        if (ce != cudaSuccess) {
+            *err = std::string("-C encoder download: ") + cudaGetErrorString(ce);
+            rc = 1;
+            break;
+        }
+        /* windows the encoder left to the host, encoded in order among the others */
+        size_t wo[5] = {};
+        for (int64_t b = 0; b < nb && rc == 0; ++b) {
+            if (!h_fb[(size_t)b]) {
+                for (int f = 0; f < 5; ++f) {
+                    const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
+                    if (bytes && fwrite(host_buf[f].data() + wo[f], 1, bytes, fb[f]) != bytes) rc = 1;
+                    wo[f] += bytes;
+                }
+                continue;
+            }
+            if (st) ++st->host_windows;
+            const int64_t w = w0 + b;
+            const int64_t len = plan.call_len[(size_t)w];
+            std::vector<SiteCall> calls((size_t)len);
+            std::vector<SiteCounts> counts;
+            ce = cudaMemcpy(calls.data(), d_calls + w * (int64_t)kWin, sizeof(SiteCall) * len, cudaMemcpyDeviceToHost);
+            const int32_t src = plan.host_src[(size_t)w];
+            if (ce == cudaSuccess && src >= 0 && src != w && d_counts) {
+                counts.resize((size_t)len);
+                ce = cudaMemcpy(counts.data(), d_counts + (int64_t)src * kWin, sizeof(SiteCounts) * len,
+                                cudaMemcpyDeviceToHost);
+            }
+            if (ce != cudaSuccess) {
+                *err = std::string("-C encoder download: ") + cudaGetErrorString(ce);
+                rc = 1;
+                break;
+            }
+            std::string parts[5];
+            if (!encode_window_host(len, src >= 0 && src != w ? 1 : (src == w ? 0 : -1), h_codes + w * (int64_t)kWin,
+                                    calls.data(), counts.empty() ? nullptr : counts.data(), dict, parts, err)) {
+                rc = 1;
+                break;
+            }
+            for (int f = 0; f < 5; ++f)
+                if (!parts[f].empty() && fwrite(parts[f].data(), 1, parts[f].size(), fb[f]) != parts[f].size()) rc = 1;
+        }
+        if (rc && err->empty()) *err = "write failed";
+        if (st) st->windows += nb;
+    }
+    (void)threads;
+    free_dev();
+    return finish();
+}
+
+}  // namespace gsnp

@@ -28,6 +28,7 @@
 
 #include "calling.cuh"
 #include "columns.h"
+#include "columns_gpu.h"
 #include "emit.h"
 #include "gsnp_gb300.h"
 #include "plan.h"
@@ -44,6 +45,7 @@ int stream_ctas_per_sm(int slots, int L, int mode, int carveout);
 cudaError_t launch_bin(const CallArgs& a, int kind, int bin, const int32_t* tiles, const BinLaunch& bl,
                        cudaStream_t stream);
 int bin_ctas_per_sm(int kind, int bin, int L, int carveout);
+void set_launch_attributes(bool on);
 cudaError_t launch_snp_log_prior(const CallArgs& a, double* out, float* out32, cudaStream_t stream);
 cudaError_t launch_deferred(const CallArgs& a, int64_t n, cudaStream_t stream,
                             const unsigned long long* d_n = nullptr, int grid = 0);
@@ -420,6 +422,10 @@ struct gsnp_context {
      * call queues all its work without waiting on the host; the resident
      * recall replays it as a captured CUDA graph. */
     bool device_driven = true, use_graphs = true;
+    /* -C files: windows encoded on the device (columns_gpu.cu), or on the
+     * host threads (columns.cpp) */
+    bool columns_gpu = true;
+    int64_t columns_host_windows = 0;
     int bin_limit[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
     int bin_carveout[2][kNumBins] = {{0, 0, 0, 0, 0, 0, 0}, {0, 72, 0, 0, 0, 0, 0}};
     int bin_grid[2][kNumBins] = {};
@@ -428,6 +434,7 @@ struct gsnp_context {
     cudaGraphExec_t graph_exec = nullptr;
     cudaStream_t capture_stream = nullptr;
     uint64_t graph_key = 0;
+    bool graph_failed = false;      /* a capture failed: graphs were turned off */
     SiteCall* d_empty_calls = nullptr;  /* [16] */
     uint8_t* d_empty_valid = nullptr;   /* [16] */
     int64_t tiles_cap = 0;
@@ -1468,6 +1475,7 @@ int gsnp_set_option(gsnp_context* c, const char* name, int64_t value) {
     else if (n == "persistent_carveout") c->stream_carveout = clamp(value, 0, 100);
     else if (n == "device_driven") c->device_driven = value != 0;
     else if (n == "graphs") c->use_graphs = value != 0;
+    else if (n == "columns_gpu") c->columns_gpu = value != 0;
     else if (n == "upload_streams") c->n_up = c->up_stream ? c->n_up : clamp(value, 1, gsnp_context::kMaxUpStreams);
     else if (n.rfind("fast_carveout_", 0) == 0 || n.rfind("fp64_carveout_", 0) == 0 || n.rfind("bin_limit_", 0) == 0) {
         const bool lim = n[0] == 'b';
@@ -1793,23 +1801,30 @@ int recall_graph(gsnp_context* c) {
         if (!c->capture_stream)
             CK(cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         const cudaStream_t user = c->stream;
+        /* the capture waits for nothing the caller queued: the pass reads
+         * only what earlier calls left on the device, whose work the last
+         * finish_device or call waited for */
+        CK(cudaStreamSynchronize(user), "graph capture");
         c->stream = c->capture_stream;
-        cudaError_t eb = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
-        if (eb != cudaSuccess) {
-            c->stream = user;
-            CK(eb, "graph capture");
-        }
-        const int rc = enqueue_device(c, segs, nullptr, nullptr, false);
-        const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        set_launch_attributes(false);
+        const cudaError_t eb = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+        int rc = eb == cudaSuccess ? enqueue_device(c, segs, nullptr, nullptr, false) : GSNP_OK;
+        const cudaError_t e = eb == cudaSuccess ? cudaStreamEndCapture(c->stream, &graph) : eb;
+        set_launch_attributes(true);
         c->stream = user;
-        if (rc != GSNP_OK) {
-            if (graph) cudaGraphDestroy(graph);
-            return rc;
+        cudaError_t ei = e;
+        if (rc == GSNP_OK && e == cudaSuccess && graph) ei = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (rc != GSNP_OK || ei != cudaSuccess || !c->graph_exec) {
+            /* the pass cannot be captured here: it runs launch by launch,
+             * now and from now on */
+            (void)cudaGetLastError();
+            if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+            c->use_graphs = false;
+            c->graph_failed = true;
+            return run_calling(c, segs, nullptr, nullptr);
         }
-        CK(e, "graph capture");
-        const cudaError_t ei = cudaGraphInstantiate(&c->graph_exec, graph, 0);
-        cudaGraphDestroy(graph);
-        CK(ei, "graph instantiate");
         c->graph_key = key;
     }
     c->n_launches = 1;
@@ -2179,6 +2194,15 @@ extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const c
         return GSNP_OK;
     }
     if (!c->called) return fail(c, GSNP_ERR_STATE, "no call results");
+    if (c->columns_gpu) {
+        /* the windows encoded on the device, from the resident calls */
+        ColumnsGpuStats st;
+        if (write_columns_gpu(c->plan, c->d_codes, c->d_out, c->have_counts ? c->d_counts : nullptr,
+                              c->h_codes.data(), chr_name, base_path, c->stream, host_threads(), &st, &err) != 0)
+            return fail(c, GSNP_ERR_INPUT, err);
+        c->columns_host_windows = st.host_windows;
+        return GSNP_OK;
+    }
     const int rc = fetch_results(c, &calls, &counts);
     if (rc != GSNP_OK) return rc;
     if (write_columns(c->plan, c->h_codes.data(), calls.get(), c->have_counts ? counts.get() : nullptr, chr_name,

@@ -168,6 +168,8 @@ int gsnp_recall_resident(gsnp_context* ctx);
  *   graphs                1: gsnp_recall_resident replays a CUDA graph
  *   upload_streams        copy streams of the upload (1-4; before the first
  *                         call only)
+ *   columns_gpu           1: gsnp_write_columns encodes the windows on the
+ *                         GPU; 0: on the host threads (same bytes)
  * GSNP_ERR_ARG for an unknown name or bin.  The environment variable
  * GSNP_OPTIONS="name=value,..." sets options when a context is created, after
  * the "name value" lines of the file GSNP_TUNE_FILE names (gsnp_tune). */
