@@ -517,13 +517,31 @@ __device__ __forceinline__ void fp64_tile(const CallArgs& a, int64_t tile, uint3
     a.out[site] = call;
 }
 
+/* The list entries [0, *count) of a grid sized to the resident CTAs (one
+ * warp each): every CTA takes entry blockIdx.x first, then the next entry not
+ * yet taken from the counter *next (zero before the launch), so that the
+ * entries in flight stay neighbours and a CTA that drew cheap tiles takes
+ * more of them. */
+template <typename F>
+__device__ __forceinline__ void for_each_listed(const int* __restrict__ count, int* next, F&& f) {
+    const int n = *count;
+    int i = blockIdx.x;
+    while (i < n) {
+        f(i);
+        __syncwarp();
+        int j = 0;
+        if ((threadIdx.x & 31) == 0) j = atomicAdd(next, 1);
+        i = __shfl_sync(0xffffffffu, j, 0) + (int)gridDim.x;
+    }
+}
+
 /* The tiles of one depth bin: tiles[blockIdx.x] with count == nullptr (one
- * CTA per tile), else the first *count tiles of the list, each CTA taking
- * every gridDim.x-th (a grid sized to the resident CTAs, whatever the count
- * the device holds). */
+ * CTA per tile), else the first *count tiles of the list, handed out by
+ * for_each_listed (a grid sized to the resident CTAs, whatever the count the
+ * device holds). */
 template <int SLOTS>
 __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallArgs a, const int32_t* __restrict__ tiles,
-                                                                           const int* __restrict__ count) {
+                                                                           const int* __restrict__ count, int* next) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint32_t* recs_all = reinterpret_cast<uint32_t*>(smem);                   /* [SLOTS][kTile] */
     uint32_t* seen_all = reinterpret_cast<uint32_t*>(smem) + SLOTS * kTile;    /* [nw][kTile] */
@@ -531,11 +549,7 @@ __global__ void __launch_bounds__(kTile, kFp64CtasPerSm) call_tiles_kernel(CallA
         fp64_tile<SLOTS>(a, tiles[blockIdx.x], recs_all, seen_all);
         return;
     }
-    const int n = *count;
-    for (int i = blockIdx.x; i < n; i += gridDim.x) {
-        fp64_tile<SLOTS>(a, tiles[i], recs_all, seen_all);
-        __syncwarp();
-    }
+    for_each_listed(count, next, [&](int i) { fp64_tile<SLOTS>(a, tiles[i], recs_all, seen_all); });
 }
 
 /* ------------------------------------------------------------------------ */
@@ -666,7 +680,7 @@ __device__ __forceinline__ void fast_tile(const CallArgs& a, int64_t tile, uint3
  * bins' record columns are the CTA's slice of a.deep_recs. */
 template <int SLOTS>
 __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallArgs a, const int32_t* __restrict__ tiles,
-                                                                          const int* __restrict__ count) {
+                                                                          const int* __restrict__ count, int* next) {
     extern __shared__ __align__(16) uint8_t smem[];
     constexpr bool kGlobal = kGlobalRecs(SLOTS, true);
     uint32_t* recs_all = kGlobal ? a.deep_recs + (size_t)blockIdx.x * SLOTS * kTile : reinterpret_cast<uint32_t*>(smem);
@@ -675,11 +689,7 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
         fast_tile<SLOTS>(a, tiles[blockIdx.x], recs_all, seen_all);
         return;
     }
-    const int n = *count;
-    for (int i = blockIdx.x; i < n; i += gridDim.x) {
-        fast_tile<SLOTS>(a, tiles[i], recs_all, seen_all);
-        __syncwarp();
-    }
+    for_each_listed(count, next, [&](int i) { fast_tile<SLOTS>(a, tiles[i], recs_all, seen_all); });
 }
 
 /* ------------------------------------------------------------------------ */
@@ -962,7 +972,7 @@ size_t call_smem_bytes(int slots, int L, bool fast) {
 cudaError_t launch_classify(const CallArgs& a, int pass, int64_t t_begin, int64_t t_end, int* d_bin_count,
                             int32_t* d_bin_tiles, cudaStream_t stream, const int32_t* list, const int* d_count,
                             int grid) {
-    cudaError_t e = cudaMemsetAsync(d_bin_count, 0, sizeof(int) * 2 * kNumBins, stream);
+    cudaError_t e = cudaMemsetAsync(d_bin_count, 0, sizeof(int) * kBinCountInts, stream);
     if (e != cudaSuccess) return e;
     const unsigned blocks =
         d_count ? (unsigned)grid : (unsigned)((t_end - t_begin + kClassifyTiles - 1) / kClassifyTiles);
@@ -1069,8 +1079,8 @@ static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles,
     const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
     const unsigned grid = (unsigned)(bl.d_count ? bl.grid : bl.count);
     if (grid == 0) return cudaSuccess;
-    if (kind == kKindFast) call_fast_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count);
-    else call_tiles_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count);
+    if (kind == kKindFast) call_fast_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count, bl.d_next);
+    else call_tiles_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count, bl.d_next);
     return cudaGetLastError();
 }
 

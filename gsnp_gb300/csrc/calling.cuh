@@ -59,14 +59,19 @@ enum WindowFlags : uint8_t {
 constexpr int kStreamChunk = 2;
 
 /* One launch of a depth bin's kernel: `count` tiles, one CTA each; or, with
- * d_count, the count the device holds, taken by `grid` CTAs in turn.  The
- * preferred shared-memory carveout in percent (0: the default). */
+ * d_count, the count the device holds, taken by `grid` CTAs from the counter
+ * d_next.  The preferred shared-memory carveout in percent (0: the default). */
 struct BinLaunch {
     int count;
     const int* d_count;
     int grid;
     int carveout;
+    int* d_next;
 };
+
+/* the ints of the bins' count area: the tile count of each FP64 bin, then of
+ * each fast bin, then the same bins' hand-out counters (classify zeroes all) */
+constexpr int kBinCountInts = 4 * kNumBins;
 
 /* work queue of one launch of the persistent FP32 kernel (call_stream_kernel) */
 struct StreamQueue {

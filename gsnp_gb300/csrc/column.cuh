@@ -48,41 +48,6 @@ GSNP_HDI void bitonic_sort(uint32_t* v) {
             }
 }
 
-/* Ascending in-register sort of v[0, T), T a power of two, by Batcher's
- * odd-even merge network: 191 comparators for T = 32 where the bitonic
- * network has 240.  Every index is a compile-time constant once the loops
- * are unrolled, so v stays in registers and every lane runs the same
- * instructions. */
-template <int T>
-GSNP_HDI void oddeven_sort(uint32_t* v) {
-#pragma unroll
-    for (int p = 1; p < T; p <<= 1)
-#pragma unroll
-        for (int k = p; k >= 1; k >>= 1)
-#pragma unroll
-            for (int j = k % p; j <= T - 1 - k; j += 2 * k)
-#pragma unroll
-                for (int i = 0; i < k; ++i) {
-                    const int x = i + j, y = i + j + k;
-                    if (y < T && x / (2 * p) == y / (2 * p)) {
-                        const uint32_t a = v[x], b = v[y];
-                        v[x] = a < b ? a : b;
-                        v[y] = a < b ? b : a;
-                    }
-                }
-}
-
-/* the network of the column sort (oddeven_sort, or bitonic_sort with
- * GSNP_BITONIC defined) */
-template <int T>
-GSNP_HDI void sort_network(uint32_t* v) {
-#ifdef GSNP_BITONIC
-    bitonic_sort<T>(v);
-#else
-    oddeven_sort<T>(v);
-#endif
-}
-
 /* Merge the ascending v[0, cnt) (cnt <= T) into the ascending column prefix
  * recs[0, P), from the back: each v[j], largest first, moves the prefix
  * records above it up by the number of v entries still to place, then takes
@@ -123,7 +88,7 @@ GSNP_HDI void sort_column(uint32_t* recs, int num) {
     uint32_t v[32];
 #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = i < num ? recs[i * kTile] : 0xFFFFFFFFu;
-    sort_network<32>(v);
+    bitonic_sort<32>(v);
 #pragma unroll
     for (int i = 0; i < 32; ++i)
         if (i < num) recs[i * kTile] = v[i];
@@ -133,7 +98,7 @@ GSNP_HDI void sort_column(uint32_t* recs, int num) {
             const int cnt = num - c0 < C ? num - c0 : C;
 #pragma unroll
             for (int i = 0; i < C; ++i) v[i] = i < cnt ? recs[(c0 + i) * kTile] : 0xFFFFFFFFu;
-            sort_network<C>(v);
+            bitonic_sort<C>(v);
             merge_back<C>(recs, c0, v, cnt);
         }
     }

@@ -399,7 +399,7 @@ struct gsnp_context {
     /* scratch */
     int* d_error = nullptr;
     unsigned long long* d_stats = nullptr;
-    int* d_bin_count = nullptr;     /* [2 * kNumBins] FP64 bins, then fast bins */
+    int* d_bin_count = nullptr;     /* [kBinCountInts]: counts of the FP64 bins, then fast bins, then counters */
     int32_t* d_bin_tiles = nullptr; /* [2 * kNumBins][n_tiles] */
     DeferredSite* d_dsites = nullptr;        /* sites the fast kernel deferred */
     uint32_t* d_dpool = nullptr;             /* their sorted records */
@@ -1084,7 +1084,8 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
                 /* after the persistent kernel, the fast bins get only tiles
                  * deeper than its record slots */
                 if (kind == kKindFast && use_stream && kSlotsOf(b) <= c->stream_slots) continue;
-                const BinLaunch bl{0, c->d_bin_count + ki * kNumBins + b, c->bin_grid[ki][b], c->bin_carveout[ki][b]};
+                const BinLaunch bl{0, c->d_bin_count + ki * kNumBins + b, c->bin_grid[ki][b], c->bin_carveout[ki][b],
+                                   c->d_bin_count + (2 + ki) * kNumBins + b};
                 const int kb = begin(kind, kSlotsOf(b), 0);
                 CK(launch_bin(a, kind, b, c->d_bin_tiles + (int64_t)(ki * kNumBins + b) * n_tiles, bl, c->stream),
                    "calling kernel");
@@ -1509,7 +1510,7 @@ int gsnp_context_create(int device, gsnp_context** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_error, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_stats, sizeof(unsigned long long) * kNumStats);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bin_count, sizeof(int) * 2 * kNumBins);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_bin_count, sizeof(int) * kBinCountInts);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_dcount, sizeof(unsigned long long) * 2);
     if (e != cudaSuccess) {
         free_all(c);
@@ -1793,7 +1794,6 @@ int recall_graph(gsnp_context* c) {
     const uint64_t key = graph_key_of(c, segs[0]);
     if (!c->graph_exec || key != c->graph_key) {
         if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-    if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
         c->graph_exec = nullptr;
         cudaGraph_t graph = nullptr;
         /* captured on a stream of its own: the caller's stream may be the
