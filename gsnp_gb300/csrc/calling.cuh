@@ -99,7 +99,8 @@ struct CallArgs {
     const float* snp_lp32;       /* [n_snp][12] the same in FP32, by table column */
     /* tables */
     const double* lik64;         /* [qa_rows][L][4][10] log10 genotype terms */
-    const float* lik32;          /* same, rounded to FP32 */
+    const float* lik32;          /* same, rounded to FP32: [qa_rows][L][4][8] columns 0-7 */
+    const float* lik32b;         /* [qa_rows][L][4][2] columns 8-9 */
     int qa_rows;
     const uint8_t* qadj;         /* [tmax][gmax][65] adjusted quality */
     int tmax, gmax;

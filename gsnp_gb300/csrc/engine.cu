@@ -650,6 +650,7 @@ CallArgs make_args(gsnp_context* c) {
     a.snp_lp32 = c->d_snp_lp32;
     a.lik64 = c->d_lik64;
     a.lik32 = c->d_lik32;
+    a.lik32b = c->d_lik32 ? c->d_lik32 + (size_t)c->tables.qa_rows * c->tables.L * 4 * 8 : nullptr;
     a.qa_rows = c->tables.qa_rows;
     a.qadj = c->d_qadj;
     a.tmax = c->tables.tmax;

@@ -135,12 +135,24 @@ struct Kahan10 {
     }
 };
 
+/* The ten FP32 terms of one table row in two loads: columns 0-7 with one
+ * 256-bit load (a.lik32 rows are 32 bytes on a 32-byte boundary), columns 8-9
+ * with one 64-bit load.  Table rows are read at random by the lanes of a warp,
+ * and the L1 data stage takes about one wavefront per lane and load
+ * instruction, so the number of loads per row, not their width, sets its
+ * cost. */
 __device__ __forceinline__ void lik32_row(const CallArgs& a, int qa, int coord, int o, float* x) {
-    const float4* row = reinterpret_cast<const float4*>(a.lik32 + ((size_t)(qa * a.L + coord) * 4 + o) * 12);
-    const float4 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2);
-    x[0] = x0.x; x[1] = x0.y; x[2] = x0.z; x[3] = x0.w;
-    x[4] = x1.x; x[5] = x1.y; x[6] = x1.z; x[7] = x1.w;
-    x[8] = x2.x; x[9] = x2.y;
+    const size_t r = (size_t)(qa * a.L + coord) * 4 + o;
+#ifdef __CUDA_ARCH__
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(x[3]), "=f"(x[4]), "=f"(x[5]), "=f"(x[6]), "=f"(x[7])
+        : "l"(a.lik32 + r * 8));
+#else
+    for (int v = 0; v < 8; ++v) x[v] = a.lik32[r * 8 + v];
+#endif
+    const float2 t = __ldg(reinterpret_cast<const float2*>(a.lik32b) + r);
+    x[8] = t.x;
+    x[9] = t.y;
 }
 
 template <int BITS = 1>

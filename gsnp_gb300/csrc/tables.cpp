@@ -75,7 +75,7 @@ int build_tables(const gsnp_params& p, const double* pm, const double* p_prior, 
     /* materialised genotype terms (kernel/likelihood_kernel.cu:137-161) for
      * the adjusted qualities and read cycles that can occur */
     t->lik64.assign((size_t)t->qa_rows * L * 4 * 10, 0.0);
-    t->lik32.assign((size_t)t->qa_rows * L * 4 * 12, 0.0f);
+    t->lik32.assign((size_t)t->qa_rows * L * 4 * 10, 0.0f);
     t->all_nonpositive = true;
     for (int q = 0; q < t->qa_rows; ++q)
         for (int c = 0; c < L; ++c)
@@ -93,9 +93,13 @@ int build_tables(const gsnp_params& p, const double* pm, const double* p_prior, 
                         ++k;
                     }
             }
-    /* FP32 copy with rows padded to 12 entries (three 16-byte loads) */
-    for (size_t r = 0; r < (size_t)t->qa_rows * L * 4; ++r)
-        for (int k = 0; k < 10; ++k) t->lik32[r * 12 + k] = (float)t->lik64[r * 10 + k];
+    /* FP32 copy in two parts, so that a row takes two loads: columns 0-7 of
+     * every row (32 bytes, one 256-bit load), then columns 8-9 (8 bytes) */
+    const size_t rows = (size_t)t->qa_rows * L * 4;
+    for (size_t r = 0; r < rows; ++r) {
+        for (int k = 0; k < 8; ++k) t->lik32[r * 8 + k] = (float)t->lik64[r * 10 + k];
+        for (int k = 8; k < 10; ++k) t->lik32[rows * 8 + r * 2 + (k - 8)] = (float)t->lik64[r * 10 + k];
+    }
 
     t->log_prior.resize(128);
     for (int i = 0; i < 128; ++i) t->log_prior[i] = gsnp_cr_log10(p_prior[i]);

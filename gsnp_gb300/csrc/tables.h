@@ -18,7 +18,8 @@ struct HostTables {
     int qa_rows = 0;                /* adjusted qualities 0 .. qa_rows-1 */
     int tmax = 0, gmax = 0;         /* q_adj table bounds: tmp < tmax, gdc < gmax */
     std::vector<double> lik64;      /* [qa_rows][L][4][10] */
-    std::vector<float> lik32;       /* [qa_rows][L][4][12], FP32, rows padded to 12 */
+    std::vector<float> lik32;       /* FP32: [qa_rows][L][4][8] columns 0-7 of each row, then
+                                       [qa_rows][L][4][2] columns 8-9 */
     std::vector<uint8_t> qadj;      /* [tmax][gmax][65] */
     std::vector<double> log_prior;  /* [128] correctly rounded log10 of p_prior */
     std::vector<float> log_prior32; /* [8][12] log_prior in FP32 by table column */

@@ -120,6 +120,7 @@ int main(int argc, char** argv) {
     a.L = t.L;
     a.lik64 = t.lik64.data();
     a.lik32 = t.lik32.data();
+    a.lik32b = t.lik32.data() + (size_t)t.qa_rows * t.L * 4 * 8;
     a.qa_rows = t.qa_rows;
     a.qadj = t.qadj.data();
     a.tmax = t.tmax;
