@@ -58,6 +58,22 @@ int64_t bin_global_words(int kind, int bin, int64_t count);
 
 /* ---- device helpers ---- */
 
+/* a site decided by the deferred pass and its call */
+struct DeferredCall {
+    int64_t site;
+    SiteCall call;
+};
+
+/* dst[i] = (site, call) of deferred site i, i < n */
+__global__ void deferred_calls_kernel(const DeferredSite* __restrict__ ds, const SiteCall* __restrict__ out, int64_t n,
+                                      DeferredCall* __restrict__ dst) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t site = ds[i].site;
+        dst[i].site = site;
+        dst[i].call = out[site];
+    }
+}
+
 /* dmax[i] = max(dmax[i], v[i]) for i < 2 (one thread each) */
 __global__ void track_max_kernel(const unsigned long long* __restrict__ v, unsigned long long* __restrict__ dmax) {
     if (threadIdx.x < 2) dmax[threadIdx.x] = max(dmax[threadIdx.x], v[threadIdx.x]);
@@ -422,6 +438,9 @@ struct gsnp_context {
      * call queues all its work without waiting on the host; the resident
      * recall replays it as a captured CUDA graph. */
     bool device_driven = true, use_graphs = true;
+    bool deferred_at_end = false;   /* the last pass ran its deferred sites after its last segment */
+    DeferredCall* d_patch = nullptr;   /* their final calls, for the host copy of the calls */
+    int64_t patch_cap = 0;
     /* -C files: windows encoded on the device (columns_gpu.cu), or on the
      * host threads (columns.cpp) */
     bool columns_gpu = true;
@@ -627,7 +646,7 @@ void free_all(gsnp_context* c) {
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
                     c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep, c->d_stream_ctl, c->d_leftover,
-                    c->d_dmax};
+                    c->d_dmax, c->d_patch};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -819,6 +838,7 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
 int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::function<int(size_t)>& before,
                 const std::function<int(size_t)>& after) {
     const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    c->deferred_at_end = false;
     {
         const int rc = prepare_calling(c);
         if (rc != GSNP_OK) return rc;
@@ -1060,6 +1080,26 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
     const bool fast = make_args(c).precision == 1;
     const bool use_stream = c->stream_path && fast;
     int* d_left = reinterpret_cast<int*>(c->d_stream_ctl + 1);
+    /* With several segments the deferred sites of all of them go to one pool
+     * and one deferred pass runs after the last segment: the pass takes about
+     * the time of its slowest site (one thread per site, serial FP64 work),
+     * whatever their number, so a pass per segment would cost that time per
+     * segment.  The segments' downloads then hold those sites pending, and
+     * call_chromosome patches them in (patch_deferred_calls). */
+    const bool defer_to_end = fast && segs.size() > 1;
+    c->deferred_at_end = defer_to_end;
+    if (defer_to_end) CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+    auto deferred_pass = [&]() -> int {
+        CallArgs a = make_args(c);
+        a.n_reads = c->n_gathered;
+        a.deep_recs = c->d_deep;
+        const int kd = begin(kKindDeferred, 0, 0);
+        CK(launch_deferred(a, 0, c->stream, c->d_dcount, c->deferred_grid), "deferred calling kernel");
+        end(kd);
+        track_max_kernel<<<1, 2, 0, c->stream>>>(c->d_dcount, c->d_dmax);
+        CK(cudaGetLastError(), "deferred counts");
+        return GSNP_OK;
+    };
     for (size_t si = 0; si < segs.size(); ++si) {
         const Segment& g = segs[si];
         if (before) {
@@ -1078,7 +1118,7 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
         a.deep_recs = c->d_deep;
         int k = begin(kKindClassify, 0, g.t1 - g.t0);
         CK(launch_tile_bounds(a, g.dlo, g.dhi, g.next_pos, c->stream), "tile bounds kernel");
-        CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
+        if (!defer_to_end) CK(cudaMemsetAsync(c->d_dcount, 0, sizeof(unsigned long long) * 2, c->stream), "memset");
         auto bins = [&](int kind, int pass) -> int {
             const int ki = kind == kKindFast ? 1 : 0;
             for (int b = 0; b < kNumBins; ++b) {
@@ -1119,11 +1159,10 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
         if (fast) {
             const int rc = bins(kKindFast, 0);
             if (rc != GSNP_OK) return rc;
-            const int kd = begin(kKindDeferred, 0, 0);
-            CK(launch_deferred(a, 0, c->stream, c->d_dcount, c->deferred_grid), "deferred calling kernel");
-            end(kd);
-            track_max_kernel<<<1, 2, 0, c->stream>>>(c->d_dcount, c->d_dmax);
-            CK(cudaGetLastError(), "deferred counts");
+            if (!defer_to_end) {
+                const int rd = deferred_pass();
+                if (rd != GSNP_OK) return rd;
+            }
         }
         /* pass 1: the windows whose likelihood another window kept */
         if (external) {
@@ -1143,6 +1182,30 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
             if (rc != GSNP_OK) return rc;
         }
     }
+    if (defer_to_end) return deferred_pass();
+    return GSNP_OK;
+}
+
+/* After a pass whose deferred sites ran once after its last segment: their
+ * final calls into the host copy `out`, whose segments were downloaded with
+ * those sites still pending.  The streams that wrote `out` are idle. */
+int patch_deferred_calls(gsnp_context* c, gsnp_site_call* out) {
+    const int64_t n = std::min<int64_t>((int64_t)c->h_dcount[0], c->dsite_cap);
+    if (n <= 0) return GSNP_OK;
+    if (n > c->patch_cap) {
+        CK(dev_alloc(&c->d_patch, (size_t)n), "cudaMalloc deferred calls");
+        c->patch_cap = n;
+    }
+    const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 1024);
+    deferred_calls_kernel<<<blocks, 256, 0, c->stream>>>(c->d_dsites, c->d_out, n, c->d_patch);
+    CK(cudaGetLastError(), "deferred calls");
+    std::vector<DeferredCall> h((size_t)n);
+    CK(cudaMemcpyAsync(h.data(), c->d_patch, (size_t)n * sizeof(DeferredCall), cudaMemcpyDeviceToHost, c->stream),
+       "download");
+    CK(cudaStreamSynchronize(c->stream), "download");
+    SiteCall* o = reinterpret_cast<SiteCall*>(out);
+    for (const DeferredCall& d : h) o[d.site] = d.call;
+    c->d2h_bytes += (uint64_t)n * sizeof(DeferredCall);
     return GSNP_OK;
 }
 
@@ -1460,6 +1523,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     memcpy(&gerr, c->h_map + kMapGerror, sizeof(int));
     if (gerr == 3) return fail(c, GSNP_ERR_STATE, "deposited alignment list does not match the window replay");
     if (gerr) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
+    if (out && c->deferred_at_end) return patch_deferred_calls(c, out);
     return GSNP_OK;
 }
 
