@@ -69,6 +69,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch settings (no autotuner)")
     ap.add_argument("--tune-windows", type=int, default=32, help="windows of 262,144 sites the autotuner samples")
+    ap.add_argument("--stream-windows", type=int, default=16,
+                    help="windows per chunk of the streamed (bounded device memory) e2e call")
     return ap.parse_args()
 
 
@@ -161,6 +163,7 @@ def load_peaks():
 # no traffic.
 NCU_BYTES_PER_SITE = {
     ("c1", 2, 40): 150.6,   # call_fast_kernel<40>: 324.6 MB (dram__bytes.sum) over 2,154,656 sites
+    ("c1", 4, 48): 95.0,    # call_stream_kernel<48>: 325.2 MB read + 150.1 MB written over 5,000,000 sites
 }
 
 
@@ -449,14 +452,58 @@ def main():
         ms = (time.perf_counter() - t1) * 1e3
         files = [os.path.join(cdir, f) for f in os.listdir(cdir)]
         columns = ({"ms": round(ms, 2), "bytes": sum(os.path.getsize(f) for f in files), "files": len(files),
-                    "note": "gsnp_write_columns of the last call: download, window encoding on the host threads, "
-                            "write to a temporary directory"}
+                    "note": "gsnp_write_columns of the last call: windows encoded on the GPU (the host encoder takes "
+                            "any window that overflows its buffers), downloaded, written to a temporary directory"}
                    if rc == 0 else {"error": "gsnp_write_columns returned %d" % rc})
     except Exception as e:   # informational only: never costs the bench line
         columns = {"error": repr(e)[:200]}
     finally:
         if cdir:
             shutil.rmtree(cdir, ignore_errors=True)
+
+    # ---- end to end in bounded device memory (gsnp_call_streamed), both forms:
+    # each step uploads the alignments chunk by chunk, calls them and writes
+    # every call to pinned host memory and the -C files to a temporary
+    # directory; measured last, since no call stays resident after it ----
+    streamed = None
+    sdir = None
+    try:
+        sdir = tempfile.mkdtemp(prefix="gsnp_bench_streamed_")
+        caller.set_option("stream_windows", args.stream_windows)
+        forms = {}
+        for prec in (precision, other):
+            caller.load_tables(api.params_from_flags(flags, prec), pm, prior, rank_tab)
+            ts = []
+            for i in range(1 + e2e_steps):
+                barrier()
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                caller.call_streamed(reads, w.chr_name, out_pinned.data_ptr(), None, os.path.join(sdir, "cns"))
+                torch.cuda.synchronize()
+                if i > 0:
+                    ts.append(time.perf_counter() - t1)
+            forms[prec] = ts
+        h2d_s, d2h_s = caller.transfer_bytes()
+        ring, writer = caller.stream_footprint()
+        ts = max_over_ranks(statistics.median(forms[precision]))
+        ts_other = max_over_ranks(statistics.median(forms[other]))
+        streamed = {"value": world * sites / ts, "unit": UNIT, "h2d_bytes_per_step": int(h2d_s),
+                    "d2h_bytes_per_step": int(d2h_s), "steps": e2e_steps, "stat": "median step",
+                    "step_ms": [round(t * 1e3, 2) for t in forms[precision]],
+                    "other_form": {"form": "fp64 plain" if other == api.PRECISION_FP64 else "fp32+fp64 fixup",
+                                   "value": world * sites / ts_other,
+                                   "step_ms": [round(t * 1e3, 2) for t in forms[other]]},
+                    "stream_windows": args.stream_windows,
+                    "device_ring_bytes": ring, "columns_writer_bytes": writer,
+                    "per_site_resident_bytes": 1 + 4 / 32,
+                    "note": "gsnp_call_streamed: chunks of stream_windows windows through a two-slot device ring "
+                            "(alignments of the chunk being uploaded and of the one being called, its calls); "
+                            "outputs: every call to pinned host memory and the six -C files"}
+    except Exception as e:   # informational: never costs the bench line
+        streamed = {"error": repr(e)[:200]}
+    finally:
+        if sdir:
+            shutil.rmtree(sdir, ignore_errors=True)
 
     # ---- roofline of the dominant kernel (the calling launch with most device time) ----
     peaks, peak_kind = load_peaks()
@@ -502,6 +549,7 @@ def main():
                     "steps": e2e_steps, "stat": "median step",
                     "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
             "e2e_text": e2e_text,
+            "e2e_streamed": streamed,
             "cns_parity": parity,
             "cns_text": ({"ms": round(min(text_ms), 2), "rows": sites,
                           "note": "gsnp_write_cns of the last call to the null device: GPU formatting, download, write"}

@@ -81,6 +81,9 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_rank_table": (ctypes.c_int, [_P]),
         "gsnp_call_chromosome": (ctypes.c_int, [_P, ctypes.POINTER(Reads)]),
         "gsnp_call_chromosome_into": (ctypes.c_int, [_P, ctypes.POINTER(Reads), _P]),
+        "gsnp_call_streamed": (ctypes.c_int, [_P, ctypes.POINTER(Reads), ctypes.c_char_p, _P, ctypes.c_char_p,
+                                              ctypes.c_char_p]),
+        "gsnp_stream_footprint": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
         "gsnp_write_cns": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p]),
         "gsnp_write_columns": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p]),
         "gsnp_recall_resident": (ctypes.c_int, [_P]),
@@ -259,6 +262,21 @@ class Caller:
         memory of length * 32 bytes, pinned for the downloads to overlap)."""
         self._check(self.lib.gsnp_call_chromosome_into(self.ctx, ctypes.byref(reads), out_ptr),
                     "gsnp_call_chromosome_into")
+
+    def call_streamed(self, reads: Reads, chr_name: Optional[str] = None, out_ptr: Optional[int] = None,
+                      cns_path: Optional[str] = None, columns_base: Optional[str] = None) -> None:
+        """Call the chromosome in chunks of the "stream_windows" option's
+        windows with bounded device memory, writing each chunk's calls to
+        out_ptr and its cns text and -C windows to the files given."""
+        enc = lambda s: s.encode() if s is not None else None
+        self._check(self.lib.gsnp_call_streamed(self.ctx, ctypes.byref(reads), enc(chr_name), out_ptr,
+                                                enc(cns_path), enc(columns_base)), "gsnp_call_streamed")
+
+    def stream_footprint(self) -> tuple:
+        """(ring bytes, -C writer bytes) a streamed call holds on the device"""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self.lib.gsnp_stream_footprint(self.ctx, ctypes.byref(a), ctypes.byref(b)), "gsnp_stream_footprint")
+        return int(a.value), int(b.value)
 
     def recall_resident(self) -> None:
         self._check(self.lib.gsnp_recall_resident(self.ctx), "gsnp_recall_resident")

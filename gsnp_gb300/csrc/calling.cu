@@ -250,8 +250,8 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
     const int64_t p = site + 1;
     const int64_t win_end = (site / kWin + 1) * (int64_t)kWin;
     const int64_t max_start = (p == win_end) ? win_end - 1 : p;
-    const int64_t lo = lower_bound_g(a.pos, a.n_reads, p - a.L + 1);
-    const int64_t hi = lower_bound_g(a.pos, a.n_reads, max_start + 1);
+    const int64_t lo = a.read_lo + lower_bound_g(a.pos + a.read_lo, a.n_reads - a.read_lo, p - a.L + 1);
+    const int64_t hi = a.read_lo + lower_bound_g(a.pos + a.read_lo, a.n_reads - a.read_lo, max_start + 1);
     int dep_uni = 0, qsum = 0;
     const signed char qmin = (signed char)a.qmin;
     for (int64_t r = lo; r < hi; ++r) {
@@ -282,24 +282,29 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
  * start of read r_end is next_pos (kNoRead past the last read), so that a
  * segment of the reads can be done before the next segment is on the device:
  * consecutive segments share their boundary thread, which writes the same
- * values twice. */
+ * values twice.  Only tiles [tile_lo, n_tiles) are written.  When the device
+ * holds reads from read_lo > 0 on (a streamed chunk, whose first read is the
+ * lower bound of its first tile's first boundary), the start before read_lo
+ * is taken as tile_lo * kTile - L: it is at least that read's start and below
+ * every boundary of the chunk's tiles. */
 __global__ void tile_bounds_kernel(const int32_t* __restrict__ pos, int64_t r_begin, int64_t r_end, int64_t next_pos,
-                                   int64_t n_tiles, int L, int64_t* __restrict__ rng) {
+                                   int64_t tile_lo, int64_t n_tiles, int64_t read_lo, int L,
+                                   int64_t* __restrict__ rng) {
     const int64_t r = r_begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r > r_end) return;
-    const int64_t lo = r == 0 ? -kNoRead : (int64_t)pos[r - 1];
+    const int64_t lo = r == 0 ? -kNoRead : r == read_lo ? tile_lo * kTile - L : (int64_t)pos[r - 1];
     const int64_t hi = r == r_end ? next_pos : (int64_t)pos[r];
     if (lo >= hi) return;
     auto fdiv = [](int64_t x) { return x >= 0 ? x / kTile : -((-x + kTile - 1) / kTile); };
     /* first boundaries t*kTile - L + 1 in (lo, hi] */
     int64_t t0 = fdiv(lo + L - 1) + 1, t1 = fdiv(hi + L - 1);
-    if (t0 < 0) t0 = 0;
+    if (t0 < tile_lo) t0 = tile_lo;
     if (t1 > n_tiles - 1) t1 = n_tiles - 1;
     for (int64_t t = t0; t <= t1; ++t) rng[t * 2] = r;
     /* second boundaries (t + 1)*kTile in (lo, hi] */
     t0 = fdiv(lo);
     t1 = fdiv(hi) - 1;
-    if (t0 < 0) t0 = 0;
+    if (t0 < tile_lo) t0 = tile_lo;
     if (t1 > n_tiles - 1) t1 = n_tiles - 1;
     for (int64_t t = t0; t <= t1; ++t) rng[t * 2 + 1] = r;
 }
@@ -307,8 +312,8 @@ __global__ void tile_bounds_kernel(const int32_t* __restrict__ pos, int64_t r_be
 cudaError_t launch_tile_bounds(const CallArgs& a, int64_t r_begin, int64_t r_end, int64_t next_pos,
                                cudaStream_t stream) {
     const int64_t n = r_end - r_begin + 1;
-    tile_bounds_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(a.pos, r_begin, r_end, next_pos, a.n_tiles,
-                                                                         a.L, a.tile_rng);
+    tile_bounds_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(a.pos, r_begin, r_end, next_pos, a.tile_lo,
+                                                                         a.n_tiles, a.read_lo, a.L, a.tile_rng);
     return cudaGetLastError();
 }
 
@@ -422,7 +427,7 @@ __global__ void __launch_bounds__(kClassifyThreads) classify_tiles_kernel(CallAr
         sbin_base[threadIdx.x] = cnt ? atomicAdd(&bin_count[threadIdx.x], cnt) : 0;
     }
     __syncthreads();
-    if (my_bin >= 0) bin_tiles[(int64_t)my_bin * a.n_tiles + sbin_base[my_bin] + my_rank] = (int32_t)tile;
+    if (my_bin >= 0) bin_tiles[(int64_t)my_bin * a.bin_stride + sbin_base[my_bin] + my_rank] = (int32_t)tile;
     __syncthreads();
     }
 }

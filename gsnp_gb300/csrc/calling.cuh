@@ -88,6 +88,7 @@ struct CallArgs {
     const uint8_t* strand;       /* '+' or '-' */
     const uint16_t* bq;          /* [n_reads][L]: base char | quality char << 8 */
     int64_t n_reads;
+    int64_t read_lo;             /* reads [read_lo, n_reads) are on the device (0 unless streamed) */
     int L;                       /* -L: read pitch and coordinate bound */
     /* reference */
     const uint8_t* ori;          /* 4-bit site code per position */
@@ -118,7 +119,9 @@ struct CallArgs {
     const uint8_t* win_flags;    /* per window */
     const int32_t* win_lik_src;  /* per window: window whose likelihood is used (-1: zeros) */
     /* tiles */
-    int64_t n_tiles;
+    int64_t n_tiles;             /* end of the tiles the tile arrays hold */
+    int64_t tile_lo;             /* their first tile (0 unless streamed) */
+    int64_t bin_stride;          /* entries of each depth bin's tile list */
     int64_t* tile_rng;           /* [n_tiles][2]: reads starting in [s0 - L + 1, s0 + kTile) of each tile */
     int64_t* warp_rng;           /* [n_tiles][2]: reads that can cover each tile's sites */
     int bin_limit[kNumBins];     /* deepest column each depth bin takes (at most its record slots) */

@@ -733,123 +733,148 @@ constexpr size_t kEncSmem = 2 * kBitmapWords * 4 + kHashCap * 8;
 
 }  // namespace
 
-int write_columns_gpu(const WindowPlan& plan, const uint8_t* d_codes, const SiteCall* d_calls,
-                      const SiteCounts* d_counts, const uint8_t* h_codes, const char* chr_name,
-                      const std::string& base, cudaStream_t stream, int threads, ColumnsGpuStats* st,
-                      std::string* err) {
+ColumnsGpuWriter::~ColumnsGpuWriter() {
+    if (fb_[0] || f12_) {
+        std::string e;
+        close(&e);
+    }
+    release();
+}
+
+void ColumnsGpuWriter::release() {
+    for (uint8_t*& p : d_out_) {
+        cudaFree(p);
+        p = nullptr;
+    }
+    cudaFree(d_bits_);
+    cudaFree(d_len_tab_);
+    cudaFree(d_len_);
+    cudaFree(d_fb_);
+    cudaFree(d_sval_);
+    cudaFree(d_sdict_);
+    cudaFree(d_saux_);
+    d_bits_ = nullptr;
+    d_len_tab_ = nullptr;
+    d_len_ = nullptr;
+    d_fb_ = nullptr;
+    d_sval_ = d_sdict_ = nullptr;
+    d_saux_ = nullptr;
+    batch_cap_ = 0;
+    len_tab_windows_ = 0;
+}
+
+int ColumnsGpuWriter::open(const WindowPlan& plan, const char* chr_name, const std::string& base, int64_t batch,
+                           std::string* err) {
+    if (fb_[0] || f12_) close(err);
+    plan_ = &plan;
+    next_window_ = 0;
     const char* ext[5] = {".3_4_6", ".5_7_8_9_14_16", ".10", ".11_12_13", ".15_17"};
-    FILE* fb[5] = {};
     for (int i = 0; i < 5; ++i) {
-        fb[i] = fopen((base + ext[i]).c_str(), "wb");
-        if (!fb[i]) {
+        fb_[i] = fopen((base + ext[i]).c_str(), "wb");
+        if (!fb_[i]) {
             *err = "cannot create " + base + ext[i];
-            for (FILE* f : fb)
-                if (f) fclose(f);
+            close(err);
+            *err = "cannot create " + base + ext[i];
             return 1;
         }
     }
-    FILE* f12 = fopen((base + ".1_2").c_str(), "w");
-    if (!f12) {
+    f12_ = fopen((base + ".1_2").c_str(), "w");
+    if (!f12_) {
+        close(err);
         *err = "cannot create " + base + ".1_2";
-        for (FILE* f : fb) fclose(f);
         return 1;
     }
-    fprintf(f12, "%lu\n", (unsigned long)plan.n_windows);
+    fprintf(f12_, "%lu\n", (unsigned long)plan.n_windows);
     for (int64_t w = 0; w < plan.n_windows; ++w)
-        fprintf(f12, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1),
+        fprintf(f12_, "%s\t%lu\t%lu\n", chr_name, (unsigned long)(w * (int64_t)kWin + 1),
                 (unsigned long)plan.call_len[w]);
-    int rc = 0;
-    auto finish = [&]() {
-        for (FILE* f : fb)
-            if (fclose(f) != 0 && rc == 0) {
-                *err = "write failed";
-                rc = 1;
-            }
-        if (fclose(f12) != 0 && rc == 0) {
-            *err = "write failed";
-            rc = 1;
-        }
-        return rc;
-    };
-    const int64_t nwin = plan.n_windows;
-    if (nwin == 0) return finish();
-    int sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t batch = std::min<int64_t>(nwin, std::max(32, sms));
-    /* device buffers of one batch; the window tables; the bits table */
-    std::vector<uint8_t> bits(kWin + 2);
-    bits[0] = 1;
-    for (size_t d = 1; d < bits.size(); ++d) bits[d] = (uint8_t)dict_bits((unsigned long)d);
-    std::vector<int32_t> hs(plan.host_src.begin(), plan.host_src.end());
-    uint8_t* d_out[5] = {};
-    uint8_t* d_bits = nullptr;
-    int64_t* d_len_tab = nullptr;
-    int32_t* d_hs = nullptr;
-    uint64_t* d_len = nullptr;
-    int* d_fb = nullptr;
-    uint64_t *d_sval = nullptr, *d_sdict = nullptr;
-    uint32_t* d_saux = nullptr;
-    auto free_dev = [&]() {
-        for (uint8_t* p : d_out) cudaFree(p);
-        cudaFree(d_bits);
-        cudaFree(d_len_tab);
-        cudaFree(d_hs);
-        cudaFree(d_len);
-        cudaFree(d_fb);
-        cudaFree(d_sval);
-        cudaFree(d_sdict);
-        cudaFree(d_saux);
-    };
+    /* device buffers of one batch of windows, kept from one use to the next */
+    batch = std::max<int64_t>(1, batch);
     cudaError_t ce = cudaSuccess;
-    for (int f = 0; f < 5 && ce == cudaSuccess; ++f) ce = cudaMalloc((void**)&d_out[f], kCapHost[f] * (size_t)batch);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_bits, bits.size());
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_len_tab, sizeof(int64_t) * nwin);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_hs, sizeof(int32_t) * nwin);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_len, sizeof(uint64_t) * 5 * batch);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_fb, sizeof(int) * batch);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sval, sizeof(uint64_t) * kWin * batch);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sdict, sizeof(uint64_t) * kWin * batch);
-    if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_saux, sizeof(uint32_t) * kWin * batch);
-    if (ce == cudaSuccess) ce = cudaMemcpy(d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemcpy(d_len_tab, plan.call_len.data(), sizeof(int64_t) * nwin, cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemcpy(d_hs, hs.data(), sizeof(int32_t) * nwin, cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess)
-        ce = cudaFuncSetAttribute(encode_windows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEncSmem);
-    if (ce != cudaSuccess) {
-        free_dev();
-        finish();
-        *err = std::string("-C encoder set-up: ") + cudaGetErrorString(ce);
+    if (batch > batch_cap_) {
+        release();
+        for (int f = 0; f < 5 && ce == cudaSuccess; ++f) ce = cudaMalloc((void**)&d_out_[f], kCapHost[f] * (size_t)batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_bits_, kWin + 2);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_len_, sizeof(uint64_t) * 5 * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_fb_, sizeof(int) * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sval_, sizeof(uint64_t) * kWin * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sdict_, sizeof(uint64_t) * kWin * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_saux_, sizeof(uint32_t) * kWin * batch);
+        if (ce == cudaSuccess) {
+            std::vector<uint8_t> bits(kWin + 2);
+            bits[0] = 1;
+            for (size_t d = 1; d < bits.size(); ++d) bits[d] = (uint8_t)dict_bits((unsigned long)d);
+            ce = cudaMemcpy(d_bits_, bits.data(), bits.size(), cudaMemcpyHostToDevice);
+        }
+        if (ce == cudaSuccess)
+            ce = cudaFuncSetAttribute(encode_windows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEncSmem);
+        if (ce != cudaSuccess) {
+            release();
+            close(err);
+            *err = std::string("-C encoder set-up: ") + cudaGetErrorString(ce);
+            return 1;
+        }
+        batch_cap_ = batch;
+    }
+    if (plan.n_windows > len_tab_windows_) {
+        cudaFree(d_len_tab_);
+        d_len_tab_ = nullptr;
+        ce = cudaMalloc((void**)&d_len_tab_, sizeof(int64_t) * std::max<int64_t>(1, plan.n_windows));
+        if (ce != cudaSuccess) {
+            len_tab_windows_ = 0;
+            close(err);
+            *err = std::string("-C encoder set-up: ") + cudaGetErrorString(ce);
+            return 1;
+        }
+        len_tab_windows_ = plan.n_windows;
+    }
+    if (plan.n_windows > 0) {
+        ce = cudaMemcpy(d_len_tab_, plan.call_len.data(), sizeof(int64_t) * plan.n_windows, cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) {
+            close(err);
+            *err = std::string("-C encoder set-up: ") + cudaGetErrorString(ce);
+            return 1;
+        }
+    }
+    return 0;
+}
+
+int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, const SiteCall* d_calls,
+                            const SiteCounts* d_counts, const int32_t* d_host_src, const int32_t* h_host_src,
+                            const uint8_t* h_codes, cudaStream_t stream, ColumnsGpuStats* st, std::string* err) {
+    if (!fb_[0] || !plan_ || w0 != next_window_ || w1 < w0 || w1 > plan_->n_windows) {
+        *err = "-C windows out of order";
         return 1;
     }
-    std::vector<uint64_t> h_len((size_t)(5 * batch));
-    std::vector<int> h_fb((size_t)batch);
-    std::vector<std::string> blocks(5);
-    std::vector<std::vector<char>> host_buf(5);
+    const WindowPlan& plan = *plan_;
+    int rc = 0;
+    cudaError_t ce = cudaSuccess;
+    std::vector<uint64_t> h_len((size_t)(5 * batch_cap_));
+    std::vector<int> h_fb((size_t)batch_cap_);
     HostDictCodec dict;
-    for (int64_t w0 = 0; w0 < nwin && rc == 0; w0 += batch) {
-        const int64_t nb = std::min(batch, nwin - w0);
+    for (int64_t b0 = w0; b0 < w1 && rc == 0; b0 += batch_cap_) {
+        const int64_t nb = std::min(batch_cap_, w1 - b0);
         EncArgs e;
-        e.w0 = w0;
-        e.call_len = d_len_tab;
-        e.host_src = d_hs;
+        e.w0 = b0;
+        e.call_len = d_len_tab_;
+        e.host_src = d_host_src;
         e.codes = d_codes;
         e.calls = d_calls;
         e.counts = d_counts;
-        e.bits = d_bits;
+        e.bits = d_bits_;
         for (int f = 0; f < 5; ++f) {
-            e.out[f] = d_out[f];
+            e.out[f] = d_out_[f];
             e.cap[f] = kCapHost[f];
         }
-        e.len = d_len;
-        e.fallback = d_fb;
-        e.s_val = d_sval;
-        e.s_aux = d_saux;
-        e.s_dict = d_sdict;
+        e.len = d_len_;
+        e.fallback = d_fb_;
+        e.s_val = d_sval_;
+        e.s_aux = d_saux_;
+        e.s_dict = d_sdict_;
         encode_windows_kernel<<<(unsigned)nb, kEncThreads, kEncSmem, stream>>>(e);
         ce = cudaGetLastError();
-        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_len.data(), d_len, sizeof(uint64_t) * 5 * nb, cudaMemcpyDeviceToHost, stream);
-        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_fb.data(), d_fb, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_len.data(), d_len_, sizeof(uint64_t) * 5 * nb, cudaMemcpyDeviceToHost, stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_fb.data(), d_fb_, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
         if (ce != cudaSuccess) {
             *err = std::string("-C encoder: ") + cudaGetErrorString(ce);
@@ -861,14 +886,15 @@ int write_columns_gpu(const WindowPlan& plan, const uint8_t* d_codes, const Site
         for (int64_t b = 0; b < nb; ++b)
             if (!h_fb[(size_t)b])
                 for (int f = 0; f < 5; ++f) tot[f] += h_len[(size_t)(5 * b + f)];
-        for (int f = 0; f < 5; ++f) host_buf[f].resize(tot[f]);
+        for (int f = 0; f < 5; ++f)
+            if (host_buf_[f].size() < tot[f]) host_buf_[f].resize(tot[f]);
         size_t off[5] = {};
         for (int64_t b = 0; b < nb && ce == cudaSuccess; ++b) {
             if (h_fb[(size_t)b]) continue;
             for (int f = 0; f < 5 && ce == cudaSuccess; ++f) {
                 const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
                 if (bytes)
-                    ce = cudaMemcpyAsync(host_buf[f].data() + off[f], d_out[f] + (size_t)b * kCapHost[f], bytes,
+                    ce = cudaMemcpyAsync(host_buf_[f].data() + off[f], d_out_[f] + (size_t)b * kCapHost[f], bytes,
                                          cudaMemcpyDeviceToHost, stream);
                 off[f] += bytes;
             }
@@ -885,18 +911,18 @@ int write_columns_gpu(const WindowPlan& plan, const uint8_t* d_codes, const Site
             if (!h_fb[(size_t)b]) {
                 for (int f = 0; f < 5; ++f) {
                     const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
-                    if (bytes && fwrite(host_buf[f].data() + wo[f], 1, bytes, fb[f]) != bytes) rc = 1;
+                    if (bytes && fwrite(host_buf_[f].data() + wo[f], 1, bytes, fb_[f]) != bytes) rc = 1;
                     wo[f] += bytes;
                 }
                 continue;
             }
             if (st) ++st->host_windows;
-            const int64_t w = w0 + b;
+            const int64_t w = b0 + b;
             const int64_t len = plan.call_len[(size_t)w];
             std::vector<SiteCall> calls((size_t)len);
             std::vector<SiteCounts> counts;
             ce = cudaMemcpy(calls.data(), d_calls + w * (int64_t)kWin, sizeof(SiteCall) * len, cudaMemcpyDeviceToHost);
-            const int32_t src = plan.host_src[(size_t)w];
+            const int32_t src = h_host_src[w];
             if (ce == cudaSuccess && src >= 0 && src != w && d_counts) {
                 counts.resize((size_t)len);
                 ce = cudaMemcpy(counts.data(), d_counts + (int64_t)src * kWin, sizeof(SiteCounts) * len,
@@ -914,14 +940,44 @@ int write_columns_gpu(const WindowPlan& plan, const uint8_t* d_codes, const Site
                 break;
             }
             for (int f = 0; f < 5; ++f)
-                if (!parts[f].empty() && fwrite(parts[f].data(), 1, parts[f].size(), fb[f]) != parts[f].size()) rc = 1;
+                if (!parts[f].empty() && fwrite(parts[f].data(), 1, parts[f].size(), fb_[f]) != parts[f].size()) rc = 1;
         }
         if (rc && err->empty()) *err = "write failed";
         if (st) st->windows += nb;
     }
-    (void)threads;
-    free_dev();
-    return finish();
+    next_window_ = w1;
+    return rc;
+}
+
+size_t ColumnsGpuWriter::device_bytes() const {
+    size_t n = 0;
+    for (int f = 0; f < 5; ++f) n += kCapHost[f] * (size_t)batch_cap_;
+    return n + (size_t)batch_cap_ * (kWin * 20 + 44) + (kWin + 2) + (size_t)len_tab_windows_ * 8;
+}
+
+int ColumnsGpuWriter::close(std::string* err) {
+    int rc = 0;
+    for (FILE*& f : fb_)
+        if (f) {
+            if (fclose(f) != 0 && rc == 0) {
+                *err = "write failed";
+                rc = 1;
+            }
+            f = nullptr;
+        }
+    if (f12_) {
+        if (fclose(f12_) != 0 && rc == 0) {
+            *err = "write failed";
+            rc = 1;
+        }
+        f12_ = nullptr;
+    }
+    if (rc == 0 && plan_ && next_window_ != plan_->n_windows) {
+        *err = "-C files closed before their last window";
+        rc = 1;
+    }
+    plan_ = nullptr;
+    return rc;
 }
 
 }  // namespace gsnp

@@ -58,6 +58,16 @@ int64_t bin_global_words(int kind, int bin, int64_t count);
 
 /* ---- device helpers ---- */
 
+/* p - first as an address, for arrays that hold elements [first, ...) of an
+ * array the kernels index from 0: only indices >= first are used with it */
+template <class T>
+T* based(T* p, int64_t first) {
+    return reinterpret_cast<T*>(reinterpret_cast<uintptr_t>(p) - (uintptr_t)(first * (int64_t)sizeof(T)));
+}
+
+struct StreamRing;
+void ring_free(StreamRing* g);
+
 /* a site decided by the deferred pass and its call */
 struct DeferredCall {
     int64_t site;
@@ -441,10 +451,34 @@ struct gsnp_context {
     bool deferred_at_end = false;   /* the last pass ran its deferred sites after its last segment */
     DeferredCall* d_patch = nullptr;   /* their final calls, for the host copy of the calls */
     int64_t patch_cap = 0;
+    /* The chunk of windows a streamed call is calling (gsnp_call_streamed):
+     * when on, make_args points the kernels at the chunk's ring slot, whose
+     * arrays hold reads [R0, R1), tiles [T0, T1) and sites [S0, S1), and at
+     * the chunk's window tables and count / likelihood stores, which hold
+     * windows [w0 - 1, w1) (entry w0 - 1 carries an earlier window). */
+    struct ChunkView {
+        bool on = false;
+        int64_t w0 = 0, S0 = 0, T0 = 0, T1 = 0, R0 = 0, R1 = 0;
+        int64_t tiles_need = 0;     /* tiles of the largest chunk */
+        int32_t* pos = nullptr;
+        int32_t* lenhit = nullptr;
+        uint8_t* strand = nullptr;
+        uint16_t* bq = nullptr;
+        SiteCall* out = nullptr;
+        SiteCounts* counts = nullptr;
+        double* lik_keep = nullptr;
+        uint8_t* win_flags = nullptr;
+        int32_t* win_lik_src = nullptr;
+        int32_t* win_host_src = nullptr;
+    } view;
+    StreamRing* ring = nullptr;
+    int64_t stream_windows = 16;    /* windows per chunk of a streamed call */
+    bool streamed = false;          /* the last call was streamed: no resident calls */
     /* -C files: windows encoded on the device (columns_gpu.cu), or on the
      * host threads (columns.cpp) */
     bool columns_gpu = true;
     int64_t columns_host_windows = 0;
+    std::unique_ptr<ColumnsGpuWriter> colw;   /* kept, with its device buffers, from one use to the next */
     int bin_limit[kNumBins] = {32, 40, 48, 64, 96, 128, 256};
     int bin_carveout[2][kNumBins] = {{0, 0, 0, 0, 0, 0, 0}, {0, 72, 0, 0, 0, 0, 0}};
     int bin_grid[2][kNumBins] = {};
@@ -693,6 +727,8 @@ CallArgs make_args(gsnp_context* c) {
     a.win_flags = c->d_win_flags;
     a.win_lik_src = c->d_win_lik_src;
     a.n_tiles = (c->chr_len + kTile - 1) / kTile;
+    a.tile_lo = 0;
+    a.bin_stride = c->tiles_cap;
     a.warp_rng = c->d_warp_rng;
     a.tile_rng = c->d_tile_rng;
     a.empty_calls = c->d_empty_calls;
@@ -707,6 +743,29 @@ CallArgs make_args(gsnp_context* c) {
     a.lik_keep = c->d_lik_keep;
     a.stats = c->d_stats;
     a.error = c->d_error;
+    a.read_lo = 0;
+    if (c->view.on) {
+        /* a streamed chunk: every array indexed by read, tile, site or window
+         * is its ring slot's, based so that the kernels' indices stay
+         * absolute */
+        const gsnp_context::ChunkView& v = c->view;
+        const int64_t L = c->params.read_length;
+        a.pos = based(v.pos, v.R0);
+        a.lenhit = based(v.lenhit, v.R0);
+        a.strand = based(v.strand, v.R0);
+        a.bq = based(v.bq, v.R0 * L);
+        a.read_lo = v.R0;
+        a.n_reads = v.R1;
+        a.n_tiles = v.T1;
+        a.tile_lo = v.T0;
+        a.warp_rng = based(c->d_warp_rng, 2 * v.T0);
+        a.tile_rng = based(c->d_tile_rng, 2 * v.T0);
+        a.out = based(v.out, v.S0);
+        a.counts = v.counts ? based(v.counts, (v.w0 - 1) * kWin) : nullptr;
+        a.lik_keep = v.lik_keep ? based(v.lik_keep, (v.w0 - 1) * kWin * 10) : nullptr;
+        a.win_flags = based(v.win_flags, v.w0 - 1);
+        a.win_lik_src = based(v.win_lik_src, v.w0 - 1);
+    }
     return a;
 }
 
@@ -727,7 +786,8 @@ struct Segment {
 /* Allocations and one-time work of a calling pass, done before any of its
  * work is queued (and outside a graph capture). */
 int prepare_calling(gsnp_context* c) {
-    const int64_t n_tiles = (c->chr_len + kTile - 1) / kTile;
+    /* the tile arrays hold the chromosome's tiles, or a streamed chunk's */
+    const int64_t n_tiles = c->view.on ? c->view.tiles_need : (c->chr_len + kTile - 1) / kTile;
     {
         const int rc = ensure_map(c, kMapWindows);
         if (rc != GSNP_OK) return rc;
@@ -763,7 +823,7 @@ int prepare_calling(gsnp_context* c) {
     }
     if (c->dsite_cap == 0) {
         /* deferred sites: about 0.1% of a 30x genome; grown on demand */
-        c->dsite_cap = std::max<int64_t>(1 << 16, c->chr_len / 256);
+        c->dsite_cap = std::max<int64_t>(1 << 16, (c->view.on ? n_tiles * kTile : c->chr_len) / 256);
         c->dpool_cap = c->dsite_cap * 48;
         CK(dev_alloc(&c->d_dsites, (size_t)c->dsite_cap), "cudaMalloc deferred");
         CK(dev_alloc(&c->d_dpool, (size_t)c->dpool_cap), "cudaMalloc deferred");
@@ -910,7 +970,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
                 const int nb = c->h_bin_count[base + b];
                 const int k = begin(kind, bin_slots(b), nb);
                 const BinLaunch bl{nb, nullptr, 0, c->bin_carveout[kind == kKindFast][b]};
-                CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, bl, c->stream),
+                CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * c->tiles_cap, bl, c->stream),
                    "calling kernel");
                 end(k);
             }
@@ -925,7 +985,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             const int nb = c->h_bin_count[base + b];
             const int k = begin_on(kind, bin_slots(b), nb, st);
             const BinLaunch bl{nb, nullptr, 0, c->bin_carveout[kind == kKindFast][b]};
-            CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * n_tiles, bl, st),
+            CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * c->tiles_cap, bl, st),
                "calling kernel");
             end_on(k, st);
         }
@@ -1128,7 +1188,7 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
                 const BinLaunch bl{0, c->d_bin_count + ki * kNumBins + b, c->bin_grid[ki][b], c->bin_carveout[ki][b],
                                    c->d_bin_count + (2 + ki) * kNumBins + b};
                 const int kb = begin(kind, kSlotsOf(b), 0);
-                CK(launch_bin(a, kind, b, c->d_bin_tiles + (int64_t)(ki * kNumBins + b) * n_tiles, bl, c->stream),
+                CK(launch_bin(a, kind, b, c->d_bin_tiles + (int64_t)(ki * kNumBins + b) * c->tiles_cap, bl, c->stream),
                    "calling kernel");
                 end(kb);
             }
@@ -1261,6 +1321,23 @@ int segment_count(int64_t n_dep, int64_t n_windows) {
  *                     segment's reads (after the upload pieces that hold
  *                     them) and the calling of this one;
  *   copy stream down: each segment's calls once they are final. */
+/* the copy streams and events of a call, made on first use */
+int ensure_call_streams(gsnp_context* c) {
+    if (c->up_stream) return GSNP_OK;
+    CK(cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (int i = 0; i + 1 < c->n_up; ++i)
+        CK(cudaStreamCreateWithFlags(&c->up_extra[i], cudaStreamNonBlocking), "cudaStreamCreate");
+    CK(cudaStreamCreateWithFlags(&c->down_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    CK(cudaStreamCreateWithFlags(&c->gather_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    CK(cudaEventCreateWithFlags(&c->ev_index, cudaEventDisableTiming), "cudaEventCreate");
+    CK(cudaEventCreateWithFlags(&c->ev_small, cudaEventDisableTiming), "cudaEventCreate");
+    CK(cudaEventCreateWithFlags(&c->ev_seg, cudaEventDisableTiming), "cudaEventCreate");
+    for (int i = 0; i < gsnp_context::kUploadChunks; ++i)
+        CK(cudaEventCreateWithFlags(&c->ev_chunk[i], cudaEventDisableTiming), "cudaEventCreate");
+    CK(dev_alloc(&c->d_gerror, 1), "cudaMalloc");
+    return GSNP_OK;
+}
+
 int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     if (!c || !r || r->n < 0 || r->pitch < 0 ||
         (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
@@ -1270,18 +1347,15 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     PhaseTimer timer("gsnp_call_chromosome");
     const int L = c->params.read_length;
     const int64_t n = r->n;
-    if (!c->up_stream) {
-        CK(cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        for (int i = 0; i + 1 < c->n_up; ++i)
-            CK(cudaStreamCreateWithFlags(&c->up_extra[i], cudaStreamNonBlocking), "cudaStreamCreate");
-        CK(cudaStreamCreateWithFlags(&c->down_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        CK(cudaStreamCreateWithFlags(&c->gather_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        CK(cudaEventCreateWithFlags(&c->ev_index, cudaEventDisableTiming), "cudaEventCreate");
-        CK(cudaEventCreateWithFlags(&c->ev_small, cudaEventDisableTiming), "cudaEventCreate");
-        CK(cudaEventCreateWithFlags(&c->ev_seg, cudaEventDisableTiming), "cudaEventCreate");
-        for (int i = 0; i < gsnp_context::kUploadChunks; ++i)
-            CK(cudaEventCreateWithFlags(&c->ev_chunk[i], cudaEventDisableTiming), "cudaEventCreate");
-        CK(dev_alloc(&c->d_gerror, 1), "cudaMalloc");
+    {
+        const int rc = ensure_call_streams(c);
+        if (rc != GSNP_OK) return rc;
+    }
+    c->streamed = false;
+    if (!c->d_out || c->out_sites < c->chr_len) {
+        /* the resident calls of the chromosome (a streamed call keeps none) */
+        CK(dev_alloc(&c->d_out, (size_t)c->chr_len), "cudaMalloc calls");
+        c->out_sites = c->chr_len;
     }
     /* 1. uploads, on their own stream */
     const size_t raw = (size_t)n * r->pitch;
@@ -1540,6 +1614,7 @@ int gsnp_set_option(gsnp_context* c, const char* name, int64_t value) {
     else if (n == "persistent_mode") c->stream_mode = clamp(value, 0, 2);
     else if (n == "persistent_carveout") c->stream_carveout = clamp(value, 0, 100);
     else if (n == "device_driven") c->device_driven = value != 0;
+    else if (n == "stream_windows") c->stream_windows = clamp(value, 1, 1 << 20);
     else if (n == "graphs") c->use_graphs = value != 0;
     else if (n == "columns_gpu") c->columns_gpu = value != 0;
     else if (n == "upload_streams") c->n_up = c->up_stream ? c->n_up : clamp(value, 1, gsnp_context::kMaxUpStreams);
@@ -1626,6 +1701,9 @@ void gsnp_context_destroy(gsnp_context* c) {
         if (u) cudaStreamSynchronize(u);
     if (c->down_stream) cudaStreamSynchronize(c->down_stream);
     free_all(c);
+    ring_free(c->ring);
+    c->ring = nullptr;
+    c->colw.reset();
     if (c->h_text) cudaFreeHost(c->h_text);
     for (int i = 0; i < 2 * gsnp_context::kMaxLaunches; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -1734,8 +1812,10 @@ int gsnp_load_reference(gsnp_context* c, const uint8_t* codes, int64_t length, c
     c->n_snp = n_snp;
     CK(dev_alloc(&c->d_snp, (size_t)std::max<int64_t>(n_snp, 1)), "cudaMalloc dbsnp");
     if (n_snp > 0) CK(cudaMemcpy(c->d_snp, snp, sizeof(gsnp_snp) * n_snp, cudaMemcpyHostToDevice), "upload dbsnp");
-    CK(dev_alloc(&c->d_out, (size_t)length), "cudaMalloc calls");
-    c->out_sites = length;
+    /* the resident calls are allocated by the first resident call */
+    if (c->d_out) cudaFree(c->d_out);
+    c->d_out = nullptr;
+    c->out_sites = 0;
     c->snp_lp_ready = false;
     c->called = false;
     return GSNP_OK;
@@ -2145,12 +2225,14 @@ constexpr int64_t kEmitChunk = 16 * (int64_t)kWin;   /* sites per emission step 
 /* Emit the cns text chunk by chunk; sink(text, bytes) receives each chunk's
  * text in host memory (pinned).  With sink == nullptr only the total size is
  * computed. */
-template <class Sink>
-int emit_cns(gsnp_context* c, const char* chr_name, uint64_t* total, Sink&& sink, bool write) {
-    const size_t chr_n = strlen(chr_name);
-    if (chr_n > 255) return fail(c, GSNP_ERR_ARG, "chromosome name longer than 255 bytes");
+/* The chromosome name on the device and the text scratch; clears the error
+ * flag that emit_finish reads. */
+int emit_prepare(gsnp_context* c, const char* chr_name, int* chr_n) {
+    const size_t n = strlen(chr_name);
+    if (n > 255) return fail(c, GSNP_ERR_ARG, "chromosome name longer than 255 bytes");
+    *chr_n = (int)n;
     if (!c->d_chr) CK(cudaMalloc((void**)&c->d_chr, 256), "cudaMalloc");
-    CK(cudaMemcpyAsync(c->d_chr, chr_name, chr_n, cudaMemcpyHostToDevice, c->stream), "upload");
+    CK(cudaMemcpyAsync(c->d_chr, chr_name, n, cudaMemcpyHostToDevice, c->stream), "upload");
     const size_t need = emit_scratch_bytes(std::min<int64_t>(kEmitChunk, c->chr_len));
     if (need > c->emit_bytes) {
         if (c->d_emit) cudaFree(c->d_emit);
@@ -2160,18 +2242,37 @@ int emit_cns(gsnp_context* c, const char* chr_name, uint64_t* total, Sink&& sink
         c->emit_bytes = need;
     }
     CK(cudaMemsetAsync(c->d_error, 0, sizeof(int), c->stream), "memset");
+    return GSNP_OK;
+}
+
+/* a cns value outside the formatter's range in any row since emit_prepare */
+int emit_finish(gsnp_context* c) {
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
+    CK(cudaStreamSynchronize(c->stream), "cns text");
+    if (err) return fail(c, GSNP_ERR_STATE, "a cns value is outside the text formatter's range");
+    return GSNP_OK;
+}
+
+/* The cns text of sites [s_begin, s_end), from calls, counts (null: none
+ * kept) and host_src indexed by absolute site and window, to sink in pieces
+ * of kEmitChunk rows; *total gets the byte count (with write false only the
+ * count is made). */
+template <class Sink>
+int emit_sites(gsnp_context* c, int chr_n, int64_t s_begin, int64_t s_end, const SiteCall* calls,
+               const SiteCounts* counts, const int32_t* host_src, uint64_t* total, Sink&& sink, bool write) {
     *total = 0;
-    for (int64_t s0 = 0; s0 < c->chr_len; s0 += kEmitChunk) {
+    for (int64_t s0 = s_begin; s0 < s_end; s0 += kEmitChunk) {
         EmitArgs e;
         memset(&e, 0, sizeof(e));
-        e.calls = c->d_out;
-        e.counts = c->have_counts ? c->d_counts : nullptr;
+        e.calls = calls;
+        e.counts = counts;
         e.codes = c->d_codes;
-        e.host_src = c->d_win_host_src;
+        e.host_src = host_src;
         e.chr = c->d_chr;
-        e.chr_n = (int)chr_n;
+        e.chr_n = chr_n;
         e.site0 = s0;
-        e.n = std::min<int64_t>(kEmitChunk, c->chr_len - s0);
+        e.n = std::min<int64_t>(kEmitChunk, s_end - s0);
         e.error = c->d_error;
         uint64_t bytes = 0;
         CK(emit_lengths(e, c->d_emit, c->stream, &bytes), "cns text lengths");
@@ -2198,10 +2299,515 @@ int emit_cns(gsnp_context* c, const char* chr_name, uint64_t* total, Sink&& sink
         c->d2h_bytes += bytes;
         if (!sink(c->h_text, bytes)) return fail(c, GSNP_ERR_INPUT, "write failed");
     }
-    int err = 0;
-    CK(cudaMemcpyAsync(&err, c->d_error, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "error flag");
-    CK(cudaStreamSynchronize(c->stream), "cns text");
-    if (err) return fail(c, GSNP_ERR_STATE, "a cns value is outside the text formatter's range");
+    return GSNP_OK;
+}
+
+/* the cns text of the resident calls of the whole chromosome */
+template <class Sink>
+int emit_cns(gsnp_context* c, const char* chr_name, uint64_t* total, Sink&& sink, bool write) {
+    int chr_n = 0;
+    int rc = emit_prepare(c, chr_name, &chr_n);
+    if (rc != GSNP_OK) return rc;
+    rc = emit_sites(c, chr_n, 0, c->chr_len, c->d_out, c->have_counts ? c->d_counts : nullptr, c->d_win_host_src,
+                    total, sink, write);
+    if (rc != GSNP_OK) return rc;
+    return emit_finish(c);
+}
+
+/* ------------------------------------------------------------------------ */
+/* streamed calls: bounded device memory                                     */
+/* ------------------------------------------------------------------------ */
+
+/* One chunk of a streamed call: windows [w0, w1), their sites and tiles, the
+ * deposited reads [R0, R1) its tiles reach (those starting in
+ * [S0 - L + 1, S1)), the alignments [raw_lo, raw_hi) that hold them, and the
+ * start of deposited read R1 (kNoRead past the last). */
+struct Chunk {
+    int64_t w0, w1, S0, S1, T0, T1, R0, R1, raw_lo, raw_hi, next_pos;
+};
+
+/* The chunks of windows_per_chunk windows each, from the window replay.  The
+ * deposited reads are the passing alignments in file order (all but the last
+ * when the replay dropped it); a chunk's reads start with the passing
+ * alignments before its first window that still reach it. */
+std::vector<Chunk> plan_chunks(const WindowPlan& P, const ReadView& v, int64_t chr_len, int L,
+                               int64_t windows_per_chunk) {
+    const int64_t n_tiles = (chr_len + kTile - 1) / kTile;
+    const int64_t nw = P.n_windows;
+    /* per window boundary w: passing alignments of the runs before it, and
+     * the first alignment of the first run at or past it */
+    std::vector<int64_t> dep_at((size_t)nw + 1, 0), raw_at((size_t)nw + 1, v.n), pos_at((size_t)nw + 1, kNoRead);
+    {
+        size_t k = 0;
+        int64_t dep = 0;
+        for (int64_t w = 0; w <= nw; ++w) {
+            while (k < P.runs.size() && P.runs[k].window < w) dep += P.runs[k++].count;
+            dep_at[(size_t)w] = dep;
+            if (k < P.runs.size()) {
+                raw_at[(size_t)w] = P.runs[k].first;
+                pos_at[(size_t)w] = v.pos[P.runs[k].first];
+            }
+        }
+    }
+    auto passing = [&](int64_t i) { return v.pos[i] >= 0 && (int64_t)v.pos[i] + v.len[i] < chr_len; };
+    std::vector<Chunk> out;
+    for (int64_t w0 = 0; w0 < nw; w0 += windows_per_chunk) {
+        const int64_t w1 = std::min(nw, w0 + windows_per_chunk);
+        Chunk ch;
+        ch.w0 = w0;
+        ch.w1 = w1;
+        ch.S0 = w0 * kWin;
+        ch.S1 = std::min(chr_len, w1 * kWin);
+        ch.T0 = ch.S0 / kTile;
+        ch.T1 = w1 == nw ? n_tiles : std::min(n_tiles, w1 * (int64_t)(kWin / kTile));
+        ch.R1 = std::min(dep_at[(size_t)w1], P.n_deposited);
+        ch.R0 = std::min(dep_at[(size_t)w0], P.n_deposited);
+        ch.raw_lo = raw_at[(size_t)w0];
+        /* the passing alignments before the chunk that reach its first site */
+        int64_t pidx = dep_at[(size_t)w0];
+        for (int64_t i = raw_at[(size_t)w0] - 1; i >= 0; --i) {
+            if (!passing(i)) continue;
+            --pidx;
+            if ((int64_t)v.pos[i] < ch.S0 - L + 1) break;
+            if (pidx < P.n_deposited) {
+                ch.R0 = pidx;
+                ch.raw_lo = i;
+            }
+        }
+        if (ch.R0 > ch.R1) ch.R0 = ch.R1;
+        ch.raw_hi = std::max(ch.raw_lo, raw_at[(size_t)w1]);
+        ch.next_pos = ch.R1 < P.n_deposited ? (int64_t)pos_at[(size_t)w1] : kNoRead;
+        out.push_back(ch);
+    }
+    return out;
+}
+
+}  // namespace
+
+/* Device buffers of a streamed call.  Two slots, each with one chunk's
+ * alignments as uploaded, their deposited index, the deposited reads packed,
+ * the chunk's calls and window tables; one store of counts and one of
+ * likelihoods for the chunk being called (its windows and the carried
+ * window), and the carried window's counts and likelihood between chunks.
+ * Sized by the largest chunk, not by the chromosome. */
+struct StreamRing {
+    struct Slot {
+        int32_t* raw_pos = nullptr;
+        int32_t* raw_len = nullptr;
+        int32_t* raw_hit = nullptr;
+        uint8_t* raw_strand = nullptr;
+        uint8_t* raw_seq = nullptr;
+        uint8_t* raw_qual = nullptr;
+        int64_t* idx = nullptr;
+        int64_t* dep_off = nullptr;
+        int32_t* pos = nullptr;
+        int32_t* lenhit = nullptr;
+        int32_t* len = nullptr;
+        uint8_t* strand = nullptr;
+        uint16_t* bq = nullptr;
+        SiteCall* out = nullptr;
+        uint8_t* win_flags = nullptr;
+        int32_t* win_lik_src = nullptr;
+        int32_t* win_host_src = nullptr;
+        /* the window tables staged on the host (pinned) */
+        uint8_t* h_tab = nullptr;
+        cudaEvent_t uploaded = nullptr, free = nullptr;
+    } slot[2];
+    int64_t raw_rows = 0, raw_bytes = 0, dep_rows = 0, sites = 0, windows = 0, dep_chunks = 0;
+    int L = 0;
+    SiteCounts* counts = nullptr;
+    SiteCounts* carry_counts = nullptr;
+    double* lik = nullptr;
+    double* carry_lik = nullptr;
+    size_t bytes = 0;   /* device bytes held */
+};
+
+void ring_free(StreamRing* g) {
+    if (!g) return;
+    for (auto& s : g->slot) {
+        void* p[] = {s.raw_pos, s.raw_len, s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, s.idx, s.dep_off,
+                     s.pos, s.lenhit, s.len, s.strand, s.bq, s.out, s.win_flags, s.win_lik_src, s.win_host_src};
+        for (void* q : p)
+            if (q) cudaFree(q);
+        if (s.h_tab) cudaFreeHost(s.h_tab);
+        if (s.uploaded) cudaEventDestroy(s.uploaded);
+        if (s.free) cudaEventDestroy(s.free);
+        s = StreamRing::Slot();
+    }
+    void* p[] = {g->counts, g->carry_counts, g->lik, g->carry_lik};
+    for (void* q : p)
+        if (q) cudaFree(q);
+    delete g;
+}
+
+namespace {
+
+/* bytes of one window-table staging area of w windows */
+size_t tab_bytes(int64_t w) { return (size_t)(((w + 15) & ~(int64_t)15) + 8 * w); }
+
+/* the ring's buffers for chunks of up to the given sizes (grown, never shrunk) */
+int ring_ensure(gsnp_context* c, StreamRing* g, int64_t raw_rows, int64_t raw_bytes, int64_t dep_rows,
+                int64_t sites, int64_t windows, bool counts, bool lik) {
+    const int L = c->params.read_length;
+    const int64_t dep_chunks = (raw_rows + kDepChunk - 1) / kDepChunk;
+    if (raw_rows > g->raw_rows || raw_bytes > g->raw_bytes || dep_rows > g->dep_rows || sites > g->sites ||
+        windows > g->windows || L != g->L) {
+        const int64_t rr = std::max(raw_rows, g->raw_rows), rb = std::max(raw_bytes, g->raw_bytes);
+        const int64_t dr = std::max(dep_rows, g->dep_rows), ns = std::max(sites, g->sites);
+        const int64_t nw = std::max(windows, g->windows), dc = std::max<int64_t>(1, (rr + kDepChunk - 1) / kDepChunk);
+        for (auto& s : g->slot) {
+            void* p[] = {s.raw_pos, s.raw_len, s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, s.idx, s.dep_off,
+                         s.pos, s.lenhit, s.len, s.strand, s.bq, s.out, s.win_flags, s.win_lik_src, s.win_host_src};
+            for (void* q : p)
+                if (q) cudaFree(q);
+            if (s.h_tab) cudaFreeHost(s.h_tab);
+            const cudaEvent_t up = s.uploaded, fr = s.free;
+            s = StreamRing::Slot();
+            s.uploaded = up;
+            s.free = fr;
+            const int64_t r1 = std::max<int64_t>(rr, 1), d1 = std::max<int64_t>(dr, 1);
+            CK(dev_alloc(&s.raw_pos, (size_t)r1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.raw_len, (size_t)r1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.raw_hit, (size_t)r1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.raw_strand, (size_t)r1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.raw_seq, (size_t)std::max<int64_t>(rb, 1)), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.raw_qual, (size_t)std::max<int64_t>(rb, 1)), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.idx, (size_t)r1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.dep_off, (size_t)dc), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.pos, (size_t)d1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.lenhit, (size_t)d1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.len, (size_t)d1), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.strand, (size_t)d1), "cudaMalloc stream ring");
+            /* slack as for the resident rows (the persistent kernel's staging copies) */
+            CK(dev_alloc(&s.bq, (size_t)d1 * L + 64), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.out, (size_t)std::max<int64_t>(ns, 1)), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.win_flags, (size_t)nw), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.win_lik_src, (size_t)nw), "cudaMalloc stream ring");
+            CK(dev_alloc(&s.win_host_src, (size_t)nw), "cudaMalloc stream ring");
+            CK(cudaMallocHost((void**)&s.h_tab, tab_bytes(nw)), "cudaMallocHost stream ring");
+        }
+        g->raw_rows = rr;
+        g->raw_bytes = rb;
+        g->dep_rows = dr;
+        g->sites = ns;
+        g->windows = nw;
+        g->dep_chunks = dc;
+        g->L = L;
+        if (g->counts) {
+            cudaFree(g->counts);
+            g->counts = nullptr;
+        }
+        if (g->lik) {
+            cudaFree(g->lik);
+            g->lik = nullptr;
+        }
+    }
+    (void)dep_chunks;
+    for (auto& s : g->slot) {
+        if (!s.uploaded) CK(cudaEventCreateWithFlags(&s.uploaded, cudaEventDisableTiming), "cudaEventCreate");
+        if (!s.free) CK(cudaEventCreateWithFlags(&s.free, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (counts && !g->counts) {
+        CK(dev_alloc(&g->counts, (size_t)g->windows * kWin), "cudaMalloc stream counts");
+        if (!g->carry_counts) CK(dev_alloc(&g->carry_counts, (size_t)kWin), "cudaMalloc stream counts");
+    }
+    if (lik && !g->lik) {
+        CK(dev_alloc(&g->lik, (size_t)g->windows * kWin * 10), "cudaMalloc stream likelihood");
+        if (!g->carry_lik) CK(dev_alloc(&g->carry_lik, (size_t)kWin * 10), "cudaMalloc stream likelihood");
+    }
+    const int64_t rr = g->raw_rows, dr = g->dep_rows;
+    g->bytes = 2 * ((size_t)rr * (4 + 4 + 4 + 1 + 8) + 2 * (size_t)g->raw_bytes + (size_t)g->dep_chunks * 8 +
+                    (size_t)dr * (4 + 4 + 4 + 1 + 2 * (size_t)L) + (size_t)g->sites * sizeof(SiteCall) +
+                    (size_t)g->windows * 9) +
+               (g->counts ? (size_t)(g->windows + 1) * kWin * sizeof(SiteCounts) : 0) +
+               (g->lik ? (size_t)(g->windows + 1) * kWin * 80 : 0);
+    return GSNP_OK;
+}
+
+/* gsnp_call_streamed: the chromosome in chunks of c->stream_windows windows,
+ * with device memory bounded by the largest chunk (StreamRing) instead of the
+ * chromosome.
+ *   copy stream up:    chunk k + 1's alignments into the other ring slot
+ *                      while chunk k is called;
+ *   compute stream:    per chunk its deposited index and packed reads, the
+ *                      calling pass over its tiles (make_args points the
+ *                      kernels at the slot through c->view), then its cns
+ *                      text and -C windows;
+ *   copy stream down:  the chunk's calls into out.
+ * Windows that show an earlier window's counts, or use its likelihood
+ * (gap windows), reach back at most to the last window before their chunk
+ * that had reads; that window is carried from chunk to chunk. */
+int call_streamed(gsnp_context* c, const gsnp_reads* r, const char* chr_name, gsnp_site_call* out,
+                  const char* cns_path, const char* columns_base) {
+    if (!c || !r || r->n < 0 || r->pitch < 0 ||
+        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
+        return fail(c, GSNP_ERR_ARG, "null read arrays");
+    if ((cns_path || columns_base) && !chr_name) return fail(c, GSNP_ERR_ARG, "the outputs need the chromosome name");
+    if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
+    cudaSetDevice(c->device);
+    PhaseTimer timer("gsnp_call_streamed");
+    {
+        const int rc = ensure_call_streams(c);
+        if (rc != GSNP_OK) return rc;
+    }
+    const int L = c->params.read_length;
+    c->called = false;
+    c->streamed = false;
+    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
+    std::string err;
+    {
+        const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, host_threads(), &c->plan, &err);
+        if (rc != 0) return fail(c, rc, err);
+    }
+    const WindowPlan& P = c->plan;
+    const int64_t W = std::max<int64_t>(1, c->stream_windows);
+    const std::vector<Chunk> chunks = plan_chunks(P, v, c->chr_len, L, W);
+    timer.mark("window replay");
+
+    /* the ring's sizes, and the carried window of every chunk */
+    int64_t raw_rows = 0, dep_rows = 0, sites = 0, tiles = 0;
+    bool need_counts = false, need_lik = false;
+    for (int64_t w = 0; w < P.n_windows; ++w) {
+        need_counts |= (P.flags[w] & kWinKeepCounts) != 0;
+        need_lik |= (P.flags[w] & kWinKeepLik) != 0;
+    }
+    const size_t nk = chunks.size();
+    std::vector<int64_t> carry_c(nk, -1), carry_l(nk, -1), save_c(nk, -1), save_l(nk, -1);
+    for (size_t k = 0; k < nk; ++k) {
+        const Chunk& ch = chunks[k];
+        raw_rows = std::max(raw_rows, ch.raw_hi - ch.raw_lo);
+        dep_rows = std::max(dep_rows, ch.R1 - ch.R0);
+        sites = std::max(sites, ch.S1 - ch.S0);
+        tiles = std::max(tiles, ch.T1 - ch.T0);
+        for (int64_t w = ch.w0; w < ch.w1; ++w) {
+            const int32_t hs = P.host_src[w], ls = P.lik_src[w];
+            if (hs >= 0 && hs < ch.w0) {
+                if (carry_c[k] >= 0 && carry_c[k] != hs) return fail(c, GSNP_ERR_STATE, "streamed call: two carried count windows");
+                carry_c[k] = hs;
+            }
+            if ((P.flags[w] & kWinExternalLik) && ls >= 0 && ls < ch.w0) {
+                if (carry_l[k] >= 0 && carry_l[k] != ls) return fail(c, GSNP_ERR_STATE, "streamed call: two carried likelihood windows");
+                carry_l[k] = ls;
+            }
+        }
+    }
+    /* a chunk saves the window a later chunk carries, if it is one of its own;
+     * the carried windows never decrease, so one buffer holds each until its
+     * last use (checked here) */
+    {
+        int64_t held_c = -1, held_l = -1;
+        for (size_t k = 0; k < nk; ++k) {
+            if (carry_c[k] >= 0 && carry_c[k] != held_c) return fail(c, GSNP_ERR_STATE, "streamed call: carried counts lost");
+            if (carry_l[k] >= 0 && carry_l[k] != held_l) return fail(c, GSNP_ERR_STATE, "streamed call: carried likelihood lost");
+            for (size_t j = k + 1; j < nk; ++j) {
+                if (carry_c[j] >= chunks[k].w0 && carry_c[j] < chunks[k].w1) save_c[k] = carry_c[j];
+                if (carry_l[j] >= chunks[k].w0 && carry_l[j] < chunks[k].w1) save_l[k] = carry_l[j];
+            }
+            if (save_c[k] >= 0) held_c = save_c[k];
+            if (save_l[k] >= 0) held_l = save_l[k];
+        }
+    }
+    if (!c->ring) c->ring = new StreamRing();
+    StreamRing* g = c->ring;
+    {
+        const int rc = ring_ensure(c, g, raw_rows, raw_rows * r->pitch, dep_rows, sites, W + 1, need_counts, need_lik);
+        if (rc != GSNP_OK) return rc;
+    }
+    c->view = gsnp_context::ChunkView();
+    c->view.tiles_need = std::max<int64_t>(tiles, 1);
+    timer.mark("ring");
+
+    /* outputs */
+    FILE* cns = nullptr;
+    int chr_n = 0;
+    if (cns_path) {
+        cns = fopen(cns_path, "wb");
+        if (!cns) return fail(c, GSNP_ERR_INPUT, std::string("cannot create ") + cns_path);
+        const int rc = emit_prepare(c, chr_name, &chr_n);
+        if (rc != GSNP_OK) {
+            fclose(cns);
+            return rc;
+        }
+    }
+    if (columns_base) {
+        if (!c->colw) c->colw.reset(new ColumnsGpuWriter());
+        if (!c->sms) CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
+        if (c->colw->open(P, chr_name, columns_base, std::min<int64_t>(W, c->sms), &err) != 0) {
+            if (cns) fclose(cns);
+            return fail(c, GSNP_ERR_INPUT, err);
+        }
+    }
+    int rc = GSNP_OK;
+    auto close_outputs = [&]() {
+        std::string e2;
+        if (cns && fclose(cns) != 0 && rc == GSNP_OK) rc = fail(c, GSNP_ERR_INPUT, "write failed");
+        cns = nullptr;
+        if (columns_base && c->colw->close(&e2) != 0 && rc == GSNP_OK) rc = fail(c, GSNP_ERR_INPUT, e2);
+    };
+    auto drain = [&]() {
+        cudaStreamSynchronize(c->up_stream);
+        cudaStreamSynchronize(c->stream);
+        cudaStreamSynchronize(c->down_stream);
+        c->view.on = false;
+    };
+
+    CK(cudaMemsetAsync(c->d_gerror, 0, sizeof(int), c->stream), "memset");
+    c->h2d_bytes = (uint64_t)nk * tab_bytes(W + 1);
+    c->d2h_bytes = 0;
+    /* chunk k's alignments into slot k & 1, once that slot's last chunk is done */
+    auto upload = [&](size_t k) -> int {
+        const Chunk& ch = chunks[k];
+        StreamRing::Slot& s = g->slot[k & 1];
+        CK(cudaStreamWaitEvent(c->up_stream, s.free, 0), "wait");
+        const int64_t n = ch.raw_hi - ch.raw_lo, b = ch.raw_lo;
+        if (n > 0) {
+            CK(cudaMemcpyAsync(s.raw_pos, r->pos + b, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
+            CK(cudaMemcpyAsync(s.raw_len, r->len + b, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
+            CK(cudaMemcpyAsync(s.raw_hit, r->hit + b, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
+            CK(cudaMemcpyAsync(s.raw_strand, r->strand + b, n, cudaMemcpyHostToDevice, c->up_stream), "upload");
+            const size_t off = (size_t)b * r->pitch, bytes = (size_t)n * r->pitch;
+            CK(cudaMemcpyAsync(s.raw_seq, r->seq + off, bytes, cudaMemcpyHostToDevice, c->up_stream), "upload seq");
+            CK(cudaMemcpyAsync(s.raw_qual, r->qual + off, bytes, cudaMemcpyHostToDevice, c->up_stream), "upload qual");
+            c->h2d_bytes += (uint64_t)n * (13 + 2 * (uint64_t)r->pitch);
+        }
+        CK(cudaEventRecord(s.uploaded, c->up_stream), "event");
+        return GSNP_OK;
+    };
+    for (auto& s : g->slot) CK(cudaEventRecord(s.free, c->stream), "event");
+    if (nk > 0) rc = upload(0);
+    uint64_t totals[kNumStats] = {};
+    const bool vec4 = L % 4 == 0 && r->pitch % 4 == 0 && L <= r->pitch;
+    const int per_row = vec4 ? L / 4 : L;
+    const int rows_per_block = std::max(1, 256 / per_row);
+    for (size_t k = 0; k < nk && rc == GSNP_OK; ++k) {
+        if (k + 1 < nk) {
+            rc = upload(k + 1);
+            if (rc != GSNP_OK) break;
+        }
+        const Chunk& ch = chunks[k];
+        StreamRing::Slot& s = g->slot[k & 1];
+        const int64_t nd = ch.R1 - ch.R0, nraw = ch.raw_hi - ch.raw_lo, nwt = ch.w1 - ch.w0 + 1;
+        /* window tables of windows [w0 - 1, w1): references before the chunk
+         * go to the carried window, entry 0 */
+        uint8_t* tf = s.h_tab;
+        int32_t* tl = reinterpret_cast<int32_t*>(s.h_tab + ((nwt + 15) & ~(int64_t)15));
+        int32_t* th = tl + nwt;
+        tf[0] = 0;
+        tl[0] = -1;
+        th[0] = -1;
+        for (int64_t w = ch.w0; w < ch.w1; ++w) {
+            const int64_t i = w - ch.w0 + 1;
+            const int32_t hs = P.host_src[w], ls = P.lik_src[w];
+            tf[i] = P.flags[w];
+            tl[i] = ls >= 0 && ls < ch.w0 ? (int32_t)(ch.w0 - 1) : ls;
+            th[i] = hs >= 0 && hs < ch.w0 ? (int32_t)(ch.w0 - 1) : hs;
+        }
+        CK(cudaMemcpyAsync(s.win_flags, tf, nwt, cudaMemcpyHostToDevice, c->stream), "window tables");
+        CK(cudaMemcpyAsync(s.win_lik_src, tl, nwt * 4, cudaMemcpyHostToDevice, c->stream), "window tables");
+        CK(cudaMemcpyAsync(s.win_host_src, th, nwt * 4, cudaMemcpyHostToDevice, c->stream), "window tables");
+        /* the chunk's deposited index and packed reads */
+        CK(cudaStreamWaitEvent(c->stream, s.uploaded, 0), "wait");
+        if (nd > 0) {
+            const int64_t n_chunks = (nraw + kDepChunk - 1) / kDepChunk;
+            dep_count_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(nraw, s.raw_pos, s.raw_len, c->chr_len,
+                                                                                s.dep_off);
+            dep_scan_kernel<<<1, 1024, 0, c->stream>>>(s.dep_off, n_chunks);
+            dep_index_kernel<<<(unsigned)n_chunks, kDepThreads, 0, c->stream>>>(nraw, s.raw_pos, s.raw_len,
+                                                                                c->chr_len, s.dep_off, nd, s.idx);
+            CK(cudaGetLastError(), "index kernels");
+            const int64_t per_block = (int64_t)rows_per_block * kGatherRows;
+            const unsigned blocks = (unsigned)((nd + per_block - 1) / per_block);
+            if (vec4)
+                gather_reads_kernel<4><<<blocks, 256, 0, c->stream>>>(
+                    0, nd, s.idx, nraw, s.raw_pos, s.raw_len, s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, r->pitch,
+                    L, rows_per_block, s.pos, s.lenhit, s.len, s.strand, s.bq, c->d_gerror);
+            else
+                gather_reads_kernel<1><<<blocks, 256, 0, c->stream>>>(
+                    0, nd, s.idx, nraw, s.raw_pos, s.raw_len, s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, r->pitch,
+                    L, rows_per_block, s.pos, s.lenhit, s.len, s.strand, s.bq, c->d_gerror);
+            CK(cudaGetLastError(), "gather kernel");
+        }
+        if (carry_c[k] >= 0) CK(cudaMemcpyAsync(g->counts, g->carry_counts, sizeof(SiteCounts) * kWin,
+                                                cudaMemcpyDeviceToDevice, c->stream), "carried counts");
+        if (carry_l[k] >= 0) CK(cudaMemcpyAsync(g->lik, g->carry_lik, sizeof(double) * kWin * 10,
+                                                cudaMemcpyDeviceToDevice, c->stream), "carried likelihood");
+        /* the calling pass over the chunk */
+        gsnp_context::ChunkView& vw = c->view;
+        vw.on = true;
+        vw.w0 = ch.w0;
+        vw.S0 = ch.S0;
+        vw.T0 = ch.T0;
+        vw.T1 = ch.T1;
+        vw.R0 = ch.R0;
+        vw.R1 = ch.R1;
+        vw.pos = s.pos;
+        vw.lenhit = s.lenhit;
+        vw.strand = s.strand;
+        vw.bq = s.bq;
+        vw.out = s.out;
+        vw.counts = g->counts;
+        vw.lik_keep = g->lik;
+        vw.win_flags = s.win_flags;
+        vw.win_lik_src = s.win_lik_src;
+        vw.win_host_src = s.win_host_src;
+        c->n_gathered = ch.R1;
+        const std::vector<Segment> seg{Segment{ch.T0, ch.T1, ch.R0, ch.R1, ch.raw_hi, ch.next_pos}};
+        rc = run_calling(c, seg, nullptr, nullptr);
+        if (rc == kRedoDeferred) rc = run_calling(c, seg, nullptr, nullptr);   /* the deferred pool was grown */
+        if (rc != GSNP_OK) break;
+        for (int i = 1; i < kNumStats; ++i)
+            totals[i] = i == 3 ? std::max(totals[i], c->stats[i]) : totals[i] + c->stats[i];
+        /* windows a later chunk carries */
+        if (save_c[k] >= 0)
+            CK(cudaMemcpyAsync(g->carry_counts, g->counts + (save_c[k] - ch.w0 + 1) * kWin, sizeof(SiteCounts) * kWin,
+                               cudaMemcpyDeviceToDevice, c->stream), "carried counts");
+        if (save_l[k] >= 0)
+            CK(cudaMemcpyAsync(g->carry_lik, g->lik + (save_l[k] - ch.w0 + 1) * kWin * 10, sizeof(double) * kWin * 10,
+                               cudaMemcpyDeviceToDevice, c->stream), "carried likelihood");
+        /* outputs */
+        const SiteCall* calls = based(s.out, ch.S0);
+        const SiteCounts* cnt = g->counts ? based(g->counts, (ch.w0 - 1) * kWin) : nullptr;
+        if (cns) {
+            uint64_t bytes = 0;
+            rc = emit_sites(c, chr_n, ch.S0, ch.S1, calls, cnt, based(s.win_host_src, ch.w0 - 1), &bytes,
+                            [&](const char* t, uint64_t n) { return fwrite(t, 1, n, cns) == n; }, true);
+            if (rc != GSNP_OK) break;
+        }
+        if (columns_base) {
+            ColumnsGpuStats st;
+            if (c->colw->write(ch.w0, ch.w1, c->d_codes, calls, cnt, based(s.win_host_src, ch.w0 - 1),
+                               based(th, ch.w0 - 1), c->h_codes.data(), c->stream, &st, &err) != 0) {
+                rc = fail(c, GSNP_ERR_INPUT, err);
+                break;
+            }
+            c->columns_host_windows += st.host_windows;
+        }
+        if (out) {
+            CK(cudaEventRecord(c->ev_seg, c->stream), "event");
+            CK(cudaStreamWaitEvent(c->down_stream, c->ev_seg, 0), "wait");
+            CK(cudaMemcpyAsync(out + ch.S0, s.out, (size_t)(ch.S1 - ch.S0) * sizeof(SiteCall), cudaMemcpyDeviceToHost,
+                               c->down_stream),
+               "download");
+            c->d2h_bytes += (uint64_t)(ch.S1 - ch.S0) * sizeof(SiteCall);
+            CK(cudaEventRecord(s.free, c->down_stream), "event");
+        } else {
+            CK(cudaEventRecord(s.free, c->stream), "event");
+        }
+    }
+    drain();
+    if (cns && rc == GSNP_OK) rc = emit_finish(c);
+    close_outputs();
+    timer.mark("chunks");
+    if (rc != GSNP_OK) return rc;
+    int gerr = 0;
+    CK(to_map(c, c->d_gerror, kMapGerror, sizeof(int)), "error flag");
+    CK(cudaStreamSynchronize(c->stream), "error flag");
+    memcpy(&gerr, c->h_map + kMapGerror, sizeof(int));
+    if (gerr == 3) return fail(c, GSNP_ERR_STATE, "deposited alignment list does not match the window replay");
+    if (gerr) return fail(c, GSNP_ERR_INPUT, "unknown base when encoding (only ACGT/acgt are accepted)");
+    totals[0] = (uint64_t)c->chr_len;
+    memcpy(c->stats, totals, sizeof(totals));
+    c->streamed = true;
     return GSNP_OK;
 }
 
@@ -2262,9 +2868,17 @@ extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const c
     if (c->columns_gpu) {
         /* the windows encoded on the device, from the resident calls */
         ColumnsGpuStats st;
-        if (write_columns_gpu(c->plan, c->d_codes, c->d_out, c->have_counts ? c->d_counts : nullptr,
-                              c->h_codes.data(), chr_name, base_path, c->stream, host_threads(), &st, &err) != 0)
-            return fail(c, GSNP_ERR_INPUT, err);
+        if (!c->colw) c->colw.reset(new ColumnsGpuWriter());
+        if (!c->sms) CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
+        const int64_t nwin = c->plan.n_windows;
+        int rc = c->colw->open(c->plan, chr_name, base_path, std::min<int64_t>(nwin, c->sms), &err);
+        if (rc == 0)
+            rc = c->colw->write(0, nwin, c->d_codes, c->d_out, c->have_counts ? c->d_counts : nullptr,
+                                c->d_win_host_src, c->plan.host_src.data(), c->h_codes.data(), c->stream, &st, &err);
+        std::string err2;
+        const int rc2 = c->colw->close(&err2);
+        if (rc != 0) return fail(c, GSNP_ERR_INPUT, err);
+        if (rc2 != 0) return fail(c, GSNP_ERR_INPUT, err2);
         c->columns_host_windows = st.host_windows;
         return GSNP_OK;
     }
@@ -2273,5 +2887,27 @@ extern "C" int gsnp_write_columns(gsnp_context* c, const char* chr_name, const c
     if (write_columns(c->plan, c->h_codes.data(), calls.get(), c->have_counts ? counts.get() : nullptr, chr_name,
                       base_path, dict, host_threads(), &err) != 0)
         return fail(c, GSNP_ERR_INPUT, err);
+    return GSNP_OK;
+}
+
+extern "C" int gsnp_call_streamed(gsnp_context* c, const gsnp_reads* r, const char* chr_name, gsnp_site_call* out,
+                                  const char* cns_path, const char* columns_base) {
+    if (!c) return GSNP_ERR_ARG;
+    /* the chunk view stays off whatever way the call ends */
+    struct ViewOff {
+        gsnp_context* c;
+        ~ViewOff() {
+            c->view.on = false;
+            c->called = false;   /* no call stays resident */
+        }
+    } off{c};
+    c->columns_host_windows = 0;
+    return gsnp::call_streamed(c, r, chr_name, out, cns_path, columns_base);
+}
+
+extern "C" int gsnp_stream_footprint(gsnp_context* c, uint64_t* ring_bytes, uint64_t* writer_bytes) {
+    if (!c || !ring_bytes || !writer_bytes) return fail(c, GSNP_ERR_ARG, "null argument");
+    *ring_bytes = c->ring ? (uint64_t)c->ring->bytes : 0;
+    *writer_bytes = c->colw ? (uint64_t)c->colw->device_bytes() : 0;
     return GSNP_OK;
 }

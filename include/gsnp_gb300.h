@@ -144,6 +144,30 @@ int gsnp_call_chromosome(gsnp_context* ctx, const gsnp_reads* reads);
  * gsnp_call_chromosome + gsnp_fetch_sites, which remain available. */
 int gsnp_call_chromosome_into(gsnp_context* ctx, const gsnp_reads* reads, gsnp_site_call* out);
 
+/* The chromosome-scale form of gsnp_call_chromosome_into
+ * (cpp/call_genotype.cc:422-669 streams the genome through its window the
+ * same way): the chromosome is called in chunks of "stream_windows" windows
+ * of 262,144 sites (gsnp_set_option, default 16), and the device holds only
+ * two chunks' alignments and calls at a time, so that its memory is set by the
+ * chunk size and the depth, not by the chromosome's length (the site codes,
+ * one byte per site, and the tables stay resident).  While chunk k is called,
+ * chunk k + 1's alignments are uploaded; each chunk's results then go to the
+ * outputs that are given (any may be NULL):
+ *   out           every site's call, as gsnp_call_chromosome_into;
+ *   cns_path      the cns text of every site (gsnp_write_cns's bytes);
+ *   columns_base  the six -C files (gsnp_write_columns's bytes).
+ * chr_name is needed for the two files.  The results equal the resident
+ * call's; afterwards no call stays resident (gsnp_fetch_sites, gsnp_write_cns
+ * and gsnp_write_columns answer GSNP_ERR_STATE until the next resident call). */
+int gsnp_call_streamed(gsnp_context* ctx, const gsnp_reads* reads, const char* chr_name, gsnp_site_call* out,
+                       const char* cns_path, const char* columns_base);
+
+/* No counterpart in the reference.  Device bytes a streamed call holds
+ * besides the per-site reference codes and the tables: the chunk ring of the
+ * last gsnp_call_streamed, and the -C writer's batch buffers (also used by
+ * gsnp_write_columns). */
+int gsnp_stream_footprint(gsnp_context* ctx, uint64_t* ring_bytes, uint64_t* writer_bytes);
+
 /* Re-run the calling kernels on the alignments already resident on the device
  * (no host transfer); used to time the kernels alone. */
 int gsnp_recall_resident(gsnp_context* ctx);
@@ -170,6 +194,7 @@ int gsnp_recall_resident(gsnp_context* ctx);
  *                         call only)
  *   columns_gpu           1: gsnp_write_columns encodes the windows on the
  *                         GPU; 0: on the host threads (same bytes)
+ *   stream_windows        windows per chunk of gsnp_call_streamed (1 and up)
  * GSNP_ERR_ARG for an unknown name or bin.  The environment variable
  * GSNP_OPTIONS="name=value,..." sets options when a context is created, after
  * the "name value" lines of the file GSNP_TUNE_FILE names (gsnp_tune). */
