@@ -74,8 +74,9 @@ struct EncArgs {
     uint8_t* out[5];                 /* [batch][cap[f]] */
     uint64_t cap[5];
     uint64_t* len;                   /* [batch][5] bytes used */
-    int* fallback;                   /* [batch] */
-    /* scratch, [batch][kWin] each */
+    int* fallback;                   /* [batch][5]: the file's block did not fit */
+    /* scratch, [batch][2][kWin] each: one slot for the run-length file, one
+     * for .11_12_13 */
     uint64_t* s_val;                 /* run values (integer or double bits), sparse values */
     uint32_t* s_aux;                 /* run starts, then run lengths */
     uint64_t* s_dict;                /* dictionary values */
@@ -144,12 +145,13 @@ struct Enc {
     int hs;
     int r0, r1;       /* this thread's rows */
     bool bad;         /* CTA-uniform: the window falls back to the host */
+    int slot;         /* the file's scratch slot (two files use scratch) */
 
     __device__ CnsRow row(int j) const { return make_row(hs, w, j, e.codes, e.calls, e.counts); }
     __device__ uint8_t* out(int f) const { return e.out[f] + (size_t)b * e.cap[f]; }
-    __device__ uint64_t* sval() const { return e.s_val + (size_t)b * kWin; }
-    __device__ uint32_t* saux() const { return e.s_aux + (size_t)b * kWin; }
-    __device__ uint64_t* sdict() const { return e.s_dict + (size_t)b * kWin; }
+    __device__ uint64_t* sval() const { return e.s_val + ((size_t)b * 2 + slot) * kWin; }
+    __device__ uint32_t* saux() const { return e.s_aux + ((size_t)b * 2 + slot) * kWin; }
+    __device__ uint64_t* sdict() const { return e.s_dict + ((size_t)b * 2 + slot) * kWin; }
     __device__ bool fits(int f, uint64_t bytes) {
         if (bytes > e.cap[f]) bad = true;
         return !bad;
@@ -207,12 +209,16 @@ struct IntDict {
         const int64_t x = v - lo;
         return pre[x >> 5] + __popc(bm[x >> 5] & ((1u << (x & 31)) - 1u));
     }
-    /* the values ascending as 4-byte integers at dst */
+    /* the values ascending as 4-byte integers at dst.  Nothing for an empty
+     * dictionary: build() leaves the bitmap as it found it then (shared
+     * memory not yet written by this CTA), and no entry is written past the
+     * d counted. */
     __device__ void put_values(uint8_t* dst) const {
+        if (d == 0) return;
         for (int k = threadIdx.x; k < kBitmapWords; k += kEncThreads) {
             uint32_t bits = bm[k];
             uint32_t r = pre[k];
-            while (bits) {
+            while (bits && r < (uint32_t)d) {
                 const int i = __ffs(bits) - 1;
                 bits &= bits - 1;
                 put32(dst + 4 * (size_t)r++, (uint32_t)(lo + (int64_t)k * 32 + i));
@@ -700,7 +706,10 @@ __global__ void __launch_bounds__(kEncThreads) encode_windows_kernel(EncArgs e) 
     ddict.negzero = &hash_negzero;
     ddict.d = 0;
 
-    Enc x{e, (int)blockIdx.x, e.w0 + blockIdx.x, 0, 0, 0, 0, false};
+    /* one CTA per (window, file): the five files of a window are
+     * independent, so a small batch of windows still fills the GPU */
+    const int f = (int)blockIdx.y;
+    Enc x{e, (int)blockIdx.x, e.w0 + blockIdx.x, 0, 0, 0, 0, false, f == kF111213 ? 1 : 0};
     x.n = (int)e.call_len[x.w];
     x.hs = e.host_src[x.w];
     x.r0 = min(x.n, (int)threadIdx.x * kEncPer);
@@ -708,16 +717,14 @@ __global__ void __launch_bounds__(kEncThreads) encode_windows_kernel(EncArgs e) 
     bool mine = true;
     for (int j = x.r0; j < x.r1; ++j) mine = mine && x.row(j).nflag;
     const bool all_n = __syncthreads_and(mine) != 0;
-    file_346(x, all_n);
-    __syncthreads();
-    if (!x.bad) file_rle(x, all_n, idict, ddict);
-    __syncthreads();
-    if (!x.bad) file_10(x, all_n);
-    __syncthreads();
-    if (!x.bad) file_111213(x, all_n, idict);
-    __syncthreads();
-    if (!x.bad) file_1517(x, all_n);
-    if (threadIdx.x == 0) e.fallback[x.b] = x.bad ? 1 : 0;
+    switch (f) {
+        case kF346: file_346(x, all_n); break;
+        case kFRle: file_rle(x, all_n, idict, ddict); break;
+        case kF10: file_10(x, all_n); break;
+        case kF111213: file_111213(x, all_n, idict); break;
+        default: file_1517(x, all_n); break;
+    }
+    if (threadIdx.x == 0) e.fallback[x.b * 5 + f] = x.bad ? 1 : 0;
 }
 
 constexpr size_t kEncSmem = 2 * kBitmapWords * 4 + kHashCap * 8;
@@ -796,10 +803,10 @@ int ColumnsGpuWriter::open(const WindowPlan& plan, const char* chr_name, const s
         for (int f = 0; f < 5 && ce == cudaSuccess; ++f) ce = cudaMalloc((void**)&d_out_[f], kCapHost[f] * (size_t)batch);
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_bits_, kWin + 2);
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_len_, sizeof(uint64_t) * 5 * batch);
-        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_fb_, sizeof(int) * batch);
-        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sval_, sizeof(uint64_t) * kWin * batch);
-        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sdict_, sizeof(uint64_t) * kWin * batch);
-        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_saux_, sizeof(uint32_t) * kWin * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_fb_, sizeof(int) * 5 * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sval_, sizeof(uint64_t) * kWin * 2 * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sdict_, sizeof(uint64_t) * kWin * 2 * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_saux_, sizeof(uint32_t) * kWin * 2 * batch);
         if (ce == cudaSuccess) {
             std::vector<uint8_t> bits(kWin + 2);
             bits[0] = 1;
@@ -850,7 +857,7 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
     int rc = 0;
     cudaError_t ce = cudaSuccess;
     std::vector<uint64_t> h_len((size_t)(5 * batch_cap_));
-    std::vector<int> h_fb((size_t)batch_cap_);
+    std::vector<int> h_fb5((size_t)(5 * batch_cap_)), h_fb((size_t)batch_cap_);
     HostDictCodec dict;
     for (int64_t b0 = w0; b0 < w1 && rc == 0; b0 += batch_cap_) {
         const int64_t nb = std::min(batch_cap_, w1 - b0);
@@ -871,11 +878,17 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
         e.s_val = d_sval_;
         e.s_aux = d_saux_;
         e.s_dict = d_sdict_;
-        encode_windows_kernel<<<(unsigned)nb, kEncThreads, kEncSmem, stream>>>(e);
+        encode_windows_kernel<<<dim3((unsigned)nb, 5), kEncThreads, kEncSmem, stream>>>(e);
         ce = cudaGetLastError();
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_len.data(), d_len_, sizeof(uint64_t) * 5 * nb, cudaMemcpyDeviceToHost, stream);
-        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_fb.data(), d_fb_, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_fb5.data(), d_fb_, sizeof(int) * 5 * nb, cudaMemcpyDeviceToHost, stream);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+        /* a window goes to the host encoder when any of its files did not fit */
+        for (int64_t b = 0; b < nb; ++b) {
+            int any = 0;
+            for (int f = 0; f < 5; ++f) any |= h_fb5[(size_t)(5 * b + f)];
+            h_fb[(size_t)b] = any;
+        }
         if (ce != cudaSuccess) {
             *err = std::string("-C encoder: ") + cudaGetErrorString(ce);
             rc = 1;
@@ -952,7 +965,7 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
 size_t ColumnsGpuWriter::device_bytes() const {
     size_t n = 0;
     for (int f = 0; f < 5; ++f) n += kCapHost[f] * (size_t)batch_cap_;
-    return n + (size_t)batch_cap_ * (kWin * 20 + 44) + (kWin + 2) + (size_t)len_tab_windows_ * 8;
+    return n + (size_t)batch_cap_ * (kWin * 40 + 60) + (kWin + 2) + (size_t)len_tab_windows_ * 8;
 }
 
 int ColumnsGpuWriter::close(std::string* err) {
