@@ -161,6 +161,10 @@ def load_peaks():
 # tiles' reads once and writes one call per site, so traffic grows with the
 # sites.  Keyed by (workload, kernel kind, record slots); other kernels report
 # no traffic.
+# file outputs of the timed e2e steps go to a RAM-backed directory where the
+# host has one, so that a disk's write-back does not time the caller
+RAM_DIR = "/dev/shm" if os.path.isdir("/dev/shm") and os.access("/dev/shm", os.W_OK) else None
+
 NCU_BYTES_PER_SITE = {
     ("c1", 2, 40): 150.6,   # call_fast_kernel<40>: 324.6 MB (dram__bytes.sum) over 2,154,656 sites
     ("c1", 4, 48): 95.0,    # call_stream_kernel<48>: 325.2 MB read + 150.1 MB written over 5,000,000 sites
@@ -445,7 +449,7 @@ def main():
     columns = None
     cdir = None
     try:
-        cdir = tempfile.mkdtemp(prefix="gsnp_bench_columns_")
+        cdir = tempfile.mkdtemp(prefix="gsnp_bench_columns_", dir=RAM_DIR)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         rc = caller.lib.gsnp_write_columns(caller.ctx, w.chr_name.encode(), os.path.join(cdir, "cns").encode())
@@ -453,7 +457,8 @@ def main():
         files = [os.path.join(cdir, f) for f in os.listdir(cdir)]
         columns = ({"ms": round(ms, 2), "bytes": sum(os.path.getsize(f) for f in files), "files": len(files),
                     "note": "gsnp_write_columns of the last call: windows encoded on the GPU (the host encoder takes "
-                            "any window that overflows its buffers), downloaded, written to a temporary directory"}
+                            "any window that overflows its buffers), downloaded, the five binary files written by a "
+                            "thread each, to a temporary directory (%s)" % (RAM_DIR or "the default")}
                    if rc == 0 else {"error": "gsnp_write_columns returned %d" % rc})
     except Exception as e:   # informational only: never costs the bench line
         columns = {"error": repr(e)[:200]}
@@ -468,7 +473,7 @@ def main():
     streamed = None
     sdir = None
     try:
-        sdir = tempfile.mkdtemp(prefix="gsnp_bench_streamed_")
+        sdir = tempfile.mkdtemp(prefix="gsnp_bench_streamed_", dir=RAM_DIR)
         caller.set_option("stream_windows", args.stream_windows)
         forms = {}
         for prec in (precision, other):

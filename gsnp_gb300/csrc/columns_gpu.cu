@@ -39,6 +39,9 @@
 
 #include "columns.h"
 #include "columns_gpu.h"
+
+#include <future>
+#include <memory>
 #include "dict.h"
 #include "rows.h"
 
@@ -46,7 +49,6 @@ namespace gsnp {
 namespace {
 
 constexpr int kEncThreads = 1024;
-constexpr int kEncPer = kWin / kEncThreads;           /* rows per thread */
 constexpr int kBitmapBits = kWin + 64;                /* value span of an integer dictionary */
 constexpr int kBitmapWords = kBitmapBits / 32;
 constexpr int kHashCap = 4096;                        /* slots of the double hash set */
@@ -80,6 +82,13 @@ struct EncArgs {
     uint64_t* s_val;                 /* run values (integer or double bits), sparse values */
     uint32_t* s_aux;                 /* run starts, then run lengths */
     uint64_t* s_dict;                /* dictionary values */
+    /* per row, from rows_prep_kernel: the six run-length columns' values
+     * (columns 5 7 8 9 14 as [5][batch][kWin] integers, 16 as [batch][kWin]
+     * double bits), and per window whether any row is not an N row */
+    uint32_t* rle32;
+    uint64_t* rle64;
+    int* not_n;
+    int64_t stride;                  /* windows of the batch buffers */
 };
 
 __device__ __forceinline__ void put8(uint8_t* p, uint8_t v) { *p = v; }
@@ -143,7 +152,6 @@ struct Enc {
     int64_t w;        /* window */
     int n;            /* rows */
     int hs;
-    int r0, r1;       /* this thread's rows */
     bool bad;         /* CTA-uniform: the window falls back to the host */
     int slot;         /* the file's scratch slot (two files use scratch) */
 
@@ -152,11 +160,57 @@ struct Enc {
     __device__ uint64_t* sval() const { return e.s_val + ((size_t)b * 2 + slot) * kWin; }
     __device__ uint32_t* saux() const { return e.s_aux + ((size_t)b * 2 + slot) * kWin; }
     __device__ uint64_t* sdict() const { return e.s_dict + ((size_t)b * 2 + slot) * kWin; }
+    /* value of run-length column k of row j */
+    __device__ uint64_t rle(int k, int64_t j) const {
+        return k < 5 ? (uint64_t)e.rle32[((size_t)k * e.stride + b) * kWin + j] : e.rle64[(size_t)b * kWin + j];
+    }
     __device__ bool fits(int f, uint64_t bytes) {
         if (bytes > e.cap[f]) bad = true;
         return !bad;
     }
 };
+
+/* Rows of a window in order, CTA-wide: warp k walks rows
+ * [k * kWarpRows, (k + 1) * kWarpRows), 32 at a time, lane l taking row
+ * base + 32 i + l, so that the lanes of a load touch consecutive rows.
+ * Ordered lists are built from a count pass (ballots per warp), the
+ * warps' prefix (warp_prefix) and a write pass, in which each lane's slot
+ * is its warp's running offset plus the ballot's lanes below it. */
+constexpr int kEncWarps = kEncThreads / 32;
+constexpr int kWarpRows = kWin / kEncWarps;
+static_assert(kWarpRows % 32 == 0, "a warp's rows are whole iterations");
+constexpr unsigned kEncFull = 0xffffffffu;
+
+__device__ __forceinline__ int64_t warp_base() { return (int64_t)(threadIdx.x >> 5) * kWarpRows; }
+__device__ __forceinline__ unsigned lanes_below() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+/* exclusive prefix, over the CTA's warps in order, of each warp's count c
+ * (the same in all its lanes); *total the sum */
+__device__ int64_t warp_prefix(int64_t c, int64_t* total) {
+    const int64_t off = block_scan((threadIdx.x & 31) == 0 ? c : 0, total);
+    return __shfl_sync(kEncFull, off, 0);
+}
+
+/* the slot of this lane's entry in an ordered list whose next free slot
+ * for the warp is *off; advances *off past the ballot's entries */
+__device__ __forceinline__ int64_t list_slot(bool p, int64_t* off) {
+    const unsigned m = __ballot_sync(kEncFull, p);
+    const int64_t k = *off + __popc(m & lanes_below());
+    *off += __popc(m);
+    return k;
+}
+
+/* the 2-bit code words of rows [first, first + 16), first = the half-warp's
+ * first row: the code of row j at bits 2 (last - 1 - j), last = min(n,
+ * first + 16), ORed over the half-warp (every lane calls it) */
+__device__ __forceinline__ uint32_t half_word(uint32_t code, int64_t j, int64_t n) {
+    const int64_t first = j & ~(int64_t)15;
+    const int64_t last = min(n, first + 16);
+    uint32_t v = j < n ? code << (2 * (last - 1 - j)) : 0u;
+#pragma unroll
+    for (int d = 8; d > 0; d >>= 1) v |= __shfl_xor_sync(kEncFull, v, d);
+    return v;
+}
 
 /* ---- dictionaries ---------------------------------------------------- */
 
@@ -364,51 +418,44 @@ __device__ void file_346(Enc& x, bool all_n) {
             *c = c_actgn[r.base1 & 7];
         }
     };
+    const int lane = threadIdx.x & 31;
+    const int64_t wb = warp_base();
     int c4 = 0, c6 = 0, cn = 0;
-    for (int j = x.r0; j < x.r1; ++j) {
-        char a, b, c;
-        abc(j, &a, &b, &c);
-        c4 += b != a;
-        c6 += c != a;
-        cn += a == 'N';
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        const bool in = j < x.n;
+        char a = 0, b = 0, c = 0;
+        if (in) abc((int)j, &a, &b, &c);
+        c4 += __popc(__ballot_sync(kEncFull, in && b != a));
+        c6 += __popc(__ballot_sync(kEncFull, in && c != a));
+        cn += __popc(__ballot_sync(kEncFull, in && a == 'N'));
     }
     int64_t N4, N6, NN;
-    int64_t o4 = block_scan(c4, &N4), o6 = block_scan(c6, &N6), on = block_scan(cn, &NN);
+    int64_t o4 = warp_prefix(c4, &N4), o6 = warp_prefix(c6, &N6), on = warp_prefix(cn, &NN);
     const uint64_t nw = (n + 15) / 16;
     const uint64_t total = 56 + 5 * N4 + 5 * N6 + 4 * NN + 4 * nw;
     if (!x.fits(kF346, total)) return;
     const uint64_t b_id4 = 56, b_v4 = b_id4 + 4 * N4, b_id6 = b_v4 + N4, b_v6 = b_id6 + 4 * N6, b_idn = b_v6 + N6,
                    b_code = b_idn + 4 * NN;
-    for (int j = x.r0; j < x.r1; ++j) {
-        char a, b, c;
-        abc(j, &a, &b, &c);
-        if (b != a) {
-            put32(o + b_id4 + 4 * o4, (uint32_t)j);
-            put8(o + b_v4 + o4, (uint8_t)b);
-            ++o4;
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        const bool in = j < x.n;
+        char a = 0, b = 0, c = 0;
+        if (in) abc((int)j, &a, &b, &c);
+        const bool p4 = in && b != a, p6 = in && c != a, pn = in && a == 'N';
+        const int64_t k4 = list_slot(p4, &o4), k6 = list_slot(p6, &o6), kn = list_slot(pn, &on);
+        if (p4) {
+            put32(o + b_id4 + 4 * k4, (uint32_t)j);
+            put8(o + b_v4 + k4, (uint8_t)b);
         }
-        if (c != a) {
-            put32(o + b_id6 + 4 * o6, (uint32_t)j);
-            put8(o + b_v6 + o6, (uint8_t)c);
-            ++o6;
+        if (p6) {
+            put32(o + b_id6 + 4 * k6, (uint32_t)j);
+            put8(o + b_v6 + k6, (uint8_t)c);
         }
-        if (a == 'N') {
-            put32(o + b_idn + 4 * on, (uint32_t)j);
-            ++on;
-        }
-    }
-    /* the 16 code words of this thread's rows */
-    for (int k = 0; k < kEncPer / 16; ++k) {
-        const int first = x.r0 + 16 * k;
-        if (first >= x.n) break;
-        const int last = min(x.n, first + 16);
-        uint32_t word = 0;
-        for (int j = first; j < last; ++j) {
-            char a, b, c;
-            abc(j, &a, &b, &c);
-            word = (word << 2) | code2(a);
-        }
-        put32(o + b_code + 4 * (uint64_t)(first / 16), word);
+        if (pn) put32(o + b_idn + 4 * kn, (uint32_t)j);
+        /* the code words of the two half-warps' 16 rows */
+        const uint32_t word = half_word(code2(a), j, x.n);
+        if ((lane & 15) == 0 && in) put32(o + b_code + 4 * (uint64_t)(j / 16), word);
     }
     if (threadIdx.x == 0) {
         const uint64_t param[7] = {0, (uint64_t)(5 * N4 + 5 * N6 + 4 * NN) + 4 * nw, n, nw, (uint64_t)NN,
@@ -450,27 +497,35 @@ __device__ void file_rle(Enc& x, bool all_n, IntDict& idict, DblDict& ddict) {
     uint64_t* rv = x.sval();    /* run values */
     uint32_t* rs = x.saux();    /* run starts */
     uint64_t* rl = x.sdict();   /* run lengths */
+    const int lane = threadIdx.x & 31;
+    const int64_t wb = warp_base();
     for (int k = 0; k < 6; ++k) {
-        /* run starts: a row whose value differs from the row before */
-        int cs = 0;
-        uint64_t prev = x.r0 > 0 && x.r0 < x.n ? rle_value(x.row(x.r0 - 1), k) : 0;
-        for (int j = x.r0; j < x.r1; ++j) {
-            const uint64_t v = rle_value(x.row(j), k);
-            cs += j == 0 || v != prev;
-            prev = v;
-        }
-        int64_t R;
-        int64_t orun = block_scan(cs, &R);
-        prev = x.r0 > 0 && x.r0 < x.n ? rle_value(x.row(x.r0 - 1), k) : 0;
-        for (int j = x.r0; j < x.r1; ++j) {
-            const uint64_t v = rle_value(x.row(j), k);
-            if (j == 0 || v != prev) {
-                rv[orun] = v;
-                rs[orun] = (uint32_t)j;
-                ++orun;
+        /* run starts: a row whose value differs from the row before (the row
+         * before a lane's is the lane below's, or for lane 0 the last row of
+         * the warp's previous 32, or the row before the warp's range) */
+        auto starts = [&](auto&& take) {
+            uint64_t carry = wb > 0 && wb < x.n ? x.rle(k, wb - 1) : 0;
+            for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+                const int64_t j = j0 + lane;
+                const bool in = j < x.n;
+                const uint64_t v = in ? x.rle(k, j) : 0;
+                const uint64_t up = __shfl_up_sync(kEncFull, v, 1);
+                const uint64_t prev = lane == 0 ? carry : up;
+                carry = __shfl_sync(kEncFull, v, 31);
+                take(in && (j == 0 || v != prev), j, v);
             }
-            prev = v;
-        }
+        };
+        int cs = 0;
+        starts([&](bool p, int64_t, uint64_t) { cs += __popc(__ballot_sync(kEncFull, p)); });
+        int64_t R;
+        int64_t orun = warp_prefix(cs, &R);
+        starts([&](bool p, int64_t j, uint64_t v) {
+            const int64_t slot = list_slot(p, &orun);
+            if (p) {
+                rv[slot] = v;
+                rs[slot] = (uint32_t)j;
+            }
+        });
         __syncthreads();
         for (int64_t r = threadIdx.x; r < R; r += kEncThreads)
             rl[r] = (uint64_t)((r + 1 < R ? (int64_t)rs[r + 1] : (int64_t)x.n) - (int64_t)rs[r]);
@@ -538,25 +593,27 @@ __device__ void file_10(Enc& x, bool all_n) {
         const CnsRow r = x.row(j);
         return (r.called() && r.base2 < 4) ? c_actgn[r.base2] : 'N';
     };
+    const int lane = threadIdx.x & 31;
+    const int64_t wb = warp_base();
     int cn = 0;
-    for (int j = x.r0; j < x.r1; ++j) cn += letter(j) == 'N';
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        cn += __popc(__ballot_sync(kEncFull, j < x.n && letter((int)j) == 'N'));
+    }
     int64_t NN;
-    int64_t on = block_scan(cn, &NN);
+    int64_t on = warp_prefix(cn, &NN);
     const uint64_t n = (uint64_t)x.n, nw = (n + 15) / 16;
     const uint64_t b_code = 4 + 24, b_nid = b_code + 4 * nw, total = b_nid + 4 * NN;
     if (!x.fits(kF10, total)) return;
-    for (int j = x.r0; j < x.r1; ++j)
-        if (letter(j) == 'N') put32(o + b_nid + 4 * on++, (uint32_t)j);
-    for (int k = 0; k < kEncPer / 16; ++k) {
-        const int first = x.r0 + 16 * k;
-        if (first >= x.n) break;
-        const int last = min(x.n, first + 16);
-        uint32_t word = 0;
-        for (int j = first; j < last; ++j) {
-            const char c = letter(j);
-            word = (word << 2) | code2(c == 'N' ? 'A' : c);
-        }
-        put32(o + b_code + 4 * (uint64_t)(first / 16), word);
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        const bool in = j < x.n;
+        const char c = in ? letter((int)j) : 'A';
+        const bool pn = in && c == 'N';
+        const int64_t kn = list_slot(pn, &on);
+        if (pn) put32(o + b_nid + 4 * kn, (uint32_t)j);
+        const uint32_t word = half_word(code2(c == 'N' ? 'A' : c), j, x.n);
+        if ((lane & 15) == 0 && in) put32(o + b_code + 4 * (uint64_t)(j / 16), word);
     }
     if (threadIdx.x == 0) {
         put64(o + 4, (uint64_t)NN);
@@ -587,16 +644,19 @@ __device__ void file_111213(Enc& x, bool all_n, IntDict& idict) {
         if (*v11 != *v13) return 2;
         return -1;
     };
+    const int lane = threadIdx.x & 31;
+    const int64_t wb = warp_base();
     int cc = 0, c12 = 0, c13 = 0;
-    for (int j = x.r0; j < x.r1; ++j) {
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
         int a, b, c;
-        const int k = cls(j, &a, &b, &c);
-        cc += k == 0;
-        c12 += k == 1;
-        c13 += k == 2;
+        const int k = j < x.n ? cls((int)j, &a, &b, &c) : -1;
+        cc += __popc(__ballot_sync(kEncFull, k == 0));
+        c12 += __popc(__ballot_sync(kEncFull, k == 1));
+        c13 += __popc(__ballot_sync(kEncFull, k == 2));
     }
     int64_t NC, N12, N13;
-    int64_t oc = block_scan(cc, &NC), o12 = block_scan(c12, &N12), o13 = block_scan(c13, &N13);
+    int64_t oc = warp_prefix(cc, &NC), o12 = warp_prefix(c12, &N12), o13 = warp_prefix(c13, &N13);
     const uint64_t b_e12id = 4 + 32, b_e12 = b_e12id + 4 * N12, b_e13id = b_e12 + 4 * N12, b_e13 = b_e13id + 4 * N13,
                    b_cid = b_e13 + 4 * N13, b_dicts = b_cid + 4 * NC;
     if (!x.fits(kF111213, b_dicts)) return;
@@ -604,23 +664,22 @@ __device__ void file_111213(Enc& x, bool all_n, IntDict& idict) {
     uint64_t* v11 = x.sval();
     uint32_t* v12 = x.saux();
     uint64_t* v13 = x.sdict();
-    for (int j = x.r0; j < x.r1; ++j) {
-        int a, b, c;
-        const int k = cls(j, &a, &b, &c);
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        int a = 0, b = 0, c = 0;
+        const int k = j < x.n ? cls((int)j, &a, &b, &c) : -1;
+        const int64_t sc = list_slot(k == 0, &oc), s12 = list_slot(k == 1, &o12), s13 = list_slot(k == 2, &o13);
         if (k == 0) {
-            put32(o + b_cid + 4 * oc, (uint32_t)j);
-            v11[oc] = (uint64_t)a;
-            v12[oc] = (uint32_t)b;
-            v13[oc] = (uint64_t)c;
-            ++oc;
+            put32(o + b_cid + 4 * sc, (uint32_t)j);
+            v11[sc] = (uint64_t)a;
+            v12[sc] = (uint32_t)b;
+            v13[sc] = (uint64_t)c;
         } else if (k == 1) {
-            put32(o + b_e12id + 4 * o12, (uint32_t)j);
-            put32(o + b_e12 + 4 * o12, (uint32_t)b);
-            ++o12;
+            put32(o + b_e12id + 4 * s12, (uint32_t)j);
+            put32(o + b_e12 + 4 * s12, (uint32_t)b);
         } else if (k == 2) {
-            put32(o + b_e13id + 4 * o13, (uint32_t)j);
-            put32(o + b_e13 + 4 * o13, (uint32_t)c);
-            ++o13;
+            put32(o + b_e13id + 4 * s13, (uint32_t)j);
+            put32(o + b_e13 + 4 * s13, (uint32_t)c);
         }
     }
     __syncthreads();
@@ -664,32 +723,67 @@ __device__ void file_1517(Enc& x, bool all_n) {
         if (threadIdx.x == 0) x.e.len[x.b * 5 + kF1517] = 4;
         return;
     }
+    const int lane = threadIdx.x & 31;
+    const int64_t wb = warp_base();
     int cr = 0, cs = 0;
-    for (int j = x.r0; j < x.r1; ++j) {
-        const CnsRow r = x.row(j);
-        if (!r.called()) continue;
-        cr += r.rank_sum != 1.0;
-        cs += (r.ori & 8) != 0;
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        bool pr = false, ps = false;
+        if (j < x.n) {
+            const CnsRow r = x.row((int)j);
+            pr = r.called() && r.rank_sum != 1.0;
+            ps = r.called() && (r.ori & 8) != 0;
+        }
+        cr += __popc(__ballot_sync(kEncFull, pr));
+        cs += __popc(__ballot_sync(kEncFull, ps));
     }
     int64_t NR, NS;
-    int64_t orr = block_scan(cr, &NR), os = block_scan(cs, &NS);
+    int64_t orr = warp_prefix(cr, &NR), os = warp_prefix(cs, &NS);
     const uint64_t b_id = 8, b_val = b_id + 4 * NR, b_cnt2 = b_val + 8 * NR, b_snp = b_cnt2 + 4, total = b_snp + 4 * NS;
     if (!x.fits(kF1517, total)) return;
-    for (int j = x.r0; j < x.r1; ++j) {
-        const CnsRow r = x.row(j);
-        if (!r.called()) continue;
-        if (r.rank_sum != 1.0) {
-            put32(o + b_id + 4 * orr, (uint32_t)j);
-            put64(o + b_val + 8 * orr, (uint64_t)__double_as_longlong(r.rank_sum));
-            ++orr;
+    for (int64_t j0 = wb; j0 < wb + kWarpRows && j0 < x.n; j0 += 32) {
+        const int64_t j = j0 + lane;
+        bool pr = false, ps = false;
+        double rs = 1.0;
+        if (j < x.n) {
+            const CnsRow r = x.row((int)j);
+            pr = r.called() && r.rank_sum != 1.0;
+            ps = r.called() && (r.ori & 8) != 0;
+            rs = r.rank_sum;
         }
-        if (r.ori & 8) put32(o + b_snp + 4 * os++, (uint32_t)j);
+        const int64_t kr = list_slot(pr, &orr), ks = list_slot(ps, &os);
+        if (pr) {
+            put32(o + b_id + 4 * kr, (uint32_t)j);
+            put64(o + b_val + 8 * kr, (uint64_t)__double_as_longlong(rs));
+        }
+        if (ps) put32(o + b_snp + 4 * ks, (uint32_t)j);
     }
     if (threadIdx.x == 0) {
         put32(o + 4, (uint32_t)NR);
         put32(o + b_cnt2, (uint32_t)NS);
         x.e.len[x.b * 5 + kF1517] = total;
     }
+}
+
+/* The rows of a batch of windows in one pass over the whole GPU, for the
+ * encoder's CTAs (one per window and file), which would otherwise each read
+ * every row's call again on every pass: the run-length columns' values, and
+ * e.not_n[b] = 1 when window b has a row that is not an N row (zeroed
+ * before).  Grid: (rows / 256, windows). */
+__global__ void __launch_bounds__(256) rows_prep_kernel(EncArgs e) {
+    const int b = (int)blockIdx.y;
+    const int64_t w = e.w0 + b;
+    const int64_t j = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    const int64_t n = e.call_len[w];
+    bool not_n = false;
+    if (j < n) {
+        const CnsRow r = make_row(e.host_src[w], w, j, e.codes, e.calls, e.counts);
+        not_n = !r.nflag;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) e.rle32[((size_t)k * e.stride + b) * kWin + j] = (uint32_t)rle_value(r, k);
+        e.rle64[(size_t)b * kWin + j] = rle_value(r, 5);
+    }
+    if (__syncthreads_or(not_n) && threadIdx.x == 0) e.not_n[b] = 1;
 }
 
 __global__ void __launch_bounds__(kEncThreads) encode_windows_kernel(EncArgs e) {
@@ -709,14 +803,10 @@ __global__ void __launch_bounds__(kEncThreads) encode_windows_kernel(EncArgs e) 
     /* one CTA per (window, file): the five files of a window are
      * independent, so a small batch of windows still fills the GPU */
     const int f = (int)blockIdx.y;
-    Enc x{e, (int)blockIdx.x, e.w0 + blockIdx.x, 0, 0, 0, 0, false, f == kF111213 ? 1 : 0};
+    Enc x{e, (int)blockIdx.x, e.w0 + blockIdx.x, 0, 0, false, f == kF111213 ? 1 : 0};
     x.n = (int)e.call_len[x.w];
     x.hs = e.host_src[x.w];
-    x.r0 = min(x.n, (int)threadIdx.x * kEncPer);
-    x.r1 = min(x.n, x.r0 + kEncPer);
-    bool mine = true;
-    for (int j = x.r0; j < x.r1; ++j) mine = mine && x.row(j).nflag;
-    const bool all_n = __syncthreads_and(mine) != 0;
+    const bool all_n = e.not_n[x.b] == 0;
     switch (f) {
         case kF346: file_346(x, all_n); break;
         case kFRle: file_rle(x, all_n, idict, ddict); break;
@@ -746,6 +836,9 @@ ColumnsGpuWriter::~ColumnsGpuWriter() {
         close(&e);
     }
     release();
+    for (int set = 0; set < 2; ++set)
+        for (int f = 0; f < 5; ++f)
+            if (hbuf_[set][f]) cudaFreeHost(hbuf_[set][f]);
 }
 
 void ColumnsGpuWriter::release() {
@@ -760,6 +853,12 @@ void ColumnsGpuWriter::release() {
     cudaFree(d_sval_);
     cudaFree(d_sdict_);
     cudaFree(d_saux_);
+    cudaFree(d_rle32_);
+    cudaFree(d_rle64_);
+    cudaFree(d_not_n_);
+    d_rle32_ = nullptr;
+    d_rle64_ = nullptr;
+    d_not_n_ = nullptr;
     d_bits_ = nullptr;
     d_len_tab_ = nullptr;
     d_len_ = nullptr;
@@ -807,6 +906,9 @@ int ColumnsGpuWriter::open(const WindowPlan& plan, const char* chr_name, const s
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sval_, sizeof(uint64_t) * kWin * 2 * batch);
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_sdict_, sizeof(uint64_t) * kWin * 2 * batch);
         if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_saux_, sizeof(uint32_t) * kWin * 2 * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_rle32_, sizeof(uint32_t) * kWin * 5 * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_rle64_, sizeof(uint64_t) * kWin * batch);
+        if (ce == cudaSuccess) ce = cudaMalloc((void**)&d_not_n_, sizeof(int) * batch);
         if (ce == cudaSuccess) {
             std::vector<uint8_t> bits(kWin + 2);
             bits[0] = 1;
@@ -878,8 +980,19 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
         e.s_val = d_sval_;
         e.s_aux = d_saux_;
         e.s_dict = d_sdict_;
-        encode_windows_kernel<<<dim3((unsigned)nb, 5), kEncThreads, kEncSmem, stream>>>(e);
-        ce = cudaGetLastError();
+        e.rle32 = d_rle32_;
+        e.rle64 = d_rle64_;
+        e.not_n = d_not_n_;
+        e.stride = batch_cap_;
+        ce = cudaMemsetAsync(d_not_n_, 0, sizeof(int) * nb, stream);
+        if (ce == cudaSuccess) {
+            rows_prep_kernel<<<dim3((unsigned)(kWin / 256), (unsigned)nb), 256, 0, stream>>>(e);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess) {
+            encode_windows_kernel<<<dim3((unsigned)nb, 5), kEncThreads, kEncSmem, stream>>>(e);
+            ce = cudaGetLastError();
+        }
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_len.data(), d_len_, sizeof(uint64_t) * 5 * nb, cudaMemcpyDeviceToHost, stream);
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_fb5.data(), d_fb_, sizeof(int) * 5 * nb, cudaMemcpyDeviceToHost, stream);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
@@ -894,20 +1007,36 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
             rc = 1;
             break;
         }
-        /* the batch's blocks, window by window, into one host buffer per file */
+        /* the batch's blocks, window by window, into one pinned host buffer
+         * per file, of the set the batch before last used (its writes are
+         * waited for first) */
+        const int set = set_;
+        set_ ^= 1;
+        if (!wait_set(set)) {
+            *err = "write failed";
+            rc = 1;
+            break;
+        }
         size_t tot[5] = {};
         for (int64_t b = 0; b < nb; ++b)
             if (!h_fb[(size_t)b])
                 for (int f = 0; f < 5; ++f) tot[f] += h_len[(size_t)(5 * b + f)];
-        for (int f = 0; f < 5; ++f)
-            if (host_buf_[f].size() < tot[f]) host_buf_[f].resize(tot[f]);
+        for (int f = 0; f < 5 && ce == cudaSuccess; ++f)
+            if (hcap_[set][f] < tot[f]) {
+                /* pinned, so that the blocks come down at the link's speed */
+                if (hbuf_[set][f]) cudaFreeHost(hbuf_[set][f]);
+                hbuf_[set][f] = nullptr;
+                hcap_[set][f] = 0;
+                ce = cudaMallocHost((void**)&hbuf_[set][f], tot[f] + tot[f] / 4);
+                if (ce == cudaSuccess) hcap_[set][f] = tot[f] + tot[f] / 4;
+            }
         size_t off[5] = {};
         for (int64_t b = 0; b < nb && ce == cudaSuccess; ++b) {
             if (h_fb[(size_t)b]) continue;
             for (int f = 0; f < 5 && ce == cudaSuccess; ++f) {
                 const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
                 if (bytes)
-                    ce = cudaMemcpyAsync(host_buf_[f].data() + off[f], d_out_[f] + (size_t)b * kCapHost[f], bytes,
+                    ce = cudaMemcpyAsync(hbuf_[set][f] + off[f], d_out_[f] + (size_t)b * kCapHost[f], bytes,
                                          cudaMemcpyDeviceToHost, stream);
                 off[f] += bytes;
             }
@@ -918,13 +1047,15 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
             rc = 1;
             break;
         }
-        /* windows the encoder left to the host, encoded in order among the others */
+        /* each file's pieces in window order: the encoder's blocks, and the
+         * windows it left to the host, encoded here */
+        std::vector<Piece> pieces[5];
         size_t wo[5] = {};
         for (int64_t b = 0; b < nb && rc == 0; ++b) {
             if (!h_fb[(size_t)b]) {
                 for (int f = 0; f < 5; ++f) {
                     const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
-                    if (bytes && fwrite(host_buf_[f].data() + wo[f], 1, bytes, fb_[f]) != bytes) rc = 1;
+                    if (bytes) pieces[f].push_back(Piece{hbuf_[set][f] + wo[f], bytes, nullptr});
                     wo[f] += bytes;
                 }
                 continue;
@@ -953,7 +1084,24 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
                 break;
             }
             for (int f = 0; f < 5; ++f)
-                if (!parts[f].empty() && fwrite(parts[f].data(), 1, parts[f].size(), fb_[f]) != parts[f].size()) rc = 1;
+                if (!parts[f].empty()) {
+                    auto own = std::make_shared<std::string>(std::move(parts[f]));
+                    pieces[f].push_back(Piece{own->data(), own->size(), own});
+                }
+        }
+        /* the files written on their own threads, each after its previous
+         * batch, while the caller goes on */
+        for (int f = 0; f < 5 && rc == 0; ++f) {
+            std::shared_future<bool> prev = last_[f];
+            FILE* file = fb_[f];
+            std::vector<Piece> ps = std::move(pieces[f]);
+            last_[f] = std::async(std::launch::async, [prev, file, ps]() {
+                           bool ok = prev.valid() ? prev.get() : true;
+                           for (const Piece& x : ps)
+                               if (fwrite(x.p, 1, x.n, file) != x.n) ok = false;
+                           return ok;
+                       }).share();
+            pend_[set][f] = last_[f];
         }
         if (rc && err->empty()) *err = "write failed";
         if (st) st->windows += nb;
@@ -965,11 +1113,34 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
 size_t ColumnsGpuWriter::device_bytes() const {
     size_t n = 0;
     for (int f = 0; f < 5; ++f) n += kCapHost[f] * (size_t)batch_cap_;
-    return n + (size_t)batch_cap_ * (kWin * 40 + 60) + (kWin + 2) + (size_t)len_tab_windows_ * 8;
+    return n + (size_t)batch_cap_ * (kWin * (40 + 28) + 64) + (kWin + 2) + (size_t)len_tab_windows_ * 8;
+}
+
+bool ColumnsGpuWriter::wait_set(int set) {
+    bool ok = true;
+    for (int f = 0; f < 5; ++f)
+        if (pend_[set][f].valid()) {
+            ok = pend_[set][f].get() && ok;
+            pend_[set][f] = std::shared_future<bool>();
+        }
+    return ok;
 }
 
 int ColumnsGpuWriter::close(std::string* err) {
     int rc = 0;
+    /* every write queued, in file order */
+    bool ok = true;
+    for (int f = 0; f < 5; ++f)
+        if (last_[f].valid()) {
+            ok = last_[f].get() && ok;
+            last_[f] = std::shared_future<bool>();
+        }
+    ok = wait_set(0) && ok;
+    ok = wait_set(1) && ok;
+    if (!ok) {
+        *err = "write failed";
+        rc = 1;
+    }
     for (FILE*& f : fb_)
         if (f) {
             if (fclose(f) != 0 && rc == 0) {

@@ -10,6 +10,8 @@
 
 #include <stdio.h>
 
+#include <future>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -62,7 +64,23 @@ private:
     int* d_fb_ = nullptr;
     uint64_t *d_sval_ = nullptr, *d_sdict_ = nullptr;
     uint32_t* d_saux_ = nullptr;
-    std::vector<char> host_buf_[5];
+    uint32_t* d_rle32_ = nullptr;
+    uint64_t* d_rle64_ = nullptr;
+    int* d_not_n_ = nullptr;
+    /* two sets of pinned buffers, a batch's blocks of each file, used in
+     * turn; the file writes of a batch run on their own threads, one per
+     * file, each after the same file's previous batch */
+    struct Piece {
+        const char* p;
+        size_t n;
+        std::shared_ptr<std::string> own;   /* a host-encoded block */
+    };
+    bool wait_set(int set);
+    char* hbuf_[2][5] = {};
+    size_t hcap_[2][5] = {};
+    int set_ = 0;
+    std::shared_future<bool> last_[5];
+    std::shared_future<bool> pend_[2][5];
 };
 
 /* One window of the -C files encoded on the host (the encoder of
