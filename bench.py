@@ -514,8 +514,8 @@ def main():
     peaks, peak_kind = load_peaks()
     bsite = site_bytes(w)
     names = {1: "call_tiles_kernel", 2: "call_fast_kernel", 3: "deferred_sites_kernel", 4: "call_stream_kernel",
-             5: "graph"}
-    dom_key = max((k for k in kernel_ms if k[0] in (1, 2, 4)), key=lambda k: sum(x[0] for x in kernel_ms[k]))
+             5: "graph", 6: "call_deep_kernel"}
+    dom_key = max((k for k in kernel_ms if k[0] in (1, 2, 4, 6)), key=lambda k: sum(x[0] for x in kernel_ms[k]))
     dom = kernel_ms[dom_key]
     dom_ms = statistics.mean(x[0] for x in dom)
     dom_sites = dom[0][1]

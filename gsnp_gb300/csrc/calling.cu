@@ -698,6 +698,274 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_fast_kernel(CallAr
 }
 
 /* ------------------------------------------------------------------------ */
+/* the deep bins of the FP32 form: one warp per site                          */
+/* ------------------------------------------------------------------------ */
+
+/* Tiles with a site of more than 64 records (hotspots of hundreds of reads)
+ * are called by a CTA of 32 warps, warp w calling site w of the tile, so that
+ * a site's hundreds of records are spread over 32 lanes instead of walked by
+ * one.  Per warp, in shared memory: the site's record column (at most 255
+ * records) and a byte counter per (base, strand, cycle) key. */
+constexpr int kDeepThreads = 32 * kTile;
+constexpr int kDeepCap = 256;
+constexpr int kDeepKeys = 4 * 2 * 256;
+constexpr size_t kDeepSmem = (size_t)kTile * (kDeepCap * 4 + kDeepKeys);
+
+/* The pileup of one site by its warp (kernel/update_kernel.cu:260-325, as
+ * PileupAcc::take): the reads [r_lo, r_hi) 32 at a time, in order.  A
+ * covering read counts in depth and repeat; one that is not N and reaches
+ * q_min is taken while the site has fewer than 255 unique records, and a
+ * unique one (hit 1) adds a record.  Whether the cap still admits a read
+ * depends only on the unique valid reads before it, which a ballot gives, so
+ * the 32 reads of a step are decided together with the reference's result.
+ * Once the cap is reached a read can only add to depth and repeat, which
+ * need no base or quality; the scan ends at the first step whose reads all
+ * start past the site. */
+__device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
+                                                  uint32_t* recs) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const signed char qmin = (signed char)a.qmin;
+    const int L = a.L;
+    SitePileup p;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        p.cu[b] = 0;
+        p.qs[b] = 0;
+        p.ca[b] = 0;
+    }
+    p.depth = 0;
+    p.repeat = 0;
+    p.dep_uni = 0;
+    p.num = 0;
+    for (int64_t rb = r_lo; rb < r_hi; rb += 32) {
+        const int64_t r = rb + lane;
+        bool cov = false;
+        uint32_t lh = 0, bq = 0;
+        int coord = -1, minus = 0;
+        const bool capped = p.dep_uni >= 0xFF;
+        if (r < r_hi) {
+            const int32_t start = __ldg(a.pos + r);
+            lh = (uint32_t)__ldg(a.lenhit + r);
+            coord = (int)(site - start);
+            cov = coord >= 0 && coord < (int)(lh >> 16);
+            if (cov && !capped) {
+                bq = __ldg(a.bq + r * L + coord);
+                minus = __ldg(a.strand + r) != '+';
+            }
+        }
+        if (__all_sync(kFull, coord < 0)) break;   /* every read from here on starts past the site */
+        const unsigned mc = __ballot_sync(kFull, cov);
+        if (mc == 0) continue;
+        const uint32_t hit = lh & 0xffffu;
+        p.depth += (uint32_t)__popc(mc);
+        p.repeat += __reduce_add_sync(kFull, cov ? hit : 0u);
+        if (capped) continue;
+        const signed char base = (signed char)(bq & 0xff);
+        const signed char qual = (signed char)(bq >> 8);
+        const bool valid = cov && base != 'N' && qual >= qmin;
+        const bool uni = valid && hit == 1;
+        const int uni_before = p.dep_uni + __popc(__ballot_sync(kFull, uni) & lt);
+        const bool acc = valid && uni_before < 0xFF;
+        const bool rec = acc && uni;
+        const unsigned mr = __ballot_sync(kFull, rec);
+        const int q = qual - qmin;
+        if (rec) {
+            const uint32_t cv = minus ? (uint32_t)((int)(lh >> 16) - 1 - coord) : (uint32_t)coord;
+            recs[p.num + __popc(mr & lt)] = make_record(base, q, cv, (uint32_t)minus);
+        }
+        p.num += __popc(mr);
+        p.dep_uni += __popc(mr);
+        const int bi = (base >> 1) & 3;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            p.cu[b] += __popc(__ballot_sync(kFull, rec && bi == b));
+            p.qs[b] += (int)__reduce_add_sync(kFull, (rec && bi == b) ? (uint32_t)q : 0u);
+            p.ca[b] += (uint32_t)__popc(__ballot_sync(kFull, acc && bi == b));
+        }
+    }
+    return p;
+}
+
+/* Ascending bitonic sort of v[0, n), n <= kDeepCap, by the lanes of a warp in
+ * shared memory (padded to a power of two with 0xFFFFFFFF, which no record
+ * word equals). */
+__device__ __forceinline__ void deep_sort(uint32_t* v, int n) {
+    const int lane = threadIdx.x & 31;
+    int P = 32;
+    while (P < n) P <<= 1;
+    for (int i = n + lane; i < P; i += 32) v[i] = 0xFFFFFFFFu;
+    __syncwarp();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int t = lane; t < P / 2; t += 32) {
+                const int i = 2 * j * (t / j) + (t % j), l = i + j;
+                const uint32_t x = v[i], y = v[l];
+                if ((x > y) == ((i & k) == 0)) {
+                    v[i] = y;
+                    v[l] = x;
+                }
+            }
+            __syncwarp();
+        }
+}
+
+/* The dependency walk and the FP32 sums of a sorted column by its warp,
+ * 32 records a step, record c0 + lane on that lane.  The walk's two counts
+ * (walk_records) come from the whole step at once:
+ *   - tmp, the earlier records of the same (base, strand, cycle) key: the
+ *     key's counter from the steps before plus the lower lanes with that key
+ *     (match-any); the highest of them then stores the new count;
+ *   - gdc, the first occurrences of a key (tmp = 0) so far in the record's
+ *     base group, less one: a ballot prefix, from the lane where the base
+ *     group starts, or carried over from the step before.
+ * Each lane sums its records' rows with compensation; the 32 sums are then
+ * added in a tree (the bound of fast_posterior's k_units 9). */
+__device__ __forceinline__ void deep_walk_sums(const CallArgs& a, const uint32_t* recs, uint8_t* cnt, int num,
+                                               float* s) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u, le = (lt << 1) | 1u;
+    for (int i = lane; i < kDeepKeys / 4; i += 32) reinterpret_cast<uint32_t*>(cnt)[i] = 0u;
+    __syncwarp();
+    Kahan10 k;
+    k.init();
+    int carry_firsts = 0, carry_base = -1;
+    for (int c0 = 0; c0 < num; c0 += 32) {
+        const int i = c0 + lane;
+        const bool valid = i < num;
+        const uint32_t w = valid ? recs[i] : 0u;
+        const int o = rec_base(w), coord = rec_coord(w);
+        const int key = valid ? (o << 9) | (rec_strand(w) << 8) | coord : kDeepKeys + lane;
+        const unsigned peers = __match_any_sync(kFull, key);
+        const int seen = valid ? (int)cnt[key] : 0;
+        __syncwarp();
+        const int tmp = seen + __popc(peers & lt);
+        if (valid && (peers >> lane) == 1u) cnt[key] = (uint8_t)(seen + __popc(peers));
+        __syncwarp();
+        const int prev_o = __shfl_up_sync(kFull, o, 1);
+        const bool brk = valid && o != (lane == 0 ? carry_base : prev_o);
+        const unsigned bm = __ballot_sync(kFull, brk) & le;
+        const unsigned fm = __ballot_sync(kFull, valid && tmp == 0) & le;
+        const int firsts = bm ? __popc(fm & ~((1u << (31 - __clz(bm))) - 1u)) : carry_firsts + __popc(fm);
+        carry_firsts = __shfl_sync(kFull, firsts, 31);
+        carry_base = __shfl_sync(kFull, o, 31);
+        if (valid) {
+            const int gdc = firsts - 1, t1 = tmp + 1;
+            const int qa = (t1 < a.tmax && gdc < a.gmax)
+                               ? (int)__ldg(a.qadj + ((size_t)t1 * a.gmax + gdc) * 65 + rec_q(w))
+                               : 1;
+            float x[10];
+            lik32_row(a, qa, coord, o, x);
+            k.add(x);
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < 10; ++v) {
+        float t = k.s[v];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) t = __fadd_rn(t, __shfl_xor_sync(kFull, t, d));
+        s[v] = t;
+    }
+}
+
+/* One deep tile: warp w calls site w (as fast_site: counts kept for later
+ * gap windows, the FP32 posterior, or the site deferred with its records). */
+__device__ __forceinline__ void deep_tile(const CallArgs& a, int64_t tile, uint32_t* recs, uint8_t* cnt) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t s0 = tile * kTile, site = s0 + w;
+    const int64_t sl = s0 + lane;
+    const uint8_t ori_l = sl < a.chr_len ? __ldg(a.ori + sl) : 0;
+    const unsigned flagged = __ballot_sync(kFull, (ori_l & 8) != 0);
+    if (site >= a.chr_len) return;
+    const uint8_t ori = (uint8_t)__shfl_sync(kFull, ori_l, w);
+    const int32_t snp_row = (ori & 8) ? a.tile_snp[tile] + __popc(flagged & ((1u << w) - 1u)) : -1;
+    const uint8_t wflags = a.win_flags[s0 / kWin];
+    const SitePileup p = deep_pileup(a, a.warp_rng[tile * 2], a.warp_rng[tile * 2 + 1], site, recs);
+    __syncwarp();
+    deep_sort(recs, p.num);
+    float s[10];
+    deep_walk_sums(a, recs, cnt, p.num, s);
+    uint8_t dflags = 0;
+    if (lane == 0) {
+        if (p.depth > 0xffff) atomicExch(a.error, 1);
+        if (wflags & kWinKeepCounts) store_counts(a, site, p);
+        SiteCall call;
+        if ((site & 4095) == 0 && a.stats) dflags = kCallSampled;
+        const bool empty = p.num == 0 && (p.ca[0] | p.ca[1] | p.ca[2] | p.ca[3]) == 0 && a.empty_valid[ori];
+        if (empty) {
+            call = a.empty_calls[ori];
+            call.depth = p.depth;
+            call.repeat_time = p.repeat;
+            call.flags |= dflags;
+        } else if (fast_posterior(a, snp_row, ori, p, s, p.num, &call, 9.0f)) {
+            call.flags |= dflags;
+        } else {
+            call = SiteCall{};
+            dflags |= kCallPending;
+            call.flags = dflags;
+        }
+        a.out[site] = call;
+    }
+    dflags = (uint8_t)__shfl_sync(kFull, dflags, 0);
+    if (!dflags) return;
+    /* the site and its sorted records to the deferred pool */
+    unsigned long long slot = 0, off = 0;
+    if (lane == 0) {
+        slot = atomicAdd(a.dcount, 1ull);
+        off = atomicAdd(a.dcount + 1, (unsigned long long)p.num);
+    }
+    slot = __shfl_sync(kFull, slot, 0);
+    off = __shfl_sync(kFull, off, 0);
+    if ((int64_t)slot >= a.dsite_cap || (int64_t)(off + p.num) > a.dpool_cap) return;
+    for (int i = lane; i < p.num; i += 32) a.dpool[off + i] = recs[i];
+    if (lane == 0) {
+        DeferredSite d;
+        d.site = site;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            d.cu[b] = (uint16_t)p.cu[b];
+            d.qs[b] = (uint16_t)p.qs[b];
+            d.ca[b] = p.ca[b];
+        }
+        d.depth = p.depth;
+        d.repeat = p.repeat;
+        d.rec_off = (uint32_t)off;
+        d.num = (uint16_t)p.num;
+        d.dep_uni = (uint16_t)p.dep_uni;
+        d.snp_row = snp_row;
+        d.flags = dflags;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) d.pad[b] = 0;
+        a.dsites[slot] = d;
+    }
+}
+
+/* The tiles of a deep FP32 bin: tiles[blockIdx.x] with count == nullptr, else
+ * the first *count tiles of the list handed out from *next (zero before the
+ * launch), one tile per CTA at a time. */
+__global__ void __launch_bounds__(kDeepThreads, 1) call_deep_kernel(CallArgs a, const int32_t* __restrict__ tiles,
+                                                                    const int* __restrict__ count, int* next) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const int w = threadIdx.x >> 5;
+    uint32_t* recs = reinterpret_cast<uint32_t*>(smem) + (size_t)w * kDeepCap;
+    uint8_t* cnt = smem + (size_t)kTile * kDeepCap * 4 + (size_t)w * kDeepKeys;
+    __shared__ int s_next;
+    if (!count) {
+        deep_tile(a, tiles[blockIdx.x], recs, cnt);
+        return;
+    }
+    const int n = *count;
+    int i = blockIdx.x;
+    while (i < n) {
+        deep_tile(a, tiles[i], recs, cnt);
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = atomicAdd(next, 1) + (int)gridDim.x;
+        __syncthreads();
+        i = s_next;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* the persistent FP32 calling kernel                                        */
 /* ------------------------------------------------------------------------ */
 
@@ -1063,16 +1331,19 @@ cudaError_t launch_stream(const CallArgs& a, const StreamQueue& q, int slots, in
  * default); with ctas_per_sm, its resident CTAs on one SM */
 template <int SLOTS>
 static cudaError_t bin_attr(int kind, int L, int carveout, int* ctas_per_sm) {
-    const int smem = (int)call_smem_bytes(SLOTS, L, kind == kKindFast);
-    const void* fn = kind == kKindFast ? reinterpret_cast<const void*>(call_fast_kernel<SLOTS>)
-                                       : reinterpret_cast<const void*>(call_tiles_kernel<SLOTS>);
+    /* the FP32 form's deep bins run one warp per site (call_deep_kernel) */
+    const bool deep = kind == kKindFast && SLOTS >= kDeepSlots;
+    const int smem = deep ? (int)kDeepSmem : (int)call_smem_bytes(SLOTS, L, kind == kKindFast);
+    const void* fn = deep                ? reinterpret_cast<const void*>(call_deep_kernel)
+                     : kind == kKindFast ? reinterpret_cast<const void*>(call_fast_kernel<SLOTS>)
+                                         : reinterpret_cast<const void*>(call_tiles_kernel<SLOTS>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     /* the carveout is a hint: a refusal only costs speed, and its error is
      * cleared so that it is not taken for the launch's */
     if (carveout > 0 && cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carveout) != cudaSuccess)
         (void)cudaGetLastError();
-    if (ctas_per_sm) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, kTile, smem);
+    if (ctas_per_sm) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, fn, deep ? kDeepThreads : kTile, smem);
     return cudaSuccess;
 }
 
@@ -1084,7 +1355,9 @@ static cudaError_t launch_one(const CallArgs& a, int kind, const int32_t* tiles,
     const int smem = (int)call_smem_bytes(SLOTS, a.L, kind == kKindFast);
     const unsigned grid = (unsigned)(bl.d_count ? bl.grid : bl.count);
     if (grid == 0) return cudaSuccess;
-    if (kind == kKindFast) call_fast_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count, bl.d_next);
+    if (kind == kKindFast && SLOTS >= kDeepSlots)
+        call_deep_kernel<<<grid, kDeepThreads, kDeepSmem, stream>>>(a, tiles, bl.d_count, bl.d_next);
+    else if (kind == kKindFast) call_fast_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count, bl.d_next);
     else call_tiles_kernel<SLOTS><<<grid, kTile, smem, stream>>>(a, tiles, bl.d_count, bl.d_next);
     return cudaGetLastError();
 }

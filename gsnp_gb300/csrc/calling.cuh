@@ -30,6 +30,7 @@ enum CallKind : int {
     kKindDeferred = 3,  /* FP64 pass over the sites the fast kernel deferred */
     kKindStream = 4,    /* the persistent FP32 kernel over a segment's tiles */
     kKindGraph = 5,     /* a whole pass replayed as a CUDA graph */
+    kKindDeep = 6,      /* FP32, one warp per site: the deep bins' tiles */
 };
 
 /* A site the fast kernel left to the FP64 pass: its pileup counts and the
@@ -54,6 +55,14 @@ enum WindowFlags : uint8_t {
     kWinKeepLik = 2,      /* a later window reuses this window's likelihood */
     kWinExternalLik = 4,  /* likelihood comes from another window (or zeros) */
 };
+
+/* FP32 bins of at least this many record slots are called one warp per
+ * site (call_deep_kernel).  At c2 (hotspots of 300-1000x) the warp form took
+ * the 256-slot bin from 26.9 to 17.9 ms, but the 96- and 128-slot bins from
+ * 2.8 and 4.7 to 12.0 and 13.4 ms: below 255 records the lanes of a warp
+ * sharing one scan of the tile's reads (one site each) beat a warp re-scanning
+ * them per site. */
+constexpr int kDeepSlots = 256;
 
 /* tiles a warp of the persistent FP32 kernel takes per counter increment */
 constexpr int kStreamChunk = 2;

@@ -68,6 +68,10 @@ T* based(T* p, int64_t first) {
 struct StreamRing;
 void ring_free(StreamRing* g);
 
+/* the launch record kind of a bin's kernel (the FP32 deep bins run
+ * call_deep_kernel) */
+inline int launch_kind(int kind, int slots) { return kind == kKindFast && slots >= kDeepSlots ? kKindDeep : kind; }
+
 /* a site decided by the deferred pass and its call */
 struct DeferredCall {
     int64_t site;
@@ -968,7 +972,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             for (int j = 0; j < m; ++j) {
                 const int b = order[j];
                 const int nb = c->h_bin_count[base + b];
-                const int k = begin(kind, bin_slots(b), nb);
+                const int k = begin(launch_kind(kind, bin_slots(b)), bin_slots(b), nb);
                 const BinLaunch bl{nb, nullptr, 0, c->bin_carveout[kind == kKindFast][b]};
                 CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * c->tiles_cap, bl, c->stream),
                    "calling kernel");
@@ -983,7 +987,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
             const int b = order[j];
             cudaStream_t st = c->bin_stream[j % ns];
             const int nb = c->h_bin_count[base + b];
-            const int k = begin_on(kind, bin_slots(b), nb, st);
+            const int k = begin_on(launch_kind(kind, bin_slots(b)), bin_slots(b), nb, st);
             const BinLaunch bl{nb, nullptr, 0, c->bin_carveout[kind == kKindFast][b]};
             CK(launch_bin(with_scratch(b), kind, b, c->d_bin_tiles + (int64_t)(base + b) * c->tiles_cap, bl, st),
                "calling kernel");
@@ -1187,7 +1191,7 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
                 if (kind == kKindFast && use_stream && kSlotsOf(b) <= c->stream_slots) continue;
                 const BinLaunch bl{0, c->d_bin_count + ki * kNumBins + b, c->bin_grid[ki][b], c->bin_carveout[ki][b],
                                    c->d_bin_count + (2 + ki) * kNumBins + b};
-                const int kb = begin(kind, kSlotsOf(b), 0);
+                const int kb = begin(launch_kind(kind, kSlotsOf(b)), kSlotsOf(b), 0);
                 CK(launch_bin(a, kind, b, c->d_bin_tiles + (int64_t)(ki * kNumBins + b) * c->tiles_cap, bl, c->stream),
                    "calling kernel");
                 end(kb);

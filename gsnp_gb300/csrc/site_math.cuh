@@ -474,9 +474,12 @@ __device__ bool site_posterior(const CallArgs& a, uint8_t ori, const SitePileup&
 
 /* The FP32 posterior of the fast kernel, for sites whose best genotype is
  * homozygous (the rank-sum value is then 1 and its log10 0).  s holds the FP32
- * likelihood sums by table column, num the record count.  Returns false,
- * writing nothing, when the best genotype is heterozygous or when the FP32
- * values do not prove the FP64 decisions.
+ * likelihood sums by table column, num the record count, and
+ * k_units u + num 2^-45 (u = 2^-24) their relative error bound: 6 for the
+ * grouping of likelihood_fp32, 9 for the warp form of the deep kernel (per-
+ * lane compensated sums, then a tree of 32).  Returns false, writing
+ * nothing, when the best genotype is heterozygous or when the FP32 values do
+ * not prove the FP64 decisions.
  *
  * E_g bounds |tp32[g] - tp64[g]| (the likelihood bound, the FP32 rounding of
  * the prior and of the addition).  With v1 = tp32[type1], v2 the largest
@@ -489,7 +492,7 @@ __device__ bool site_posterior(const CallArgs& a, uint8_t ori, const SitePileup&
  * is relative to these small values; the bounds are then grown to cover
  * those roundings. */
 __device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t snp_row, uint8_t ori, const SitePileup& p,
-                                               const float* s, int num, SiteCall* out) {
+                                               const float* s, int num, SiteCall* out, float k_units = 6.0f) {
     const int ori7 = ori & 7;
     const float* src = a.log_prior32 + ori7 * 12;
     if ((ori & 0x8) && a.refine) src = a.snp_lp32 + snp_row * 12;
@@ -504,7 +507,7 @@ __device__ __forceinline__ bool fast_posterior(const CallArgs& a, int64_t snp_ro
     /* |s - S64| <= |s| k; the prior's rounding <= 2^-24 |lp|; the addition's
      * <= 2^-24 |tp| <= 2^-24 (|s| + |lp|); grown by 2^-20 for the rounding of
      * the bound itself */
-    const float kk1 = __fadd_rn(__fadd_rn(6.0f * 0x1p-24f, __fmul_rn((float)num, 0x1p-45f)), 0x1p-23f);
+    const float kk1 = __fadd_rn(__fadd_rn(k_units * 0x1p-24f, __fmul_rn((float)num, 0x1p-45f)), 0x1p-23f);
     const float grow = 1.0f + 0x1p-20f;
     float tp[10], E[10];
     int t1 = -1;

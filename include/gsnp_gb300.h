@@ -254,9 +254,11 @@ int gsnp_check_columns(const char* cns_path, const char* base, char* report, int
  * context's stream. */
 typedef struct gsnp_launch_info {
     int kind;          /* 0: tile classification; calling kernel of one depth bin: 1 FP64,
-                          2 FP32 fast form, 3 FP64 pass over the fast form's deferred sites */
+                          2 FP32 fast form, 6 FP32 fast form with one warp per site (the deep
+                          bins); 3 FP64 pass over the fast form's deferred sites; 4 the
+                          persistent FP32 kernel; 5 a whole pass replayed as a CUDA graph */
     int slots;         /* record slots per site of the bin (calling kernels) */
-    int64_t tiles;     /* 128-site tiles processed */
+    int64_t tiles;     /* 32-site tiles processed (0 when the count is read on the device) */
     int64_t sites;
     float ms;          /* device time of the launch */
 } gsnp_launch_info;
