@@ -6,7 +6,10 @@
  *
  *  1. likelihood_fp32 stays within its bound: |S32 - S64| <= eps for every
  *     genotype, S64 being likelihood_fp64's sums in the reference's record
- *     order and eps = |S32| GSNP_FP32_K(num);
+ *     order and eps = |S32| GSNP_FP32_K(num); and so do the sums of the deep
+ *     kernel's warp form (record i on lane i mod 32, compensated per lane,
+ *     the 32 lane sums then added by an xor butterfly) within
+ *     |S32| (9 u + num 2^-45), the bound fast_posterior takes for them;
  *  2. every call decided from the FP32 sums equals the FP64 posterior's
  *     (site_posterior over S64):
  *       fast_posterior (the fast kernel's homozygous calls), and
@@ -188,6 +191,35 @@ int main(int argc, char** argv) {
                 printf("site %ld: genotype %d: |S32 - S64| = %.3g above the bound %.3g (num %d)\n", site, g, d,
                        eps[g], sp.num);
                 return 1;
+            }
+        }
+        {
+            /* the warp form of call_deep_kernel over the same walk */
+            std::vector<Kahan10> lane(32);
+            for (Kahan10& k : lane) k.init();
+            walk_records<false, 2>(a, recs.data(), seen.data(), 1, sp.num, [&](int i, int qa, int coord, int o) {
+                float x[10];
+                lik32_row(a, qa, coord, o, x);
+                lane[(size_t)(i & 31)].add(x);
+            });
+            float t[32][10];
+            for (int l = 0; l < 32; ++l)
+                for (int v = 0; v < 10; ++v) t[l][v] = lane[(size_t)l].s[v];
+            for (int d = 16; d > 0; d >>= 1) {
+                float u[32][10];
+                for (int l = 0; l < 32; ++l)
+                    for (int v = 0; v < 10; ++v) u[l][v] = __fadd_rn(t[l][v], t[l ^ d][v]);
+                memcpy(t, u, sizeof t);
+            }
+            const double kw = 9.0 * 0x1p-24 + (double)sp.num * 0x1p-45;
+            for (int k = 0; k < 10; ++k) {
+                const int g = genotype_of(k);
+                const double sw = (double)t[0][k], d = fabs(sw - tl64[g]);
+                if (!(d <= fabs(sw) * kw) && !isinf(sw)) {
+                    printf("site %ld: genotype %d: warp form |S32 - S64| = %.3g above %.3g (num %d)\n", site, g, d,
+                           fabs(sw) * kw, sp.num);
+                    return 1;
+                }
             }
         }
         a.monoploid = site % 10 == 0;   /* -m: homozygous genotypes only */
