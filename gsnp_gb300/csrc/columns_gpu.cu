@@ -51,7 +51,11 @@ namespace {
 constexpr int kEncThreads = 1024;
 constexpr int kBitmapBits = kWin + 64;                /* value span of an integer dictionary */
 constexpr int kBitmapWords = kBitmapBits / 32;
-constexpr int kHashCap = 4096;                        /* slots of the double hash set */
+/* slots of the double hash set: 128 KB of shared memory, which costs the
+ * encoder no occupancy (its 1024-thread CTAs take every register of an SM);
+ * with 4096 slots, the repeat / depth column of windows of varied depth (c2's
+ * copy-number segments and hotspots) overflowed and went to the host */
+constexpr int kHashCap = 16384;
 constexpr int kHashMax = kHashCap / 2;                /* distinct doubles a column may have */
 constexpr unsigned long long kEmptyKey = ~0ull;       /* a NaN pattern, never a value */
 
@@ -818,6 +822,7 @@ __global__ void __launch_bounds__(kEncThreads) encode_windows_kernel(EncArgs e) 
 }
 
 constexpr size_t kEncSmem = 2 * kBitmapWords * 4 + kHashCap * 8;
+static_assert(kEncSmem <= 220 * 1024, "the encoder's shared memory fits one CTA per SM");
 
 #define CKE(x, what)                                                      \
     do {                                                                  \
@@ -960,7 +965,6 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
     cudaError_t ce = cudaSuccess;
     std::vector<uint64_t> h_len((size_t)(5 * batch_cap_));
     std::vector<int> h_fb5((size_t)(5 * batch_cap_)), h_fb((size_t)batch_cap_);
-    HostDictCodec dict;
     for (int64_t b0 = w0; b0 < w1 && rc == 0; b0 += batch_cap_) {
         const int64_t nb = std::min(batch_cap_, w1 - b0);
         EncArgs e;
@@ -1047,11 +1051,53 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
             rc = 1;
             break;
         }
+        /* the windows the encoder left to the host, encoded on host threads
+         * (a window each) while the pieces are assembled */
+        struct HostWindow {
+            std::string parts[5];
+            std::string err;
+            bool ok = false;
+        };
+        const int dev = [] {
+            int d = 0;
+            cudaGetDevice(&d);
+            return d;
+        }();
+        std::vector<std::future<std::shared_ptr<HostWindow>>> host_win((size_t)nb);
+        for (int64_t b = 0; b < nb; ++b) {
+            if (!h_fb[(size_t)b]) continue;
+            if (st) ++st->host_windows;
+            const int64_t w = b0 + b;
+            host_win[(size_t)b] = std::async(std::launch::async, [=, &plan]() {
+                auto hw = std::make_shared<HostWindow>();
+                cudaSetDevice(dev);
+                const int64_t len = plan.call_len[(size_t)w];
+                std::vector<SiteCall> calls((size_t)len);
+                std::vector<SiteCounts> counts;
+                cudaError_t e2 =
+                    cudaMemcpy(calls.data(), d_calls + w * (int64_t)kWin, sizeof(SiteCall) * len, cudaMemcpyDeviceToHost);
+                const int32_t src = h_host_src[w];
+                if (e2 == cudaSuccess && src >= 0 && src != w && d_counts) {
+                    counts.resize((size_t)len);
+                    e2 = cudaMemcpy(counts.data(), d_counts + (int64_t)src * kWin, sizeof(SiteCounts) * len,
+                                    cudaMemcpyDeviceToHost);
+                }
+                if (e2 != cudaSuccess) {
+                    hw->err = std::string("-C encoder download: ") + cudaGetErrorString(e2);
+                    return hw;
+                }
+                HostDictCodec codec;
+                hw->ok = encode_window_host(len, src >= 0 && src != w ? 1 : (src == w ? 0 : -1),
+                                            h_codes + w * (int64_t)kWin, calls.data(),
+                                            counts.empty() ? nullptr : counts.data(), codec, hw->parts, &hw->err);
+                return hw;
+            });
+        }
         /* each file's pieces in window order: the encoder's blocks, and the
-         * windows it left to the host, encoded here */
+         * host-encoded windows in their places */
         std::vector<Piece> pieces[5];
         size_t wo[5] = {};
-        for (int64_t b = 0; b < nb && rc == 0; ++b) {
+        for (int64_t b = 0; b < nb; ++b) {
             if (!h_fb[(size_t)b]) {
                 for (int f = 0; f < 5; ++f) {
                     const size_t bytes = (size_t)h_len[(size_t)(5 * b + f)];
@@ -1060,32 +1106,15 @@ int ColumnsGpuWriter::write(int64_t w0, int64_t w1, const uint8_t* d_codes, cons
                 }
                 continue;
             }
-            if (st) ++st->host_windows;
-            const int64_t w = b0 + b;
-            const int64_t len = plan.call_len[(size_t)w];
-            std::vector<SiteCall> calls((size_t)len);
-            std::vector<SiteCounts> counts;
-            ce = cudaMemcpy(calls.data(), d_calls + w * (int64_t)kWin, sizeof(SiteCall) * len, cudaMemcpyDeviceToHost);
-            const int32_t src = h_host_src[w];
-            if (ce == cudaSuccess && src >= 0 && src != w && d_counts) {
-                counts.resize((size_t)len);
-                ce = cudaMemcpy(counts.data(), d_counts + (int64_t)src * kWin, sizeof(SiteCounts) * len,
-                                cudaMemcpyDeviceToHost);
-            }
-            if (ce != cudaSuccess) {
-                *err = std::string("-C encoder download: ") + cudaGetErrorString(ce);
+            std::shared_ptr<HostWindow> hw = host_win[(size_t)b].get();
+            if (!hw->ok) {
+                if (rc == 0) *err = hw->err;
                 rc = 1;
-                break;
-            }
-            std::string parts[5];
-            if (!encode_window_host(len, src >= 0 && src != w ? 1 : (src == w ? 0 : -1), h_codes + w * (int64_t)kWin,
-                                    calls.data(), counts.empty() ? nullptr : counts.data(), dict, parts, err)) {
-                rc = 1;
-                break;
+                continue;
             }
             for (int f = 0; f < 5; ++f)
-                if (!parts[f].empty()) {
-                    auto own = std::make_shared<std::string>(std::move(parts[f]));
+                if (!hw->parts[f].empty()) {
+                    auto own = std::make_shared<std::string>(std::move(hw->parts[f]));
                     pieces[f].push_back(Piece{own->data(), own->size(), own});
                 }
         }

@@ -488,6 +488,7 @@ struct gsnp_context {
     int bin_grid[2][kNumBins] = {};
     int grid_L = -1, deferred_grid = 0, classify_grid = 0, sms = 0;
     unsigned long long* d_dmax = nullptr;   /* [2] largest deferred request of the call's segments */
+    int* d_bin_hist = nullptr;              /* [2][2 * kNumBins] bin counts of each pass (launch records) */
     cudaGraphExec_t graph_exec = nullptr;
     cudaStream_t capture_stream = nullptr;
     uint64_t graph_key = 0;
@@ -503,6 +504,7 @@ struct gsnp_context {
     static const int kMaxLaunches = 128;
     cudaEvent_t ev[2 * kMaxLaunches] = {};
     gsnp_launch_info launches[kMaxLaunches];
+    int launch_ref[kMaxLaunches] = {};   /* a device-driven bin launch: its count in d_bin_hist, else -1 */
     int n_launches = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;
     /* the call's copy streams: uploads in chunks, downloads per segment */
@@ -647,7 +649,8 @@ constexpr size_t kMapError = 96;     /* int */
 constexpr size_t kMapGerror = 100;   /* int */
 constexpr size_t kMapLeftover = 104; /* int */
 constexpr size_t kMapStats = 128;    /* unsigned long long[kNumStats] */
-constexpr size_t kMapWindows = 256;  /* the call's window tables */
+constexpr size_t kMapBinHist = 256;  /* int[2][2 * kNumBins]: each pass's bin counts */
+constexpr size_t kMapWindows = 512;  /* the call's window tables */
 static_assert(sizeof(int) * 2 * kNumBins <= kMapDcount, "bin counts overlap the deferred counts");
 
 int ensure_map(gsnp_context* c, size_t bytes) {
@@ -684,7 +687,7 @@ void free_all(gsnp_context* c) {
                     c->d_text, c->d_chr, c->d_tile_snp, c->d_tile_rng, c->d_empty_calls, c->d_empty_valid,
                     c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq, c->d_raw_qual,
                     c->d_idx, c->d_dep_off, c->d_gerror, c->d_deep, c->d_stream_ctl, c->d_leftover,
-                    c->d_dmax, c->d_patch};
+                    c->d_dmax, c->d_patch, c->d_bin_hist};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -843,6 +846,10 @@ int prepare_calling(gsnp_context* c) {
     }
     if (c->device_driven) {
         if (!c->d_dmax) CK(dev_alloc(&c->d_dmax, 2), "cudaMalloc");
+        if (!c->d_bin_hist) {
+            CK(dev_alloc(&c->d_bin_hist, 4 * kNumBins), "cudaMalloc");
+            CK(cudaMemset(c->d_bin_hist, 0, sizeof(int) * 4 * kNumBins), "memset");
+        }
         if (c->grid_L != c->params.read_length) {
             /* grids of the device-driven launches: the resident CTAs */
             CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device), "device attribute");
@@ -873,7 +880,18 @@ int finish_device(gsnp_context* c) {
     CK(to_map(c, c->d_error, kMapError, sizeof(int)), "error flag");
     CK(to_map(c, c->d_stats, kMapStats, sizeof(c->stats)), "stats");
     CK(to_map(c, c->d_dmax, kMapDcount, sizeof(c->h_dcount)), "deferred counts");
+    if (c->d_bin_hist) CK(to_map(c, c->d_bin_hist, kMapBinHist, sizeof(int) * 4 * kNumBins), "bin counts");
     CK(cudaStreamSynchronize(c->stream), "calling");
+    if (c->d_bin_hist) {
+        /* the tiles each recorded bin launch took, now that they are known */
+        int hist[4 * kNumBins];
+        memcpy(hist, c->h_map + kMapBinHist, sizeof hist);
+        for (int k = 0; k < c->n_launches; ++k)
+            if (c->launch_ref[k] >= 0) {
+                c->launches[k].tiles = hist[c->launch_ref[k]];
+                c->launches[k].sites = std::min<int64_t>((int64_t)hist[c->launch_ref[k]] * kTile, c->chr_len);
+            }
+    }
     int err = 0;
     memcpy(&err, c->h_map + kMapError, sizeof(int));
     memcpy(c->stats, c->h_map + kMapStats, sizeof(c->stats));
@@ -926,6 +944,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         c->launches[k].tiles = tiles;
         c->launches[k].sites = std::min<int64_t>(tiles * kTile, c->chr_len);
         c->launches[k].ms = 0.f;
+        c->launch_ref[k] = -1;
         cudaEventRecord(c->ev[2 * k], c->stream);
         return k;
     };
@@ -1135,6 +1154,7 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
         c->launches[k].tiles = tiles;
         c->launches[k].sites = std::min<int64_t>(tiles * kTile, c->chr_len);
         c->launches[k].ms = 0.f;
+        c->launch_ref[k] = -1;
         cudaEventRecord(c->ev[2 * k], c->stream);
         return k;
     };
@@ -1192,11 +1212,11 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
                 const BinLaunch bl{0, c->d_bin_count + ki * kNumBins + b, c->bin_grid[ki][b], c->bin_carveout[ki][b],
                                    c->d_bin_count + (2 + ki) * kNumBins + b};
                 const int kb = begin(launch_kind(kind, kSlotsOf(b)), kSlotsOf(b), 0);
+                if (kb >= 0) c->launch_ref[kb] = pass * 2 * kNumBins + ki * kNumBins + b;
                 CK(launch_bin(a, kind, b, c->d_bin_tiles + (int64_t)(ki * kNumBins + b) * c->tiles_cap, bl, c->stream),
                    "calling kernel");
                 end(kb);
             }
-            (void)pass;
             return GSNP_OK;
         };
         /* pass 0 */
@@ -1216,6 +1236,9 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
             CK(launch_classify(a, 0, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
         }
         end(k);
+        CK(cudaMemcpyAsync(c->d_bin_hist, c->d_bin_count, sizeof(int) * 2 * kNumBins, cudaMemcpyDeviceToDevice,
+                           c->stream),
+           "bin counts");
         if (!fast || keep_lik) {
             const int rc = bins(kKindFP64, 0);
             if (rc != GSNP_OK) return rc;
@@ -1238,6 +1261,9 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
             else
                 CK(launch_classify(a, 1, g.t0, g.t1, c->d_bin_count, c->d_bin_tiles, c->stream), "classify kernel");
             end(kc);
+            CK(cudaMemcpyAsync(c->d_bin_hist + 2 * kNumBins, c->d_bin_count, sizeof(int) * 2 * kNumBins,
+                               cudaMemcpyDeviceToDevice, c->stream),
+               "bin counts");
             const int rc = bins(kKindFP64, 1);
             if (rc != GSNP_OK) return rc;
         }
