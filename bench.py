@@ -81,6 +81,23 @@ def dist_info():
     return rank, world, local
 
 
+def replica_max(dist, x, device="cuda"):
+    """The largest x over the ranks (x itself without a process group): each
+    rank times its own replica, and the job's step takes the slowest."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world, units_per_rank, seconds):
+    """Whole-job rate of replicas: every rank's units over the slowest rank's
+    time (per-rank work fixed as ranks are added: weak scaling)."""
+    return world * units_per_rank / seconds
+
+
 class ClockSampler:
     """nvidia-smi clock and throttle samples during the timed region."""
 
@@ -324,11 +341,7 @@ def main():
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_max(dist, x)
 
     def time_form(prec):
         """Per-kernel times from passes launched one kernel at a time (each
@@ -358,7 +371,7 @@ def main():
         torch.cuda.synchronize()
         barrier()
         ms_step = max_over_ranks(start.elapsed_time(end)) / args.steps
-        return {"ms_step": ms_step, "value": world * sites / (ms_step / 1000.0), "launches": n_launch,
+        return {"ms_step": ms_step, "value": replica_rate(world, sites, ms_step / 1000.0), "launches": n_launch,
                 "kernel_ms": kernel_ms, "stats": caller.stats()}
 
     compare = time_form(other) if not args.no_compare else None
@@ -384,7 +397,7 @@ def main():
     # median step: the host link is shared with the other GPUs of the machine,
     # and a step that meets their traffic is reported in step_ms, not averaged in
     e2e_s = max_over_ranks(max(statistics.median(e2e_times), 1e-9))
-    e2e_value = world * sites / e2e_s
+    e2e_value = replica_rate(world, sites, e2e_s)
 
     # ---- end to end with the cns text, the output the reference's pass writes ----
     # each step: upload and call (gsnp_call_chromosome), then the text of every
