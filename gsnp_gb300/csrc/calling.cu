@@ -250,12 +250,26 @@ __device__ int neighbour_qsum(const CallArgs& a, int64_t site, int b) {
     const int64_t p = site + 1;
     const int64_t win_end = (site / kWin + 1) * (int64_t)kWin;
     const int64_t max_start = (p == win_end) ? win_end - 1 : p;
-    const int64_t lo = a.read_lo + lower_bound_g(a.pos + a.read_lo, a.n_reads - a.read_lo, p - a.L + 1);
-    const int64_t hi = a.read_lo + lower_bound_g(a.pos + a.read_lo, a.n_reads - a.read_lo, max_start + 1);
+    const int64_t t = p / kTile;
+    int64_t lo, hi;
+    if (p < win_end && t >= a.tile_lo && t < a.n_tiles) {
+        /* p's tile's read range, [lower_bound(32 t - L + 1), lower_bound(32 t
+         * + 32)): the same reads in the same order and a few more, which the
+         * checks below skip, without two searches over every read.  (The
+         * window's end is left to the searches: its next site can lie in a
+         * tile the pass has not ranged.) */
+        lo = a.tile_rng[t * 2];
+        hi = a.tile_rng[t * 2 + 1];
+    } else {
+        lo = a.read_lo + lower_bound_g(a.pos + a.read_lo, a.n_reads - a.read_lo, p - a.L + 1);
+        hi = a.read_lo + lower_bound_g(a.pos + a.read_lo, a.n_reads - a.read_lo, max_start + 1);
+    }
     int dep_uni = 0, qsum = 0;
     const signed char qmin = (signed char)a.qmin;
     for (int64_t r = lo; r < hi; ++r) {
-        const int coord = (int)(p - __ldg(a.pos + r));
+        const int64_t start = __ldg(a.pos + r);
+        if (start > max_start) break;   /* the starts ascend */
+        const int coord = (int)(p - start);
         const uint32_t lh = (uint32_t)__ldg(a.lenhit + r);
         if (coord >= (int)(lh >> 16)) continue;
         const uint16_t bq = __ldg(a.bq + r * a.L + coord);
@@ -1159,6 +1173,121 @@ __global__ void __launch_bounds__(kTile, kFastCtasPerSm) call_stream_kernel(Call
     }
 }
 
+/* The adjusted-quality table index of every record of a sorted column whose
+ * records have occurrence 1 (the deferred pool's), or -1 where q_adj is 1:
+ * walk_records' counts with BITS per key, without its table loads, so that
+ * the loads can be issued many at a time afterwards. */
+template <int BITS>
+__device__ void walk_qidx(const CallArgs& a, const uint32_t* recs, uint32_t* seen, int num, int* qidx) {
+    constexpr int kPer = 32 / BITS;
+    constexpr uint32_t kMax = (1u << BITS) - 1u;
+    const int L = a.L;
+    const int nw = pcr_words(L, BITS);
+    const bool sat_exact = BITS == 4 && a.tmax <= 16;
+    int gdc = -1, last_o = -1, gstart = 0;
+    for (int i = 0; i < num; ++i) {
+        const uint32_t w = recs[i];
+        const int o = rec_base(w);
+        const int key = rec_strand(w) * L + rec_coord(w);
+        if (o != last_o) {
+            for (int k = 0; k < nw; ++k) seen[k] = 0u;
+            gstart = i;
+            gdc = -1;
+            last_o = o;
+        }
+        uint32_t* cw = seen + key / kPer;
+        const int sh = (key % kPer) * BITS;
+        const uint32_t word = *cw;
+        const uint32_t cnt = (word >> sh) & kMax;
+        int tmp = (int)cnt;
+        if (cnt == kMax && !sat_exact) {
+            tmp = 0;
+            for (int j = gstart; j < i; ++j)
+                if (((recs[j] ^ w) & 0x1ff00u) == 0) tmp += 1;
+        }
+        if (cnt != kMax) *cw = (word & ~(kMax << sh)) | ((cnt + 1u) << sh);
+        if (tmp == 0) gdc += 1;
+        tmp++;
+        qidx[i] = (tmp < a.tmax && gdc < a.gmax) ? (tmp * a.gmax + gdc) * 65 + rec_q(w) : -1;
+    }
+}
+
+/* adjusted quality of record i from walk_qidx's index */
+__device__ __forceinline__ int qa_of(const CallArgs& a, const int* qidx, int i) {
+    return qidx[i] >= 0 ? (int)__ldg(a.qadj + qidx[i]) : 1;
+}
+
+/* likelihood_fp32's sums from walk_qidx's indices: four records' loads at a
+ * time, added in the same grouping ((x0 + x1) + (x2 + x3)) and compensation,
+ * so the values are those of likelihood_fp32 and of the fast kernels */
+__device__ void deferred_fp32(const CallArgs& a, const uint32_t* recs, const int* qidx, int num, double* tl,
+                              double* eps) {
+    Kahan10 k;
+    k.init();
+    for (int i = 0; i < num; i += 4) {
+        int qa[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) qa[u] = i + u < num ? qa_of(a, qidx, i + u) : 1;
+        float x[10], y[10];
+        lik32_row(a, qa[0], rec_coord(recs[i]), rec_base(recs[i]), x);
+        if (i + 1 < num) {
+            lik32_row(a, qa[1], rec_coord(recs[i + 1]), rec_base(recs[i + 1]), y);
+#pragma unroll
+            for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
+        }
+        if (i + 2 < num) {
+            float z[10];
+            lik32_row(a, qa[2], rec_coord(recs[i + 2]), rec_base(recs[i + 2]), y);
+            if (i + 3 < num) {
+                lik32_row(a, qa[3], rec_coord(recs[i + 3]), rec_base(recs[i + 3]), z);
+#pragma unroll
+                for (int v = 0; v < 10; ++v) y[v] = __fadd_rn(y[v], z[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < 10; ++v) x[v] = __fadd_rn(x[v], y[v]);
+        }
+        k.add(x);
+    }
+    const double kk = GSNP_FP32_K(num);
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        const int g = genotype_of(i);
+        tl[g] = (double)k.s[i];
+        eps[g] = isinf(tl[g]) ? 0.0 : fabs(tl[g]) * kk;
+    }
+}
+
+/* likelihood_fp64's sums from walk_qidx's indices: four records' rows loaded
+ * together, their terms added record by record in the reference's order */
+__device__ void deferred_fp64(const CallArgs& a, const uint32_t* recs, const int* qidx, int num, double* tl) {
+    double s[10];
+#pragma unroll
+    for (int v = 0; v < 10; ++v) s[v] = 0.0;
+    for (int i = 0; i < num; i += 4) {
+        double2 r[4][5];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u < num) {
+                const uint32_t w = recs[i + u];
+                const double2* row = reinterpret_cast<const double2*>(
+                    a.lik64 + ((size_t)(qa_of(a, qidx, i + u) * a.L + rec_coord(w)) * 4 + rec_base(w)) * 10);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) r[u][v] = __ldg(row + v);
+            }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u < num) {
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    s[2 * v] = GSNP_DADD(s[2 * v], r[u][v].x);
+                    s[2 * v + 1] = GSNP_DADD(s[2 * v + 1], r[u][v].y);
+                }
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 10; ++i) tl[genotype_of(i)] = s[i];
+}
+
 /* The FP64 pass over the deferred sites, one thread per site: the FP32 sums
  * again (the same pairing, hence the same values) with the double-precision
  * bound checks, then the FP64 sums where those fail.  Sampled sites also get
@@ -1193,12 +1322,15 @@ __device__ __forceinline__ void deferred_site(const CallArgs& a, int64_t i) {
     double tl[16], eps[16];
 #pragma unroll
     for (int g = 0; g < 16; ++g) { tl[g] = 0.0; eps[g] = 0.0; }
-    likelihood_fp32<4>(a, recs, seen, 1, p.num, tl, eps);
+    /* the walk's table indices once, then the sums with their loads batched */
+    int qidx[256];
+    walk_qidx<4>(a, recs, seen, p.num, qidx);
+    deferred_fp32(a, recs, qidx, p.num, tl, eps);
     if (d.flags & kCallSampled) {
         double t64[16];
 #pragma unroll
         for (int g = 0; g < 16; ++g) t64[g] = 0.0;
-        likelihood_fp64<4>(a, recs, seen, 1, p.num, t64);
+        deferred_fp64(a, recs, qidx, p.num, t64);
         double m = 0.0;
 #pragma unroll
         for (int g = 0; g < 16; ++g) m = fmax(m, fabs(t64[g] - tl[g]));
@@ -1212,7 +1344,7 @@ __device__ __forceinline__ void deferred_site(const CallArgs& a, int64_t i) {
     SiteCall call;
     if (!site_posterior<true>(a, ori, p, tl, eps, lp, recs, 1, nq, &call)) {
         /* FP64 fixup: the FP32 likelihood is too close to a decision boundary */
-        likelihood_fp64<4>(a, recs, seen, 1, p.num, tl);
+        deferred_fp64(a, recs, qidx, p.num, tl);
         site_posterior<true>(a, ori, p, tl, nullptr, lp, recs, 1, nq, &call);
         call.flags |= kCallFixup;
         atomicAdd(a.stats + 1, 1ull);
