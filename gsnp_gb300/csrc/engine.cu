@@ -23,6 +23,7 @@
 #include <functional>
 #include <string>
 #include <thread>
+#include <future>
 #include <memory>
 #include <vector>
 
@@ -787,9 +788,8 @@ struct Segment {
 };
 
 /* The calling pass, segment by segment.  before(s) runs first for each
- * segment (the call gathers the reads there; it must leave the reads of
- * segment s + 1 on the device too, which the tile ranges and the next-site
- * lookups of segment s reach), after(s) once its calls are queued. */
+ * segment (the call gathers the reads there: those of segments 0 .. s must be
+ * on the device), after(s) once its calls are queued. */
 /* Allocations and one-time work of a calling pass, done before any of its
  * work is queued (and outside a graph capture). */
 int prepare_calling(gsnp_context* c) {
@@ -1387,6 +1387,16 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(dev_alloc(&c->d_out, (size_t)c->chr_len), "cudaMalloc calls");
         c->out_sites = c->chr_len;
     }
+    /* the host's window replay on a thread of its own from the start: it
+     * reads the caller's arrays while the uploads below are issued */
+    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
+    std::string err;
+    const int64_t chr_len = c->chr_len;
+    const int qmin = c->params.q_min;
+    WindowPlan* plan_out = &c->plan;
+    std::future<int> replay = std::async(std::launch::async, [v, chr_len, L, qmin, plan_out, &err]() {
+        return replay_windows(v, chr_len, L, qmin, host_threads(), plan_out, &err);
+    });
     /* 1. uploads, on their own stream */
     const size_t raw = (size_t)n * r->pitch;
     if (n > c->raw_cap || raw > c->raw_bytes) {
@@ -1444,10 +1454,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         cudaStreamSynchronize(c->stream);
         cudaStreamSynchronize(c->down_stream);
     };
-    /* 2. host: the length check and the window replay */
-    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
-    std::string err;
-    const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, host_threads(), &c->plan, &err);
+    /* 2. host: the length check and the window replay, started above */
+    const int rc = replay.get();
     if (rc != 0) {
         drain();
         return fail(c, rc, err);
@@ -1525,8 +1533,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         CK(cudaGetLastError(), "index kernels");
     }
 
-    /* 4. segments: gathers on their own stream two segments ahead (segment s
-     *    is called once segment s + 1 is gathered), calls, downloads */
+    /* 4. segments: gathers on their own stream one segment ahead (segment s
+     *    is called once it is gathered), calls, downloads */
     CK(cudaEventRecord(c->ev_index, c->stream), "event");
     CK(cudaStreamWaitEvent(c->gather_stream, c->ev_index, 0), "wait");
     const std::vector<Segment> segs = plan_segments(c, v, segment_count(nd, P.n_windows));
@@ -1569,9 +1577,13 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         return GSNP_OK;
     };
     auto before = [&](size_t si) -> int {
+        /* segment si's kernels read only its own reads and those before it:
+         * its tile ranges end at its last read (tile_bounds_kernel takes the
+         * next read's start from the host replay), and the next-site lookup
+         * at a window's end takes only reads starting inside the window */
         const int64_t last = (int64_t)segs.size() - 1;
-        const int64_t need = std::min<int64_t>((int64_t)si + 1, last);
-        const int rc = gather_through(std::min<int64_t>((int64_t)si + 2, last));
+        const int64_t need = (int64_t)si;
+        const int rc = gather_through(std::min<int64_t>((int64_t)si + 1, last));
         if (rc != GSNP_OK) return rc;
         CK(cudaStreamWaitEvent(c->stream, c->ev_gather[(size_t)need], 0), "wait");
         c->n_gathered = segs[(size_t)need].dhi;   /* the rows the kernels of si may read */
