@@ -1029,7 +1029,7 @@ int run_calling(gsnp_context* c, const std::vector<Segment>& segs, const std::fu
         /* In the FP32 form the persistent kernel calls the segment's tiles;
          * the binned kernels take only the tiles it leaves (the FP64 windows'
          * and those with a site deeper than its record slots). */
-        const bool use_stream = c->stream_path && c->params.precision == 1;
+        const bool use_stream = c->stream_path && c->params.precision == 1 && segs.size() == 1 && !c->view.on;
         int64_t n_left = 0;
         auto run_stream = [&](const CallArgs& as) -> int {
             CK(cudaMemsetAsync(c->d_stream_ctl, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
@@ -1162,7 +1162,11 @@ int enqueue_device(gsnp_context* c, const std::vector<Segment>& segs, const std:
         if (k >= 0) cudaEventRecord(c->ev[2 * k + 1], c->stream);
     };
     const bool fast = make_args(c).precision == 1;
-    const bool use_stream = c->stream_path && fast;
+    /* the persistent kernel for a whole-chromosome pass: a call in segments
+     * (or chunks) ends each segment's launch of it in a tail of its own, and
+     * its binned kernels, handing out tiles from counters, were the faster
+     * there (c1 e2e in 7 segments: 28.6-29.0 against 29.9 ms) */
+    const bool use_stream = c->stream_path && fast && segs.size() == 1 && !c->view.on;
     int* d_left = reinterpret_cast<int*>(c->d_stream_ctl + 1);
     /* With several segments the deferred sites of all of them go to one pool
      * and one deferred pass runs after the last segment: the pass takes about
