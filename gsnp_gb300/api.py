@@ -48,6 +48,8 @@ class Reads(ctypes.Structure):
         ("seq", ctypes.c_void_p),
         ("qual", ctypes.c_void_p),
         ("pitch", ctypes.c_int32),
+        ("packed", ctypes.c_void_p),
+        ("packed_qmin", ctypes.c_int32),
     ]
 
 
@@ -84,6 +86,7 @@ def declare(lib: ctypes.CDLL) -> None:
         "gsnp_call_streamed": (ctypes.c_int, [_P, ctypes.POINTER(Reads), ctypes.c_char_p, _P, ctypes.c_char_p,
                                               ctypes.c_char_p]),
         "gsnp_stream_footprint": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+        "gsnp_pack_reads": (ctypes.c_int, [_P, _P, _P, _I64, ctypes.c_int32, ctypes.c_int, _P, ctypes.c_int]),
         "gsnp_write_cns": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p]),
         "gsnp_write_columns": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p]),
         "gsnp_recall_resident": (ctypes.c_int, [_P]),
@@ -99,6 +102,24 @@ def declare(lib: ctypes.CDLL) -> None:
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
+
+
+def pack_reads(seq: np.ndarray, qual: np.ndarray, length: np.ndarray, q_min: int, out: Optional[np.ndarray] = None,
+               threads: int = 0) -> np.ndarray:
+    """gsnp_pack_reads: bases and qualities in one byte per position (out, or a
+    new [n][pitch] uint8 array); raises on a base other than ACGT/acgt or a
+    quality above q_min + 62."""
+    from . import native
+    seq = np.ascontiguousarray(seq, dtype=np.uint8)
+    qual = np.ascontiguousarray(qual, dtype=np.uint8)
+    length = np.ascontiguousarray(length, dtype=np.int32)
+    if out is None:
+        out = np.empty(seq.shape, dtype=np.uint8)
+    rc = native().gsnp_pack_reads(seq.ctypes.data, qual.ctypes.data, length.ctypes.data, int(seq.shape[0]),
+                                  int(seq.shape[1]), int(q_min), out.ctypes.data, int(threads))
+    if rc != 0:
+        raise RuntimeError("gsnp_pack_reads failed (%d)" % rc)
+    return out
 
 
 def params_from_flags(flags: Sequence[str], precision: int = PRECISION_FP64) -> Params:
@@ -212,16 +233,20 @@ class Caller:
         self._check(self.lib.gsnp_set_stream(self.ctx, _P(stream_ptr)), "gsnp_set_stream")
 
     @staticmethod
-    def reads_struct(pos, length, hit, strand, seq, qual) -> Reads:
+    def reads_struct(pos, length, hit, strand, seq, qual, packed=None, packed_qmin: int = 0) -> Reads:
+        """The C ABI's read arrays; with packed (gsnp_pack_reads's bytes),
+        seq and qual may be None and are not read."""
         r = Reads()
         r.n = int(pos.shape[0])
         r.pos = pos.ctypes.data
         r.len = length.ctypes.data
         r.hit = hit.ctypes.data
         r.strand = strand.ctypes.data
-        r.seq = seq.ctypes.data
-        r.qual = qual.ctypes.data
-        r.pitch = int(seq.shape[1])
+        r.seq = seq.ctypes.data if seq is not None else None
+        r.qual = qual.ctypes.data if qual is not None else None
+        r.pitch = int((packed if packed is not None else seq).shape[1])
+        r.packed = packed.ctypes.data if packed is not None else None
+        r.packed_qmin = int(packed_qmin)
         return r
 
     def load_reference(self, codes: np.ndarray, snp: Optional[np.ndarray] = None) -> None:

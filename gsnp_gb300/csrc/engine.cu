@@ -22,6 +22,7 @@
 #include <cstring>
 #include <functional>
 #include <string>
+#include <atomic>
 #include <thread>
 #include <future>
 #include <memory>
@@ -211,14 +212,23 @@ __device__ __forceinline__ uint8_t upper_base(uint8_t b, bool* bad) {
  * case ('A' past the read's end; a base other than ACGT/acgt sets *error to
  * 2).  Rows [row_begin, row_end); a block holds rows_per_block rows, each
  * thread VEC consecutive columns of one row (VEC = 4 when L and the pitch are
- * multiples of 4 and L <= pitch: 32-bit loads, 64-bit stores). */
-template <int VEC>
+ * multiples of 4 and L <= pitch: 32-bit loads, 64-bit stores).  PACKED: seq
+ * holds gsnp_pack_reads's bytes (qual is not read), which give the base and
+ * quality - qmin, or 63 for a quality below qmin (written as qmin - 1). */
+__device__ __forceinline__ uint32_t unpack_bq(uint32_t byte, int qmin) {
+    const uint32_t code = byte & 63u;
+    const uint32_t base = (uint32_t)(uint8_t)"ACTG"[byte >> 6];
+    const uint32_t q = code == 63u ? (uint32_t)(uint8_t)(qmin - 1) : (uint32_t)(uint8_t)(qmin + (int)code);
+    return base | (q << 8);
+}
+
+template <int VEC, bool PACKED = false>
 __global__ void __launch_bounds__(256) gather_reads_kernel(
     int64_t row_begin, int64_t row_end, const int64_t* __restrict__ idx, int64_t n_raw, const int32_t* __restrict__ rpos,
     const int32_t* __restrict__ rlen, const int32_t* __restrict__ rhit, const uint8_t* __restrict__ rstrand,
     const uint8_t* __restrict__ seq, const uint8_t* __restrict__ qual, int pitch, int L, int rows_per_block,
     int32_t* __restrict__ pos, int32_t* __restrict__ lenhit, int32_t* __restrict__ len,
-    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq, int* __restrict__ error) {
+    uint8_t* __restrict__ strand, uint16_t* __restrict__ bq, int* __restrict__ error, int qmin = 0) {
     /* kGatherRows groups of rows per block, one row of each group per thread:
      * the groups' load chains (index, length, bases and qualities) are
      * independent, so they are in flight together */
@@ -249,10 +259,10 @@ __global__ void __launch_bounds__(256) gather_reads_kernel(
         rl[g] = rlen[src[g]];
         if (VEC == 4) {
             s4[g] = *reinterpret_cast<const uint32_t*>(seq + src[g] * pitch + c0);
-            q4[g] = *reinterpret_cast<const uint32_t*>(qual + src[g] * pitch + c0);
+            if (!PACKED) q4[g] = *reinterpret_cast<const uint32_t*>(qual + src[g] * pitch + c0);
         } else if (c0 < pitch) {
             s4[g] = seq[src[g] * pitch + c0];
-            q4[g] = qual[src[g] * pitch + c0];
+            if (!PACKED) q4[g] = qual[src[g] * pitch + c0];
         }
     }
 #pragma unroll
@@ -269,12 +279,19 @@ __global__ void __launch_bounds__(256) gather_reads_kernel(
             uint32_t lo = 0, hi = 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const uint8_t b = c0 + k < rl[g] ? upper_base((uint8_t)(s4[g] >> (8 * k)), &bad) : (uint8_t)'A';
-                const uint32_t v = (uint32_t)b | (((q4[g] >> (8 * k)) & 0xffu) << 8);
+                uint32_t v;
+                if (PACKED) {
+                    v = c0 + k < rl[g] ? unpack_bq((s4[g] >> (8 * k)) & 0xffu, qmin) : (uint32_t)'A';
+                } else {
+                    const uint8_t b = c0 + k < rl[g] ? upper_base((uint8_t)(s4[g] >> (8 * k)), &bad) : (uint8_t)'A';
+                    v = (uint32_t)b | (((q4[g] >> (8 * k)) & 0xffu) << 8);
+                }
                 if (k < 2) lo |= v << (16 * k);
                 else hi |= v << (16 * (k - 2));
             }
             *reinterpret_cast<uint2*>(bq + row * L + c0) = make_uint2(lo, hi);
+        } else if (PACKED) {
+            bq[row * L + c0] = (uint16_t)(c0 < pitch && c0 < rl[g] ? unpack_bq(s4[g] & 0xffu, qmin) : (uint32_t)'A');
         } else {
             uint8_t b = 'A';
             if (c0 < pitch && c0 < rl[g]) b = upper_base((uint8_t)s4[g], &bad);
@@ -283,6 +300,39 @@ __global__ void __launch_bounds__(256) gather_reads_kernel(
     }
     const unsigned any_bad = __ballot_sync(0xffffffffu, bad), any_idx = __ballot_sync(0xffffffffu, bad_idx);
     if ((threadIdx.x & 31) == 0 && (any_bad | any_idx)) atomicMax(error, any_idx ? 3 : 2);
+}
+
+/* gather_reads_kernel in the form the pitch and the read layout allow */
+cudaError_t launch_gather(bool vec4, bool packed, unsigned blocks, cudaStream_t stream, int64_t row_begin,
+                          int64_t row_end, const int64_t* idx, int64_t n_raw, const int32_t* rpos, const int32_t* rlen,
+                          const int32_t* rhit, const uint8_t* rstrand, const uint8_t* seq, const uint8_t* qual,
+                          int pitch, int L, int rows_per_block, int32_t* pos, int32_t* lenhit, int32_t* len,
+                          uint8_t* strand, uint16_t* bq, int* error, int qmin) {
+#define GSNP_GATHER(V, P)                                                                                      \
+    gather_reads_kernel<V, P><<<blocks, 256, 0, stream>>>(row_begin, row_end, idx, n_raw, rpos, rlen, rhit,    \
+                                                          rstrand, seq, qual, pitch, L, rows_per_block, pos,  \
+                                                          lenhit, len, strand, bq, error, qmin)
+    if (vec4) {
+        if (packed) GSNP_GATHER(4, true);
+        else GSNP_GATHER(4, false);
+    } else {
+        if (packed) GSNP_GATHER(1, true);
+        else GSNP_GATHER(1, false);
+    }
+#undef GSNP_GATHER
+    return cudaGetLastError();
+}
+
+/* gsnp_pack_reads's bytes back to base and quality chars (the calibration
+ * histogram's input; seq may be packed itself); a quality below qmin becomes
+ * qmin - 1 */
+__global__ void unpack_reads_kernel(const uint8_t* packed, size_t n, int qmin, uint8_t* seq,
+                                    uint8_t* __restrict__ qual) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t v = unpack_bq(packed[i], qmin);
+        seq[i] = (uint8_t)(v & 0xffu);
+        qual[i] = (uint8_t)(v >> 8);
+    }
 }
 
 /* pass-1 calibration histogram (cpp/matrix.cc:58-118): unique reads, non-N
@@ -1374,8 +1424,10 @@ int ensure_call_streams(gsnp_context* c) {
 
 int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     if (!c || !r || r->n < 0 || r->pitch < 0 ||
-        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
+        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || (!r->packed && (!r->seq || !r->qual)))))
         return fail(c, GSNP_ERR_ARG, "null read arrays");
+    if (r->packed && r->packed_qmin != c->params.q_min)
+        return fail(c, GSNP_ERR_ARG, "reads packed with another q_min than the tables'");
     if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
     cudaSetDevice(c->device);
     PhaseTimer timer("gsnp_call_chromosome");
@@ -1393,7 +1445,7 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     }
     /* the host's window replay on a thread of its own from the start: it
      * reads the caller's arrays while the uploads below are issued */
-    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
+    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch, r->packed};
     std::string err;
     const int64_t chr_len = c->chr_len;
     const int qmin = c->params.q_min;
@@ -1434,8 +1486,14 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
         cudaStream_t us = c->up(k);
         if (e > b) {
             const size_t off = (size_t)b * r->pitch, bytes = (size_t)(e - b) * r->pitch;
-            CK(cudaMemcpyAsync(c->d_raw_seq + off, r->seq + off, bytes, cudaMemcpyHostToDevice, us), "upload seq");
-            CK(cudaMemcpyAsync(c->d_raw_qual + off, r->qual + off, bytes, cudaMemcpyHostToDevice, us), "upload qual");
+            if (r->packed) {
+                CK(cudaMemcpyAsync(c->d_raw_seq + off, r->packed + off, bytes, cudaMemcpyHostToDevice, us),
+                   "upload packed reads");
+            } else {
+                CK(cudaMemcpyAsync(c->d_raw_seq + off, r->seq + off, bytes, cudaMemcpyHostToDevice, us), "upload seq");
+                CK(cudaMemcpyAsync(c->d_raw_qual + off, r->qual + off, bytes, cudaMemcpyHostToDevice, us),
+                   "upload qual");
+            }
         }
         CK(cudaEventRecord(c->ev_chunk[k], us), "event");
         if (k == 0 || k == gsnp_context::kUploadChunks / 2 - 1 || k == gsnp_context::kUploadChunks - 1)
@@ -1517,7 +1575,8 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
     }
     c->n_dep = nd;
     c->n_gathered = 0;
-    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) + 2ULL * (uint64_t)n * r->pitch;
+    c->h2d_bytes = (uint64_t)P.n_windows * 9 + (uint64_t)n * (4 + 4 + 4 + 1) +
+                   (r->packed ? 1ULL : 2ULL) * (uint64_t)n * r->pitch;
     c->d2h_bytes = out ? (uint64_t)c->chr_len * sizeof(SiteCall) : 0;
 
     /* 3. the deposited index list, once the small arrays are on the device */
@@ -1563,16 +1622,11 @@ int call_chromosome(gsnp_context* c, const gsnp_reads* r, gsnp_site_call* out) {
                 const int64_t rows = g.dhi - g.dlo;
                 const int64_t per_block = (int64_t)rows_per_block * kGatherRows;
                 const unsigned blocks = (unsigned)((rows + per_block - 1) / per_block);
-                if (vec4)
-                    gather_reads_kernel<4><<<blocks, 256, 0, c->gather_stream>>>(
-                        g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
-                        c->d_raw_seq, c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
-                        c->d_strand, c->d_bq, c->d_gerror);
-                else
-                    gather_reads_kernel<1><<<blocks, 256, 0, c->gather_stream>>>(
-                        g.dlo, g.dhi, c->d_idx, n, c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand,
-                        c->d_raw_seq, c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
-                        c->d_strand, c->d_bq, c->d_gerror);
+                CK(launch_gather(vec4, r->packed != nullptr, blocks, c->gather_stream, g.dlo, g.dhi, c->d_idx, n,
+                                 c->d_raw_pos, c->d_raw_len, c->d_raw_hit, c->d_raw_strand, c->d_raw_seq,
+                                 c->d_raw_qual, r->pitch, L, rows_per_block, c->d_pos, c->d_lenhit, c->d_len,
+                                 c->d_strand, c->d_bq, c->d_gerror, c->params.q_min),
+                   "gather kernel");
                 CK(cudaGetLastError(), "gather kernel");
             }
             CK(cudaEventRecord(c->ev_gather[(size_t)gathered_seg], c->gather_stream), "event");
@@ -1876,6 +1930,11 @@ int gsnp_call_chromosome_into(gsnp_context* c, const gsnp_reads* r, gsnp_site_ca
 
 int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, double* pm) {
     if (!c || !p || !r || !pm) return fail(c, GSNP_ERR_ARG, "null argument");
+    if (r->n < 0 || r->pitch < 0 ||
+        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || (!r->packed && (!r->seq || !r->qual)))))
+        return fail(c, GSNP_ERR_ARG, "null read arrays");
+    if (r->packed && r->packed_qmin != p->q_min)
+        return fail(c, GSNP_ERR_ARG, "reads packed with another q_min than the parameters'");
     if (!c->d_codes) return fail(c, GSNP_ERR_STATE, "reference must be loaded first");
     if (p->read_length <= 0 || p->read_length > 255) return fail(c, GSNP_ERR_ARG, "read_length must be 1..255");
     if (p->q_max < p->q_min) return fail(c, GSNP_ERR_ARG, "q_max below q_min");
@@ -1903,8 +1962,17 @@ int gsnp_calibrate(gsnp_context* c, const gsnp_params* p, const gsnp_reads* r, d
     CK(cudaMemcpyAsync(d_len, r->len, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
     CK(cudaMemcpyAsync(d_hit, r->hit, r->n * 4, cudaMemcpyHostToDevice, c->stream), "upload");
     CK(cudaMemcpyAsync(d_strand, r->strand, r->n, cudaMemcpyHostToDevice, c->stream), "upload");
-    CK(cudaMemcpyAsync(d_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload");
-    CK(cudaMemcpyAsync(d_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload");
+    if (r->packed) {
+        CK(cudaMemcpyAsync(d_seq, r->packed, raw, cudaMemcpyHostToDevice, c->stream), "upload");
+        if (raw > 0) {
+            unpack_reads_kernel<<<(unsigned)std::min<size_t>((raw + 255) / 256, 1u << 16), 256, 0, c->stream>>>(
+                d_seq, raw, (int)(signed char)p->q_min, d_seq, d_qual);
+            CK(cudaGetLastError(), "unpack kernel");
+        }
+    } else {
+        CK(cudaMemcpyAsync(d_seq, r->seq, raw, cudaMemcpyHostToDevice, c->stream), "upload");
+        CK(cudaMemcpyAsync(d_qual, r->qual, raw, cudaMemcpyHostToDevice, c->stream), "upload");
+    }
     if (r->n > 0) {
         /* the matching bins in shared memory when they fit (41 qualities x
          * 4 bases x 100 cycles: 64 KB), else every bin in global memory */
@@ -2586,8 +2654,10 @@ int ring_ensure(gsnp_context* c, StreamRing* g, int64_t raw_rows, int64_t raw_by
 int call_streamed(gsnp_context* c, const gsnp_reads* r, const char* chr_name, gsnp_site_call* out,
                   const char* cns_path, const char* columns_base) {
     if (!c || !r || r->n < 0 || r->pitch < 0 ||
-        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || !r->seq || !r->qual)))
+        (r->n > 0 && (!r->pos || !r->len || !r->hit || !r->strand || (!r->packed && (!r->seq || !r->qual)))))
         return fail(c, GSNP_ERR_ARG, "null read arrays");
+    if (r->packed && r->packed_qmin != c->params.q_min)
+        return fail(c, GSNP_ERR_ARG, "reads packed with another q_min than the tables'");
     if ((cns_path || columns_base) && !chr_name) return fail(c, GSNP_ERR_ARG, "the outputs need the chromosome name");
     if (!c->have_tables || !c->d_codes) return fail(c, GSNP_ERR_STATE, "tables and reference must be loaded first");
     cudaSetDevice(c->device);
@@ -2599,7 +2669,7 @@ int call_streamed(gsnp_context* c, const gsnp_reads* r, const char* chr_name, gs
     const int L = c->params.read_length;
     c->called = false;
     c->streamed = false;
-    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch};
+    ReadView v{r->n, r->pos, r->len, r->hit, r->seq, r->qual, r->pitch, r->packed};
     std::string err;
     {
         const int rc = replay_windows(v, c->chr_len, L, c->params.q_min, host_threads(), &c->plan, &err);
@@ -2712,9 +2782,15 @@ int call_streamed(gsnp_context* c, const gsnp_reads* r, const char* chr_name, gs
             CK(cudaMemcpyAsync(s.raw_hit, r->hit + b, n * 4, cudaMemcpyHostToDevice, c->up_stream), "upload");
             CK(cudaMemcpyAsync(s.raw_strand, r->strand + b, n, cudaMemcpyHostToDevice, c->up_stream), "upload");
             const size_t off = (size_t)b * r->pitch, bytes = (size_t)n * r->pitch;
-            CK(cudaMemcpyAsync(s.raw_seq, r->seq + off, bytes, cudaMemcpyHostToDevice, c->up_stream), "upload seq");
-            CK(cudaMemcpyAsync(s.raw_qual, r->qual + off, bytes, cudaMemcpyHostToDevice, c->up_stream), "upload qual");
-            c->h2d_bytes += (uint64_t)n * (13 + 2 * (uint64_t)r->pitch);
+            if (r->packed) {
+                CK(cudaMemcpyAsync(s.raw_seq, r->packed + off, bytes, cudaMemcpyHostToDevice, c->up_stream),
+                   "upload packed reads");
+            } else {
+                CK(cudaMemcpyAsync(s.raw_seq, r->seq + off, bytes, cudaMemcpyHostToDevice, c->up_stream), "upload seq");
+                CK(cudaMemcpyAsync(s.raw_qual, r->qual + off, bytes, cudaMemcpyHostToDevice, c->up_stream),
+                   "upload qual");
+            }
+            c->h2d_bytes += (uint64_t)n * (13 + (r->packed ? 1 : 2) * (uint64_t)r->pitch);
         }
         CK(cudaEventRecord(s.uploaded, c->up_stream), "event");
         return GSNP_OK;
@@ -2763,15 +2839,10 @@ int call_streamed(gsnp_context* c, const gsnp_reads* r, const char* chr_name, gs
             CK(cudaGetLastError(), "index kernels");
             const int64_t per_block = (int64_t)rows_per_block * kGatherRows;
             const unsigned blocks = (unsigned)((nd + per_block - 1) / per_block);
-            if (vec4)
-                gather_reads_kernel<4><<<blocks, 256, 0, c->stream>>>(
-                    0, nd, s.idx, nraw, s.raw_pos, s.raw_len, s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, r->pitch,
-                    L, rows_per_block, s.pos, s.lenhit, s.len, s.strand, s.bq, c->d_gerror);
-            else
-                gather_reads_kernel<1><<<blocks, 256, 0, c->stream>>>(
-                    0, nd, s.idx, nraw, s.raw_pos, s.raw_len, s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, r->pitch,
-                    L, rows_per_block, s.pos, s.lenhit, s.len, s.strand, s.bq, c->d_gerror);
-            CK(cudaGetLastError(), "gather kernel");
+            CK(launch_gather(vec4, r->packed != nullptr, blocks, c->stream, 0, nd, s.idx, nraw, s.raw_pos, s.raw_len,
+                             s.raw_hit, s.raw_strand, s.raw_seq, s.raw_qual, r->pitch, L, rows_per_block, s.pos,
+                             s.lenhit, s.len, s.strand, s.bq, c->d_gerror, c->params.q_min),
+               "gather kernel");
         }
         if (carry_c[k] >= 0) CK(cudaMemcpyAsync(g->counts, g->carry_counts, sizeof(SiteCounts) * kWin,
                                                 cudaMemcpyDeviceToDevice, c->stream), "carried counts");
@@ -2956,4 +3027,49 @@ extern "C" int gsnp_stream_footprint(gsnp_context* c, uint64_t* ring_bytes, uint
     *ring_bytes = c->ring ? (uint64_t)c->ring->bytes : 0;
     *writer_bytes = c->colw ? (uint64_t)c->colw->device_bytes() : 0;
     return GSNP_OK;
+}
+
+extern "C" int gsnp_pack_reads(const uint8_t* seq, const uint8_t* qual, const int32_t* len, int64_t n, int32_t pitch,
+                               int q_min, uint8_t* out, int threads) {
+    if (n < 0 || pitch < 0 || (n > 0 && (!seq || !qual || !len || !out))) return GSNP_ERR_ARG;
+    /* the kernels compare qualities as signed chars; the quality below
+     * q_min that a skipped base is unpacked to must be one too */
+    if (q_min < -127 || q_min > 127) return GSNP_ERR_ARG;
+    std::atomic<int> rc{GSNP_OK};
+    auto work = [&](int64_t a, int64_t b) {
+        for (int64_t i = a; i < b && rc.load(std::memory_order_relaxed) == GSNP_OK; ++i) {
+            const int l = len[i];
+            if (l < 0 || l > pitch) {
+                rc = GSNP_ERR_INPUT;
+                return;
+            }
+            const uint8_t* s = seq + i * pitch;
+            const uint8_t* q = qual + i * pitch;
+            uint8_t* o = out + i * pitch;
+            for (int c = 0; c < l; ++c) {
+                int code;
+                switch (s[c]) {
+                    case 'A': case 'a': code = 0; break;
+                    case 'C': case 'c': code = 1; break;
+                    case 'T': case 't': code = 2; break;
+                    case 'G': case 'g': code = 3; break;
+                    default: rc = GSNP_ERR_INPUT; return;
+                }
+                const int qq = (int)(signed char)q[c] - q_min;
+                if (qq > 62) {
+                    rc = GSNP_ERR_INPUT;
+                    return;
+                }
+                o[c] = (uint8_t)((code << 6) | (qq < 0 ? 63 : qq));
+            }
+            memset(o + l, 0, (size_t)(pitch - l));
+        }
+    };
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(threads > 0 ? threads : host_threads(), n / 4096 + 1));
+    std::vector<std::thread> pool;
+    const int64_t per = (n + nt - 1) / nt;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work, std::min(n, t * per), std::min(n, (t + 1) * per));
+    work(0, std::min(n, per));
+    for (std::thread& th : pool) th.join();
+    return rc.load();
 }

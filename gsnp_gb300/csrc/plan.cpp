@@ -104,6 +104,10 @@ bool window_has_records(const ReadView& r, int64_t chr_len, int64_t start, int64
         if (p < w0 - L + 1 || r.hit[i] != 1) continue;
         const int64_t c0 = std::max<int64_t>(0, w0 - p), c1 = std::min<int64_t>(r.len[i], w1 - p);
         for (int64_t c = c0; c < c1; ++c) {
+            if (r.packed) {
+                if ((r.packed[i * r.pitch + c] & 63) != 63) return true;
+                continue;
+            }
             const signed char b = (signed char)r.seq[i * r.pitch + c];
             const signed char q = (signed char)r.qual[i * r.pitch + c];
             if (b != 'N' && q >= (signed char)qmin) return true;

@@ -53,6 +53,9 @@ struct ReadView {
     const uint8_t* seq;
     const uint8_t* qual;
     int32_t pitch;
+    /* gsnp_pack_reads's bytes in place of seq and qual when set (packed with
+     * the replay's q_min: 63 in bits 5:0 is a quality below it) */
+    const uint8_t* packed = nullptr;
 };
 
 /* An alignment passes the position filters when 0 <= pos and pos + len <

@@ -83,7 +83,25 @@ typedef struct gsnp_reads {
     const uint8_t* seq;       /* [n][pitch] base chars */
     const uint8_t* qual;      /* [n][pitch] quality chars */
     int32_t pitch;
+    /* Optional, in place of seq and qual (NULL: not used): [n][pitch] bytes
+     * of gsnp_pack_reads, base and quality in one byte, which halves the
+     * bytes a call uploads; packed_qmin is the q_min they were packed with
+     * and must equal the tables' (GSNP_ERR_ARG otherwise). */
+    const uint8_t* packed;
+    int32_t packed_qmin;
 } gsnp_reads;
+
+/* No counterpart in the reference.  Pack the bases and qualities of n reads
+ * ([n][pitch] each, len[i] positions of read i used) into out ([n][pitch]
+ * bytes) for gsnp_reads.packed: base A C T G (either case) as 0 1 2 3 in bits
+ * 7:6, quality - q_min in bits 5:0, and 63 in bits 5:0 for a quality below
+ * q_min (a base the caller skips in the pileup, the calibration and the
+ * window replay alike); positions past a read's length are 0.  Runs on up to
+ * `threads` host threads (0: all).  GSNP_ERR_INPUT for another base, as the
+ * calls do, or for a quality above q_min + 62, which has no code (pass seq and
+ * qual then). */
+int gsnp_pack_reads(const uint8_t* seq, const uint8_t* qual, const int32_t* len, int64_t n, int32_t pitch, int q_min,
+                    uint8_t* out, int threads);
 
 /* Per-site call (32 bytes), the binary form of one cns row. */
 typedef struct gsnp_site_call {
