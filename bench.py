@@ -15,7 +15,10 @@ beside it in the same run (the "compare" object).
   e2e   : sites/s through the C ABI (gsnp_call_chromosome_into) from pinned
           host buffers: upload of the alignments, window replay, gather,
           calling, and the download of every site's 32-byte call, all inside
-          the timed step (the library overlaps them segment by segment).
+          the timed step (the library overlaps them segment by segment).  The
+          reads are uploaded packed, base and quality in one byte per
+          position (gsnp_pack_reads, untimed, its time given as pack_ms);
+          e2e_unpacked is the same call with two bytes per position.
 The calling kernels' roofline is the HBM bandwidth; the algorithmic bytes of a
 site are 2*D + 9*D/Lbar + 0.5 + 32 (bases and qualities of the covering reads,
 per-read start/length/strand, the 4-bit reference code, a 32-byte call).
@@ -318,6 +321,14 @@ def main():
     out_pinned = torch.empty(w.genome_len * 32, dtype=torch.uint8, pin_memory=True)
     reads = api.Caller.reads_struct(*arrs)
     p = api.params_from_flags(flags, precision)
+    # the same reads with base and quality in one byte per position, the form
+    # the e2e steps upload (gsnp_pack_reads on all host threads, untimed; its
+    # time is reported beside the e2e figure)
+    packed = torch.empty(tuple(w.seq.shape), dtype=torch.uint8, pin_memory=True).numpy()
+    t1 = time.perf_counter()
+    api.pack_reads(arrs[4], arrs[5], arrs[1], p.q_min, out=packed)
+    pack_ms = (time.perf_counter() - t1) * 1e3
+    reads_packed = api.Caller.reads_struct(*arrs[:4], None, None, packed=packed, packed_qmin=p.q_min)
     pm = caller.calibrate(p, reads)
     prior, rank_tab = caller.prior_table(p), caller.rank_table()
     caller.load_tables(p, pm, prior, rank_tab)
@@ -384,20 +395,28 @@ def main():
 
     # ---- end to end through the C ABI from pinned host buffers ----
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 5)
-    e2e_times = []
-    for i in range(1 + e2e_steps):           # the first pass warms the pinned result buffer, untimed
-        barrier()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        caller.call_into(reads, out_pinned.data_ptr())
-        torch.cuda.synchronize()
-        if i > 0:
-            e2e_times.append(time.perf_counter() - t1)
-    h2d, d2h = caller.transfer_bytes()
-    # median step: the host link is shared with the other GPUs of the machine,
-    # and a step that meets their traffic is reported in step_ms, not averaged in
-    e2e_s = max_over_ranks(max(statistics.median(e2e_times), 1e-9))
+
+    def e2e_run(rd):
+        times = []
+        for i in range(1 + e2e_steps):       # the first pass warms the pinned result buffer, untimed
+            barrier()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            caller.call_into(rd, out_pinned.data_ptr())
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(time.perf_counter() - t1)
+        # median step: the host link is shared with the other GPUs of the
+        # machine, and a step that meets their traffic is reported in step_ms,
+        # not averaged in
+        return times, caller.transfer_bytes(), max_over_ranks(max(statistics.median(times), 1e-9))
+
+    e2e_times, (h2d, d2h), e2e_s = e2e_run(reads_packed)
     e2e_value = replica_rate(world, sites, e2e_s)
+    un_times, (h2d_u, d2h_u), un_s = e2e_run(reads)
+    e2e_unpacked = {"value": replica_rate(world, sites, un_s), "unit": UNIT, "h2d_bytes_per_step": int(h2d_u),
+                    "d2h_bytes_per_step": int(d2h_u), "step_ms": [round(t * 1e3, 2) for t in un_times],
+                    "note": "the same call with bases and qualities as two bytes per position"}
 
     # ---- end to end with the cns text, the output the reference's pass writes ----
     # each step: upload and call (gsnp_call_chromosome), then the text of every
@@ -408,7 +427,7 @@ def main():
         barrier()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        caller.call(reads)
+        caller.call(reads_packed)
         rc = caller.lib.gsnp_write_cns(caller.ctx, w.chr_name.encode(), os.devnull.encode())
         torch.cuda.synchronize()
         if rc != 0:
@@ -496,7 +515,7 @@ def main():
                 barrier()
                 torch.cuda.synchronize()
                 t1 = time.perf_counter()
-                caller.call_streamed(reads, w.chr_name, out_pinned.data_ptr(), None, os.path.join(sdir, "cns"))
+                caller.call_streamed(reads_packed, w.chr_name, out_pinned.data_ptr(), None, os.path.join(sdir, "cns"))
                 torch.cuda.synchronize()
                 if i > 0:
                     ts.append(time.perf_counter() - t1)
@@ -565,7 +584,10 @@ def main():
             "bases_per_s": value * depth,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": e2e_steps, "stat": "median step",
-                    "step_ms": [round(t * 1e3, 2) for t in e2e_times]},
+                    "step_ms": [round(t * 1e3, 2) for t in e2e_times],
+                    "input": "packed reads (base and quality in one byte per position)",
+                    "pack_ms": round(pack_ms, 1)},
+            "e2e_unpacked": e2e_unpacked,
             "e2e_text": e2e_text,
             "e2e_streamed": streamed,
             "cns_parity": parity,

@@ -3029,6 +3029,33 @@ extern "C" int gsnp_stream_footprint(gsnp_context* c, uint64_t* ring_bytes, uint
     return GSNP_OK;
 }
 
+namespace {
+/* One read of gsnp_pack_reads; nonzero for a base other than ACGT/acgt or a
+ * quality above q_min + 62.  Branch-free in 8-bit lanes, so that the compiler
+ * vectorizes it.  k = (b >> 1) & 3 is 0 1 2 3 for A C T G in either case, and
+ * a byte is one of those letters exactly when its upper-case form (b & 0xdf)
+ * is the letter of its own k: 0x41 | k << 1 gives A C E G, and k == 2 turns
+ * E into T (0x45 ^ 0x11 = 0x54).  The quality tests are on signed bytes, as
+ * the kernels compare them; q_min is within [-127, 127]. */
+unsigned pack_row(const uint8_t* __restrict s, const uint8_t* __restrict q, uint8_t* __restrict o, int l, int q_min) {
+    const int8_t lo = (int8_t)q_min;
+    const int8_t hi = (int8_t)(q_min + 62 > 127 ? 127 : q_min + 62);
+    const uint8_t qm = (uint8_t)q_min;
+    uint8_t bad = 0;
+    for (int c = 0; c < l; ++c) {
+        const uint8_t b = s[c];
+        const uint8_t k = (uint8_t)((b >> 1) & 3);
+        const uint8_t letter = (uint8_t)((0x41 | (k << 1)) ^ (k == 2 ? 0x11 : 0));
+        const int8_t qs = (int8_t)q[c];
+        bad |= (uint8_t)((uint8_t)(b & 0xdf) != letter);
+        bad |= (uint8_t)(qs > hi);
+        const uint8_t code = qs < lo ? (uint8_t)63 : (uint8_t)(q[c] - qm);
+        o[c] = (uint8_t)((uint8_t)(k << 6) | code);
+    }
+    return bad;
+}
+}  // namespace
+
 extern "C" int gsnp_pack_reads(const uint8_t* seq, const uint8_t* qual, const int32_t* len, int64_t n, int32_t pitch,
                                int q_min, uint8_t* out, int threads) {
     if (n < 0 || pitch < 0 || (n > 0 && (!seq || !qual || !len || !out))) return GSNP_ERR_ARG;
@@ -3046,21 +3073,9 @@ extern "C" int gsnp_pack_reads(const uint8_t* seq, const uint8_t* qual, const in
             const uint8_t* s = seq + i * pitch;
             const uint8_t* q = qual + i * pitch;
             uint8_t* o = out + i * pitch;
-            for (int c = 0; c < l; ++c) {
-                int code;
-                switch (s[c]) {
-                    case 'A': case 'a': code = 0; break;
-                    case 'C': case 'c': code = 1; break;
-                    case 'T': case 't': code = 2; break;
-                    case 'G': case 'g': code = 3; break;
-                    default: rc = GSNP_ERR_INPUT; return;
-                }
-                const int qq = (int)(signed char)q[c] - q_min;
-                if (qq > 62) {
-                    rc = GSNP_ERR_INPUT;
-                    return;
-                }
-                o[c] = (uint8_t)((code << 6) | (qq < 0 ? 63 : qq));
+            if (pack_row(s, q, o, l, q_min)) {
+                rc = GSNP_ERR_INPUT;
+                return;
             }
             memset(o + l, 0, (size_t)(pitch - l));
         }

@@ -34,6 +34,23 @@ def test_pack_reads_layout(native_lib):
         assert np.array_equal(got, layout(seq, qual, length, q_min))
 
 
+@pytest.mark.parametrize("q_min", [-127, -5, 0, 33, 64, 65, 100, 127])
+def test_pack_reads_every_byte_pair(q_min, native_lib):
+    """every (base byte, quality byte) pair: the valid ones packed as the
+    layout says, a sample of the others refused one read at a time"""
+    b = np.repeat(np.arange(256, dtype=np.uint8), 256).reshape(-1, 1)
+    q = np.tile(np.arange(256, dtype=np.uint8), 256).reshape(-1, 1)
+    ones = np.ones(len(b), dtype=np.int32)
+    qq = q[:, 0].view(np.int8).astype(int) - q_min
+    good = np.isin(b[:, 0], np.frombuffer(b"ACGTacgt", dtype=np.uint8)) & (qq <= 62)
+    got = api.pack_reads(b[good], q[good], ones[good], q_min)
+    want = [(CODE[int(x)] << 6) | (63 if y < 0 else y) for x, y in zip(b[good, 0], qq[good])]
+    assert np.array_equal(got[:, 0], np.array(want, dtype=np.uint8))
+    for i in np.flatnonzero(~good)[::97]:
+        with pytest.raises(RuntimeError):
+            api.pack_reads(b[i:i + 1], q[i:i + 1], ones[i:i + 1], q_min)
+
+
 def test_pack_reads_refusals(native_lib):
     seq = np.frombuffer(b"ACGN", dtype=np.uint8).reshape(1, 4).copy()
     qual = np.full((1, 4), 70, dtype=np.uint8)
