@@ -801,27 +801,54 @@ __device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_l
     return p;
 }
 
-/* Ascending bitonic sort of v[0, n), n <= kDeepCap, by the lanes of a warp in
- * shared memory (padded to a power of two with 0xFFFFFFFF, which no record
- * word equals). */
+/* Ascending bitonic sort of v[0, n), n <= kDeepCap = 256, by the lanes of a
+ * warp in registers: lane l holds elements 8l .. 8l+7 (padded with
+ * 0xFFFFFFFF, which no record word equals).  The network's stages of
+ * distance j < 8 are compare-exchanges within a lane; those of distance
+ * j >= 8 pair lane l with lane l ^ (j / 8), which keeps the smaller or the
+ * larger of each of its eight elements.  Every loop bound is a constant, so
+ * the 36 stages unroll into straight code with no index arithmetic and no
+ * shared-memory traffic between them. */
 __device__ __forceinline__ void deep_sort(uint32_t* v, int n) {
+    static_assert(kDeepCap == 256, "eight elements a lane");
     const int lane = threadIdx.x & 31;
-    int P = 32;
-    while (P < n) P <<= 1;
-    for (int i = n + lane; i < P; i += 32) v[i] = 0xFFFFFFFFu;
-    __syncwarp();
-    for (int k = 2; k <= P; k <<= 1)
+    uint32_t x[8];
+    const uint4 lo4 = reinterpret_cast<const uint4*>(v)[lane * 2];
+    const uint4 hi4 = reinterpret_cast<const uint4*>(v)[lane * 2 + 1];
+    x[0] = lo4.x, x[1] = lo4.y, x[2] = lo4.z, x[3] = lo4.w;
+    x[4] = hi4.x, x[5] = hi4.y, x[6] = hi4.z, x[7] = hi4.w;
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        if (lane * 8 + e >= n) x[e] = 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 2; k <= 256; k <<= 1) {
+#pragma unroll
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int t = lane; t < P / 2; t += 32) {
-                const int i = 2 * j * (t / j) + (t % j), l = i + j;
-                const uint32_t x = v[i], y = v[l];
-                if ((x > y) == ((i & k) == 0)) {
-                    v[i] = y;
-                    v[l] = x;
+            if (j >= 8) {
+                const int d = j >> 3;
+                const bool keep_min = (((lane * 8) & k) == 0) == ((lane & d) == 0);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const uint32_t y = __shfl_xor_sync(kFull, x[e], d);
+                    x[e] = keep_min ? min(x[e], y) : max(x[e], y);
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    if (e & j) continue;
+                    const int f = e | j;
+                    const bool asc = ((lane * 8 + e) & k) == 0;
+                    const uint32_t a = min(x[e], x[f]), b = max(x[e], x[f]);
+                    x[e] = asc ? a : b;
+                    x[f] = asc ? b : a;
                 }
             }
-            __syncwarp();
         }
+    }
+    __syncwarp();
+    reinterpret_cast<uint4*>(v)[lane * 2] = make_uint4(x[0], x[1], x[2], x[3]);
+    reinterpret_cast<uint4*>(v)[lane * 2 + 1] = make_uint4(x[4], x[5], x[6], x[7]);
+    __syncwarp();
 }
 
 /* The dependency walk and the FP32 sums of a sorted column by its warp,
