@@ -734,7 +734,17 @@ constexpr size_t kDeepSmem = (size_t)kTile * (kDeepCap * 4 + kDeepKeys);
  * the 32 reads of a step are decided together with the reference's result.
  * Once the cap is reached a read can only add to depth and repeat, which
  * need no base or quality; the scan ends at the first step whose reads all
- * start past the site. */
+ * start past the site.
+ *
+ * The scan is bound by load latency (each step's base and quality load
+ * depends on the read's start), so its loads run ahead of the decisions: an
+ * iteration loads the starts and lengths of its kDeepAhead steps' reads in
+ * the iteration before, and their bases, qualities and strands all at its
+ * start (for every covering read, when the site was below the cap as the
+ * iteration began; a step that finds the site capped leaves its loads
+ * unused).  The steps are then decided in order, as above. */
+constexpr int kDeepAhead = 2;
+
 __device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_lo, int64_t r_hi, int64_t site,
                                                   uint32_t* recs) {
     const int lane = threadIdx.x & 31;
@@ -752,51 +762,74 @@ __device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_l
     p.repeat = 0;
     p.dep_uni = 0;
     p.num = 0;
-    for (int64_t rb = r_lo; rb < r_hi; rb += 32) {
-        const int64_t r = rb + lane;
-        bool cov = false;
-        uint32_t lh = 0, bq = 0;
-        int coord = -1, minus = 0;
-        const bool capped = p.dep_uni >= 0xFF;
-        if (r < r_hi) {
-            const int32_t start = __ldg(a.pos + r);
-            lh = (uint32_t)__ldg(a.lenhit + r);
-            coord = (int)(site - start);
-            cov = coord >= 0 && coord < (int)(lh >> 16);
-            if (cov && !capped) {
-                bq = __ldg(a.bq + r * L + coord);
-                minus = __ldg(a.strand + r) != '+';
+    int32_t nst[kDeepAhead];
+    uint32_t nlh[kDeepAhead];
+#pragma unroll
+    for (int u = 0; u < kDeepAhead; ++u) {
+        const int64_t r = r_lo + 32 * u + lane;
+        nst[u] = r < r_hi ? __ldg(a.pos + r) : 0;
+        nlh[u] = r < r_hi ? (uint32_t)__ldg(a.lenhit + r) : 0u;
+    }
+    for (int64_t rb = r_lo; rb < r_hi; rb += 32 * kDeepAhead) {
+        int coord[kDeepAhead];
+        uint32_t lh[kDeepAhead], bq[kDeepAhead];
+        bool cov[kDeepAhead], minus[kDeepAhead];
+        const bool capped_at_start = p.dep_uni >= 0xFF;
+#pragma unroll
+        for (int u = 0; u < kDeepAhead; ++u) {
+            const int64_t r = rb + 32 * u + lane;
+            const bool in = r < r_hi;
+            coord[u] = in ? (int)(site - nst[u]) : -1;
+            lh[u] = nlh[u];
+            cov[u] = in && coord[u] >= 0 && coord[u] < (int)(lh[u] >> 16);
+            bq[u] = 0;
+            minus[u] = false;
+            if (cov[u] && !capped_at_start) {
+                bq[u] = __ldg(a.bq + r * L + coord[u]);
+                minus[u] = __ldg(a.strand + r) != '+';
+            }
+            const int64_t rn = r + 32 * kDeepAhead;
+            nst[u] = rn < r_hi ? __ldg(a.pos + rn) : 0;
+            nlh[u] = rn < r_hi ? (uint32_t)__ldg(a.lenhit + rn) : 0u;
+        }
+        bool past = false;
+#pragma unroll
+        for (int u = 0; u < kDeepAhead; ++u) {
+            if (__all_sync(kFull, coord[u] < 0)) {   /* every read from here on starts past the site */
+                past = true;
+                break;
+            }
+            const unsigned mc = __ballot_sync(kFull, cov[u]);
+            if (mc == 0) continue;
+            const uint32_t hit = lh[u] & 0xffffu;
+            p.depth += (uint32_t)__popc(mc);
+            p.repeat += __reduce_add_sync(kFull, cov[u] ? hit : 0u);
+            if (p.dep_uni >= 0xFF) continue;
+            const signed char base = (signed char)(bq[u] & 0xff);
+            const signed char qual = (signed char)(bq[u] >> 8);
+            const bool valid = cov[u] && base != 'N' && qual >= qmin;
+            const bool uni = valid && hit == 1;
+            const int uni_before = p.dep_uni + __popc(__ballot_sync(kFull, uni) & lt);
+            const bool acc = valid && uni_before < 0xFF;
+            const bool rec = acc && uni;
+            const unsigned mr = __ballot_sync(kFull, rec);
+            const int q = qual - qmin;
+            if (rec) {
+                const uint32_t cv =
+                    minus[u] ? (uint32_t)((int)(lh[u] >> 16) - 1 - coord[u]) : (uint32_t)coord[u];
+                recs[p.num + __popc(mr & lt)] = make_record(base, q, cv, (uint32_t)minus[u]);
+            }
+            p.num += __popc(mr);
+            p.dep_uni += __popc(mr);
+            const int bi = (base >> 1) & 3;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                p.cu[b] += __popc(__ballot_sync(kFull, rec && bi == b));
+                p.qs[b] += (int)__reduce_add_sync(kFull, (rec && bi == b) ? (uint32_t)q : 0u);
+                p.ca[b] += (uint32_t)__popc(__ballot_sync(kFull, acc && bi == b));
             }
         }
-        if (__all_sync(kFull, coord < 0)) break;   /* every read from here on starts past the site */
-        const unsigned mc = __ballot_sync(kFull, cov);
-        if (mc == 0) continue;
-        const uint32_t hit = lh & 0xffffu;
-        p.depth += (uint32_t)__popc(mc);
-        p.repeat += __reduce_add_sync(kFull, cov ? hit : 0u);
-        if (capped) continue;
-        const signed char base = (signed char)(bq & 0xff);
-        const signed char qual = (signed char)(bq >> 8);
-        const bool valid = cov && base != 'N' && qual >= qmin;
-        const bool uni = valid && hit == 1;
-        const int uni_before = p.dep_uni + __popc(__ballot_sync(kFull, uni) & lt);
-        const bool acc = valid && uni_before < 0xFF;
-        const bool rec = acc && uni;
-        const unsigned mr = __ballot_sync(kFull, rec);
-        const int q = qual - qmin;
-        if (rec) {
-            const uint32_t cv = minus ? (uint32_t)((int)(lh >> 16) - 1 - coord) : (uint32_t)coord;
-            recs[p.num + __popc(mr & lt)] = make_record(base, q, cv, (uint32_t)minus);
-        }
-        p.num += __popc(mr);
-        p.dep_uni += __popc(mr);
-        const int bi = (base >> 1) & 3;
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            p.cu[b] += __popc(__ballot_sync(kFull, rec && bi == b));
-            p.qs[b] += (int)__reduce_add_sync(kFull, (rec && bi == b) ? (uint32_t)q : 0u);
-            p.ca[b] += (uint32_t)__popc(__ballot_sync(kFull, acc && bi == b));
-        }
+        if (past) break;
     }
     return p;
 }
