@@ -762,6 +762,9 @@ __device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_l
     p.repeat = 0;
     p.dep_uni = 0;
     p.num = 0;
+    /* repeat and the quality sums per lane, added over the warp after the
+     * scan (the same sums, modulo 2^32 as before) */
+    uint32_t rep_l = 0, qs_l[4] = {0u, 0u, 0u, 0u};
     int32_t nst[kDeepAhead];
     uint32_t nlh[kDeepAhead];
 #pragma unroll
@@ -803,7 +806,7 @@ __device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_l
             if (mc == 0) continue;
             const uint32_t hit = lh[u] & 0xffffu;
             p.depth += (uint32_t)__popc(mc);
-            p.repeat += __reduce_add_sync(kFull, cov[u] ? hit : 0u);
+            rep_l += cov[u] ? hit : 0u;
             if (p.dep_uni >= 0xFF) continue;
             const signed char base = (signed char)(bq[u] & 0xff);
             const signed char qual = (signed char)(bq[u] >> 8);
@@ -825,12 +828,15 @@ __device__ __forceinline__ SitePileup deep_pileup(const CallArgs& a, int64_t r_l
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 p.cu[b] += __popc(__ballot_sync(kFull, rec && bi == b));
-                p.qs[b] += (int)__reduce_add_sync(kFull, (rec && bi == b) ? (uint32_t)q : 0u);
+                qs_l[b] += (rec && bi == b) ? (uint32_t)q : 0u;
                 p.ca[b] += (uint32_t)__popc(__ballot_sync(kFull, acc && bi == b));
             }
         }
         if (past) break;
     }
+    p.repeat = __reduce_add_sync(kFull, rep_l);
+#pragma unroll
+    for (int b = 0; b < 4; ++b) p.qs[b] = (int)__reduce_add_sync(kFull, qs_l[b]);
     return p;
 }
 
@@ -942,10 +948,11 @@ __device__ __forceinline__ void deep_walk_sums(const CallArgs& a, const uint32_t
     }
 }
 
-/* One deep tile: warp w calls site w (as fast_site: counts kept for later
- * gap windows, the FP32 posterior, or the site deferred with its records). */
-__device__ __forceinline__ void deep_tile(const CallArgs& a, int64_t tile, uint32_t* recs, uint8_t* cnt) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+/* Site w of a deep tile, called by one warp (as fast_site: counts kept for
+ * later gap windows, the FP32 posterior, or the site deferred with its
+ * records). */
+__device__ __forceinline__ void deep_tile(const CallArgs& a, int64_t tile, int w, uint32_t* recs, uint8_t* cnt) {
+    const int lane = threadIdx.x & 31;
     const int64_t s0 = tile * kTile, site = s0 + w;
     const int64_t sl = s0 + lane;
     const uint8_t ori_l = sl < a.chr_len ? __ldg(a.ori + sl) : 0;
@@ -1014,28 +1021,27 @@ __device__ __forceinline__ void deep_tile(const CallArgs& a, int64_t tile, uint3
     }
 }
 
-/* The tiles of a deep FP32 bin: tiles[blockIdx.x] with count == nullptr, else
- * the first *count tiles of the list handed out from *next (zero before the
- * launch), one tile per CTA at a time. */
+/* The tiles of a deep FP32 bin: tiles[blockIdx.x] with count == nullptr, warp
+ * w calling its site w; else the sites of the first *count tiles of the list,
+ * handed out one at a time to each warp from *next (zero before the launch),
+ * so that no warp waits for the deepest site of a tile. */
 __global__ void __launch_bounds__(kDeepThreads, 1) call_deep_kernel(CallArgs a, const int32_t* __restrict__ tiles,
                                                                     const int* __restrict__ count, int* next) {
     extern __shared__ __align__(16) uint8_t smem[];
-    const int w = threadIdx.x >> 5;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t* recs = reinterpret_cast<uint32_t*>(smem) + (size_t)w * kDeepCap;
     uint8_t* cnt = smem + (size_t)kTile * kDeepCap * 4 + (size_t)w * kDeepKeys;
-    __shared__ int s_next;
     if (!count) {
-        deep_tile(a, tiles[blockIdx.x], recs, cnt);
+        deep_tile(a, tiles[blockIdx.x], w, recs, cnt);
         return;
     }
-    const int n = *count;
-    int i = blockIdx.x;
-    while (i < n) {
-        deep_tile(a, tiles[i], recs, cnt);
-        __syncthreads();
-        if (threadIdx.x == 0) s_next = atomicAdd(next, 1) + (int)gridDim.x;
-        __syncthreads();
-        i = s_next;
+    const unsigned items = (unsigned)*count * kTile;   /* tile-list index * kTile + site */
+    unsigned item = blockIdx.x * kTile + w;
+    while (item < items) {
+        deep_tile(a, tiles[item / kTile], (int)(item % kTile), recs, cnt);
+        unsigned nx = 0;
+        if (lane == 0) nx = (unsigned)atomicAdd(next, 1) + gridDim.x * kTile;
+        item = __shfl_sync(kFull, nx, 0);
     }
 }
 
