@@ -171,6 +171,33 @@ static Case make_case(int windows, int64_t n, int kind) {
     return c;
 }
 
+/* the case's reads as packed bytes (gsnp_pack_reads's layout); an N is
+ * written as the skip code 63, which the replay takes as it takes an N:
+ * neither base counts as a record */
+static std::vector<uint8_t> pack_case(const Case& c) {
+    std::vector<uint8_t> out(c.seq.size(), 0);
+    for (size_t i = 0; i < c.pos.size(); ++i)
+        for (int k = 0; k < c.pitch && k < c.len[i]; ++k) {
+            const size_t at = i * (size_t)c.pitch + (size_t)k;
+            const uint8_t b = c.seq[at];
+            const int q = (int)(signed char)c.qual[at] - c.qmin;
+            out[at] = (b == 'N' || q < 0) ? (uint8_t)63 : (uint8_t)((((b >> 1) & 3) << 6) | q);
+        }
+    return out;
+}
+
+static bool same_plan(const WindowPlan& a, const WindowPlan& b) {
+    if (a.n_windows != b.n_windows || a.call_len != b.call_len || a.host_src != b.host_src ||
+        a.lik_src != b.lik_src || a.flags != b.flags || a.n_valid != b.n_valid || a.n_deposited != b.n_deposited ||
+        a.skipped != b.skipped || a.dropped_last != b.dropped_last || a.runs.size() != b.runs.size())
+        return false;
+    for (size_t k = 0; k < a.runs.size(); ++k)
+        if (a.runs[k].first != b.runs[k].first || a.runs[k].count != b.runs[k].count ||
+            a.runs[k].window != b.runs[k].window)
+            return false;
+    return true;
+}
+
 static int cases = 0;
 static bool compare(const Case& c, int threads, const char* what) {
     ++cases;
@@ -185,6 +212,17 @@ static bool compare(const Case& c, int threads, const char* what) {
         return false;
     };
     if (rc != want.rc || err != want.err) return fail("return code");
+    /* the same reads packed: the same plan, or the same error */
+    const std::vector<uint8_t> pk = pack_case(c);
+    ReadView pv = v;
+    pv.seq = nullptr;
+    pv.qual = nullptr;
+    pv.packed = pk.data();
+    WindowPlan got_packed;
+    std::string err_packed;
+    const int rc_packed = replay_windows(pv, c.chr_len, c.L, c.qmin, threads, &got_packed, &err_packed);
+    if (rc_packed != rc || err_packed != err) return fail("packed reads: return code");
+    if (rc == 0 && !same_plan(got, got_packed)) return fail("packed reads: plan");
     if (rc != 0) return true;
     if (got.call_len != want.call_len) return fail("call_len");
     if (got.host_src != want.host_src) return fail("host_src");
